@@ -1,0 +1,211 @@
+/*
+ * sph_gb300.h -- C ABI of libsph_gb300.so, the GB300 (sm_103a) implementation
+ * of the opencl-sph per-substep particle pipeline.
+ *
+ * Every declaration below either replaces one function of the reference's
+ * libSPH.so (its header and line are cited beside it) or is an addition
+ * marked NEW.  Types and struct layouts are those of the reference, so the
+ * reference's ctypes bindings (scripts/sph/bindings.py) and its Python
+ * driver code can load this library unchanged; the `_opencl` names are kept
+ * as aliases of the `_cuda` ones.  No torch or CUDA type appears here: the
+ * device side is reached only through the opaque handle below.
+ *
+ * Error behaviour follows the reference: void functions that fail record a
+ * message (sph_last_error) and, unless sph_set_abort_on_error(0) was called,
+ * abort the process as the reference's ASSERT/HANDLE_CL_ERROR do; int
+ * functions return non-zero.  Kernel launches are asynchronous on the
+ * handle's CUDA stream; every sync_* call, sph_synchronize and the
+ * free/terminate calls wait for the stream, so host views of the psdata
+ * blob are current after a device-to-host sync exactly as in the reference.
+ */
+#ifndef SPH_GB300_H_
+#define SPH_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- store types ---------------------------------------------------------- */
+
+/* src/datatypes.h:7-14 */
+typedef enum { T_CHAR, T_UINT, T_INT, T_FLOAT32, T_FLOAT64, TYPE_COUNT } FieldType;
+
+/* src/datatypes.h:16-26 */
+typedef struct {
+    FieldType type;
+    union {
+        char *c;
+        uint32_t *u;
+        int32_t *i;
+        float *f4;
+        double *f8;
+        void *ptr;
+    };
+} DataPtr;
+
+/* src/particle_system.h:18-48: a flat, self-describing particle store.
+ * Field f occupies data_sizes[f] bytes at data + data_offsets[f]; its shape
+ * is dimensions[dimensions_offsets[f] .. + num_dimensions[f]] (first
+ * dimension fastest). */
+typedef struct {
+    unsigned int num_fields;
+    const char *names;
+    unsigned int *names_offsets;
+    unsigned int *dimensions;
+    unsigned int *num_dimensions;
+    unsigned int *dimensions_offsets;
+    unsigned int *entry_sizes;
+
+    void *data;
+    unsigned int *data_sizes;
+    unsigned int *data_offsets;
+
+    DataPtr *data_ptrs;
+
+    unsigned int num_host_fields;
+    char **host_names;
+    void **host_data;
+    unsigned int *host_data_size;
+} psdata;
+
+/* src/opencl/particle_system_host.h:7-47, same member layout.  Each cl_mem
+ * slot holds a CUDA device pointer (or NULL), the kernel slots are unused,
+ * and ps_prog holds the opaque per-store device state (stream, resolved
+ * field table, material pipeline, scratch, CUDA graph).  The struct is
+ * passed by value, like the reference's; copies share the device state. */
+typedef struct {
+    psdata host_psdata;
+
+    unsigned int num_fields;
+    void *names;
+    void *names_offsets;
+    void *dimensions;
+    void *num_dimensions;
+    void *dimensions_offsets;
+    void *field_types;
+    void *entry_sizes;
+
+    void *data;              /* device copy of the whole psdata blob */
+    void *data_sizes;
+    void *data_offsets;
+
+    void *block_totals;      /* device scratch: scan partial sums */
+    void *backup_prefix_sum; /* device scratch: per-particle slot in its cell */
+
+    size_t num_kernels;
+    const char *const *kernel_names;
+    const void *kernels;
+
+    void *ps_prog;           /* opaque device state */
+
+    unsigned int num_grid_cells;
+    size_t po2_workgroup_size;
+    unsigned int num_blocks;
+} psdata_cuda;
+
+typedef psdata_cuda psdata_opencl;
+
+/* ---- host store: src/build_psdata.h, src/particle_system.h --------------- */
+
+void build_psdata_from_string(psdata *data, const char *string);   /* build_psdata.h:6 */
+void build_psdata(psdata *data, const char *path);                  /* build_psdata.h:7 */
+void display_psdata(psdata data, const char *const *mask);          /* particle_system.h:56 */
+int get_field_psdata(psdata data, const char *name);                /* particle_system.h:61 */
+void set_field_psdata(psdata *data, const char *name, void *field,  /* particle_system.h:62 */
+                      unsigned int size, unsigned int offset);
+unsigned int psdata_names_size(psdata data);                        /* particle_system.h:64 */
+unsigned int psdata_dimensions_size(psdata data);                   /* particle_system.h:65 */
+unsigned int psdata_data_size(psdata data);                         /* particle_system.h:66 */
+int create_host_field_psdata(psdata *data, const char *name,        /* particle_system.h:68 */
+                             void *field, unsigned int size);
+int get_host_field_psdata(psdata *data, const char *name);          /* particle_system.h:69 */
+void free_psdata(psdata *data);                                     /* particle_system.h:77 */
+
+/* ---- config and logging: src/config.h, src/note.h ------------------------ */
+
+int load_config(const char *relative_path);                         /* config.h:4 */
+const char *get_config_section(const char *heading);                /* config.h:5 */
+void unload_config(void);                                           /* config.h:6 */
+void set_log_level(unsigned int loglevel);                          /* note.h:4 */
+void note(unsigned int level, const char *fmt, ...);                /* note.h:5 */
+
+/* ---- device driver: src/opencl/particle_system_host.h -------------------- */
+
+void init_cuda(void);                                               /* :55 init_opencl */
+void terminate_cuda(void);                                          /* :60 terminate_opencl */
+psdata_cuda create_psdata_cuda(psdata *data, const char *file_list);/* :56 create_psdata_opencl */
+void free_psdata_cuda(psdata_cuda *pso);                            /* :59 free_psdata_opencl */
+
+void sync_psdata_device_to_host(psdata data, psdata_cuda pso);      /* :62 */
+void sync_psdata_fields_device_to_host(psdata data, psdata_cuda pso,/* :63 */
+                                       size_t num_fields, const char *const *field_names);
+void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int full);              /* :64 */
+void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso,/* :65 */
+                                       size_t num_fields, const char *const *field_names);
+
+void populate_position_cuboid_device_cuda(psdata_cuda pso,          /* :67-72 */
+                                          float x1, float y1, float z1,
+                                          float x2, float y2, float z2,
+                                          unsigned int xsize, unsigned int ysize,
+                                          unsigned int zsize);
+void rotate_particles_device_cuda(psdata_cuda pso, float angle_x,   /* :73 */
+                                  float angle_y, float angle_z);
+void call_for_all_particles_device_cuda(psdata_cuda pso,            /* :74 */
+                                        const char *kernel_name);
+void compute_particle_bins_device_cuda(psdata_cuda pso);            /* :76 */
+void compute_density_device_cuda(psdata_cuda pso);                  /* :78 */
+void compute_forces_device_cuda(psdata_cuda pso);                   /* :79 */
+void step_forward_device_cuda(psdata_cuda pso);                     /* :80 */
+/* particle_system_host.c:562-588 (defined but not declared there) */
+void set_body_position_device_cuda(psdata_cuda pso, unsigned int body, float *position);
+void set_body_rotation_device_cuda(psdata_cuda pso, unsigned int body, float *euler_angles);
+
+/* the reference's own names, aliases of the above */
+void init_opencl(void);
+void terminate_opencl(void);
+psdata_opencl create_psdata_opencl(psdata *data, const char *file_list);
+void free_psdata_opencl(psdata_opencl *pso);
+void populate_position_cuboid_device_opencl(psdata_opencl pso, float x1, float y1, float z1,
+                                            float x2, float y2, float z2, unsigned int xsize,
+                                            unsigned int ysize, unsigned int zsize);
+void rotate_particles_device_opencl(psdata_opencl pso, float angle_x, float angle_y, float angle_z);
+void call_for_all_particles_device_opencl(psdata_opencl pso, const char *kernel_name);
+void compute_particle_bins_device_opencl(psdata_opencl pso);
+void compute_density_device_opencl(psdata_opencl pso);
+void compute_forces_device_opencl(psdata_opencl pso);
+void step_forward_device_opencl(psdata_opencl pso);
+void set_body_position_device_opencl(psdata_opencl pso, unsigned int body, float *position);
+void set_body_rotation_device_opencl(psdata_opencl pso, unsigned int body, float *euler_angles);
+
+/* ---- NEW: errors, streams, whole substeps -------------------------------- */
+
+/* Message of the last failure in this process ("" if none). */
+const char *sph_last_error(void);
+void sph_clear_error(void);
+/* 1 (default, the reference's behaviour): a failing void call aborts.
+ * 0: it records the error and returns. */
+void sph_set_abort_on_error(int abort_on_error);
+/* Waits for the store's stream; returns 0 or a non-zero CUDA error. */
+int sph_synchronize(psdata_cuda pso);
+/* Runs `num_steps` substeps of the store's material recipe (the sequence a
+ * reference driver issues through call_for_all_particles:
+ * scripts/sph/systems.py:194-204 for corotational solids, :225-235 for SVK,
+ * src/mex/simstep_fluid.c:18-23 for fluids), as one CUDA graph per substep
+ * captured on first use.  Returns 0 or non-zero on failure. */
+int sph_update(psdata_cuda pso, unsigned int num_steps);
+/* Device status word accumulated since the last sph_clear_status():
+ * bit 0 = a NaN/Inf position was written, bit 1 = a particle was binned
+ * outside the grid bounds (and clamped into an edge cell). */
+unsigned int sph_status(psdata_cuda pso);
+void sph_clear_status(psdata_cuda pso);
+/* Library and device description (static string). */
+const char *sph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

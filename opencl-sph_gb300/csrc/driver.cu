@@ -1,0 +1,557 @@
+// driver.cu -- the drop-in device driver of libsph_gb300.so: the C ABI of
+// src/opencl/particle_system_host.h re-implemented on CUDA streams, with
+// the psdata blob mirrored as one device allocation and the reference's
+// kernel names dispatched to the sm_103a kernels (launch.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "launch.h"
+#include "sph_gb300.h"
+#include "sph_internal.h"
+#include "store.h"
+
+// ---------------------------------------------------------------------------
+// errors
+
+namespace {
+std::mutex g_err_mu;
+std::string g_error;
+int g_abort_on_error = 1;
+}  // namespace
+
+void sph_set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_error = buf;
+}
+
+void sph_fail() {
+    if (!g_abort_on_error) return;
+    std::string msg;
+    {
+        std::lock_guard<std::mutex> lk(g_err_mu);
+        msg = g_error;
+    }
+    fprintf(stderr, "sph: %s\n", msg.c_str());
+    abort();
+}
+
+extern "C" const char *sph_last_error(void) {
+    static thread_local std::string copy;
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    copy = g_error;
+    return copy.c_str();
+}
+extern "C" void sph_clear_error(void) {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_error.clear();
+}
+extern "C" void sph_set_abort_on_error(int a) { g_abort_on_error = a; }
+
+extern "C" const char *sph_version(void) {
+    return "sph_gb300 1.0 (sm_103a; opencl-sph psdata ABI; FP32 pipeline, FP64 polar decomposition)";
+}
+
+// ---------------------------------------------------------------------------
+// the per-store device state behind psdata_cuda.ps_prog
+
+namespace {
+
+struct Store {
+    psdata host;                 // the host struct this store mirrors
+    unsigned programs = 0;
+    int material = -1;
+    cudaStream_t stream = nullptr;
+    Arena arena;                 // blob + scratch + tables
+    char *d_blob = nullptr;
+    size_t blob_size = 0;
+    SceneDesc desc{};
+    SceneDesc *d_desc = nullptr;
+    Launch L{};
+    cudaGraphExec_t step_graph = nullptr;
+};
+
+std::mutex g_stores_mu;
+std::set<Store *> g_stores;
+
+bool cuda_ok(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    sph_set_error("%s: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+Store *store_of(const psdata_cuda &pso, const char *what) {
+    Store *s = static_cast<Store *>(pso.ps_prog);
+    std::lock_guard<std::mutex> lk(g_stores_mu);
+    if (!s || !g_stores.count(s)) {
+        sph_set_error("%s: not a live device store (created by create_psdata_cuda and not freed)", what);
+        return nullptr;
+    }
+    return s;
+}
+
+void destroy(Store *s) {
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
+    if (s->arena.base) cudaFree(s->arena.base);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+// Builds the device mirror of a host store.
+Store *create_store(psdata *data, const char *file_list, std::string *err) {
+    unsigned programs = sph_parse_programs(file_list, err);
+    if (!programs) return nullptr;
+    SceneDesc probe;
+    if (!sph_resolve_scene(*data, nullptr, programs, &probe, err)) return nullptr;
+
+    Store *s = new Store();
+    s->host = *data;
+    s->programs = programs;
+    s->material = sph_material_of(programs);
+    s->blob_size = psdata_data_size(*data);
+
+    const unsigned block = 256, pair_block = 128;
+    std::vector<SceneDesc> descs(1, probe);
+    HostMaps maps;
+    sph_build_maps(descs, {0u}, block, pair_block, &maps);
+
+    size_t o_blob = 0;
+    size_t o_scratch = o_blob + Arena::align(s->blob_size);
+    size_t o_desc = o_scratch + Arena::align(sph_scratch_bytes(probe));
+    size_t o_pm = o_desc + Arena::align(sizeof(SceneDesc));
+    size_t o_ppm = o_pm + Arena::align(maps.particles.size() * sizeof(BlockWork));
+    size_t o_cm = o_ppm + Arena::align(maps.pair_particles.size() * sizeof(BlockWork));
+    size_t o_sm = o_cm + Arena::align(maps.cells.size() * sizeof(BlockWork));
+    size_t total = o_sm + Arena::align(maps.scan.size() * sizeof(BlockWork));
+
+    if (!cuda_ok(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+        !cuda_ok(cudaMalloc(&s->arena.base, total), "cudaMalloc(store)")) {
+        *err = sph_last_error();
+        destroy(s);
+        return nullptr;
+    }
+    s->arena.size = total;
+    char *b = s->arena.base;
+    s->d_blob = b + o_blob;
+    std::string e2;
+    sph_resolve_scene(*data, s->d_blob, programs, &s->desc, &e2);
+    sph_place_scratch(&s->desc, b + o_scratch);
+    s->d_desc = reinterpret_cast<SceneDesc *>(b + o_desc);
+    auto up = [&](size_t off, const void *src, size_t bytes) {
+        return bytes == 0 || cuda_ok(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, s->stream),
+                                     "cudaMemcpy(store)");
+    };
+    bool ok = up(o_blob, data->data, s->blob_size) && up(o_desc, &s->desc, sizeof(SceneDesc)) &&
+              up(o_pm, maps.particles.data(), maps.particles.size() * sizeof(BlockWork)) &&
+              up(o_ppm, maps.pair_particles.data(), maps.pair_particles.size() * sizeof(BlockWork)) &&
+              up(o_cm, maps.cells.data(), maps.cells.size() * sizeof(BlockWork)) &&
+              up(o_sm, maps.scan.data(), maps.scan.size() * sizeof(BlockWork)) &&
+              cuda_ok(cudaMemsetAsync(s->desc.status, 0, 4, s->stream), "cudaMemset(status)") &&
+              cuda_ok(cudaStreamSynchronize(s->stream), "create_psdata_cuda");
+    if (!ok) {
+        *err = sph_last_error();
+        destroy(s);
+        return nullptr;
+    }
+    Launch &L = s->L;
+    L.scenes = s->d_desc;
+    L.num_scenes = 1;
+    L.particles = {reinterpret_cast<BlockWork *>(b + o_pm), (unsigned)maps.particles.size()};
+    L.pair_particles = {reinterpret_cast<BlockWork *>(b + o_ppm), (unsigned)maps.pair_particles.size()};
+    L.cells = {reinterpret_cast<BlockWork *>(b + o_cm), (unsigned)maps.cells.size()};
+    L.scan = {reinterpret_cast<BlockWork *>(b + o_sm), (unsigned)maps.scan.size()};
+    L.block = block;
+    L.pair_block = pair_block;
+    L.grid_cap = 1u << 30;
+    L.stream = s->stream;
+    {
+        std::lock_guard<std::mutex> lk(g_stores_mu);
+        g_stores.insert(s);
+    }
+    return s;
+}
+
+// After enqueueing work: report launch errors (and, in the synchronous
+// mode the reference's clFinish implies, execution errors).
+bool finish(Store *s, const char *what, bool sync) {
+    if (sph_check_launch(what) != cudaSuccess) return false;
+    if (sync && !cuda_ok(cudaStreamSynchronize(s->stream), what)) return false;
+    return true;
+}
+
+const char *kNeedsArgs[] = {"populate_position_cuboid", "rotate_particles", "set_body_position",
+                            "set_body_rotation"};
+
+// call_for_all_particles_device_opencl (particle_system_host.c:517-528):
+// the reference's kernel names mapped onto launch sequences.  Pair kernels
+// first refresh the cell-sorted copies from the current fields, so a named
+// call sees exactly the fields the reference's kernel would read.
+bool dispatch(Store *s, const char *name) {
+    const Launch &L = s->L;
+    const unsigned P = s->programs;
+    auto need = [&](unsigned bits, const char *file) {
+        if (P & bits) return true;
+        sph_set_error("kernel '%s' is not in this store's program (needs %s.cl)", name, file);
+        return false;
+    };
+    std::string k = name ? name : "";
+    if (k == "find_particle_bins") { sph_launch_find_bins(L); return true; }
+    if (k == "zero_gridcount") { sph_launch_zero_cells(L); return true; }
+    if (k == "count_particles_in_bins") { sph_launch_count(L); return true; }
+    if (k == "prefix_sum") { sph_launch_scan(L); return true; }
+    // the arrival slots recorded by the count replace the backup cursor
+    if (k == "copy_celloffset_to_backup") return true;
+    if (k == "insert_particles_in_bin_array") { sph_launch_insert(L); return true; }
+    if (k == "compute_density") {
+        sph_launch_gather(L, false, false);
+        sph_launch_density(L, false);
+        return true;
+    }
+    if (k == "step_forward") { sph_launch_step_forward(L); return true; }
+    if (k == "compute_forces_fluids") {
+        if (!need(PROG_FLUIDS, "fluids")) return false;
+        sph_launch_gather(L, true, true);
+        sph_launch_forces_fluids(L, false);
+        return true;
+    }
+    if (k == "init_original_position") {
+        if (!need(PROG_SOLIDS, "solids")) return false;
+        sph_launch_init_original_position(L);
+        return true;
+    }
+    if (k == "compute_original_density") {
+        if (!need(PROG_SOLIDS, "solids")) return false;
+        sph_launch_gather(L, false, false);
+        sph_launch_density(L, true);
+        return true;
+    }
+    if (k == "compute_rotations_and_strains") {
+        if (!need(PROG_COROT, "solid_corotation")) return false;
+        sph_launch_gather(L, false, false);
+        sph_launch_rotations_and_strains(L);
+        return true;
+    }
+    if (k == "compute_deformations") {
+        if (!need(PROG_SVK, "solid_svk")) return false;
+        sph_launch_gather(L, false, false);
+        sph_launch_deformations(L);
+        return true;
+    }
+    if (k == "compute_stresses") {
+        if (!need(PROG_COROT | PROG_SVK, "solid_corotation or solid_svk")) return false;
+        sph_launch_stresses(L, (P & PROG_COROT) != 0);
+        return true;
+    }
+    if (k == "compute_forces_solids") {
+        if (!need(PROG_COROT | PROG_SVK, "solid_corotation or solid_svk")) return false;
+        sph_launch_gather(L, false, false);
+        sph_launch_forces_solids(L, (P & PROG_COROT) != 0);
+        return true;
+    }
+    if (k == "apply_plane_constraints") {
+        if (!need(PROG_CONSTRAINTS, "constraints")) return false;
+        sph_launch_plane_constraints(L);
+        return true;
+    }
+    for (const char *a : kNeedsArgs)
+        if (k == a) {
+            sph_set_error("kernel '%s' takes arguments; call its own entry point", name);
+            return false;
+        }
+    sph_set_error("no kernel named '%s'", name);
+    return false;
+}
+
+template <typename F>
+void with_store(const psdata_cuda &pso, const char *what, bool sync, F &&body) {
+    Store *s = store_of(pso, what);
+    if (!s) { sph_fail(); return; }
+    if (!body(s) || !finish(s, what, sync)) sph_fail();
+}
+
+bool copy_field(Store *s, const psdata &data, const char *name, bool to_device) {
+    int f = get_field_psdata(data, name);
+    if (f < 0) {
+        note(1, "Field %s not found.\n", name);
+        return true;  // the reference logs and skips (particle_system_host.c:819-822)
+    }
+    size_t off = data.data_offsets[f], sz = data.data_sizes[f];
+    if (off + sz > s->blob_size) {
+        sph_set_error("field %s lies outside the device store", name);
+        return false;
+    }
+    char *host = (char *)data.data + off;
+    char *dev = s->d_blob + off;
+    return cuda_ok(to_device ? cudaMemcpyAsync(dev, host, sz, cudaMemcpyHostToDevice, s->stream)
+                             : cudaMemcpyAsync(host, dev, sz, cudaMemcpyDeviceToHost, s->stream),
+                   "field copy");
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// ABI
+
+extern "C" void init_cuda(void) {
+    if (!cuda_ok(cudaFree(nullptr), "init_cuda")) sph_fail();
+}
+extern "C" void terminate_cuda(void) {
+    if (!cuda_ok(cudaDeviceSynchronize(), "terminate_cuda")) sph_fail();
+}
+
+extern "C" psdata_cuda create_psdata_cuda(psdata *data, const char *file_list) {
+    psdata_cuda pso;
+    memset(&pso, 0, sizeof(pso));
+    std::string err;
+    Store *s = data ? create_store(data, file_list, &err) : nullptr;
+    if (!s) {
+        sph_set_error("create_psdata_cuda: %s", data ? err.c_str() : "null store");
+        sph_fail();
+        return pso;
+    }
+    pso.host_psdata = *data;
+    pso.num_fields = data->num_fields;
+    pso.data = s->d_blob;
+    pso.block_totals = s->desc.scan_sums;
+    pso.backup_prefix_sum = s->desc.slot;
+    pso.ps_prog = s;
+    pso.num_grid_cells = s->desc.num_cells;
+    // the reference's work-group bookkeeping (particle_system_host.c:661-674)
+    pso.po2_workgroup_size = 256;
+    pso.num_blocks = (s->desc.num_cells - 1) / 512 + 1;
+    return pso;
+}
+
+extern "C" void free_psdata_cuda(psdata_cuda *pso) {
+    if (!pso) return;
+    Store *s = store_of(*pso, "free_psdata_cuda");
+    if (!s) { sph_fail(); return; }
+    {
+        std::lock_guard<std::mutex> lk(g_stores_mu);
+        g_stores.erase(s);
+    }
+    destroy(s);
+    pso->ps_prog = nullptr;
+    pso->data = nullptr;
+    pso->block_totals = nullptr;
+    pso->backup_prefix_sum = nullptr;
+}
+
+// particle_system_host.c:837-841
+extern "C" void sync_psdata_device_to_host(psdata data, psdata_cuda pso) {
+    with_store(pso, "sync_psdata_device_to_host", true, [&](Store *s) {
+        size_t sz = psdata_data_size(data);
+        if (sz > s->blob_size) {
+            sph_set_error("store layout differs from the device copy");
+            return false;
+        }
+        return cuda_ok(cudaMemcpyAsync(data.data, s->d_blob, sz, cudaMemcpyDeviceToHost, s->stream), "sync");
+    });
+}
+
+// particle_system_host.c:780-809; the layout tables never change on the
+// device (field offsets are resolved once), so `full` has nothing more to
+// upload.
+extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int full) {
+    (void)full;
+    with_store(pso, "sync_psdata_host_to_device", true, [&](Store *s) {
+        size_t sz = psdata_data_size(data);
+        if (sz > s->blob_size) {
+            sph_set_error("store layout differs from the device copy");
+            return false;
+        }
+        return cuda_ok(cudaMemcpyAsync(s->d_blob, data.data, sz, cudaMemcpyHostToDevice, s->stream), "sync");
+    });
+}
+
+// particle_system_host.c:812-829
+extern "C" void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso, size_t num_fields,
+                                                  const char *const *names) {
+    with_store(pso, "sync_psdata_fields_host_to_device", true, [&](Store *s) {
+        for (size_t i = 0; i < num_fields; ++i)
+            if (names[i] && !copy_field(s, data, names[i], true)) return false;
+        return true;
+    });
+}
+
+// particle_system_host.c:843-858
+extern "C" void sync_psdata_fields_device_to_host(psdata data, psdata_cuda pso, size_t num_fields,
+                                                  const char *const *names) {
+    with_store(pso, "sync_psdata_fields_device_to_host", true, [&](Store *s) {
+        for (size_t i = 0; i < num_fields; ++i)
+            if (names[i] && !copy_field(s, data, names[i], false)) return false;
+        return true;
+    });
+}
+
+extern "C" void call_for_all_particles_device_cuda(psdata_cuda pso, const char *kernel_name) {
+    with_store(pso, kernel_name ? kernel_name : "call_for_all_particles", false,
+               [&](Store *s) { return dispatch(s, kernel_name); });
+}
+
+// particle_system_host.c:448-454
+extern "C" void compute_particle_bins_device_cuda(psdata_cuda pso) {
+    with_store(pso, "compute_particle_bins", false, [&](Store *s) {
+        sph_launch_bins(s->L);
+        return true;
+    });
+}
+
+extern "C" void compute_density_device_cuda(psdata_cuda pso) {
+    call_for_all_particles_device_cuda(pso, "compute_density");
+}
+
+// particle_system_host.c:477-495 launches a kernel named "compute_forces",
+// which no reference program defines; here it is the store's force pass.
+extern "C" void compute_forces_device_cuda(psdata_cuda pso) {
+    Store *s = store_of(pso, "compute_forces");
+    if (!s) { sph_fail(); return; }
+    call_for_all_particles_device_cuda(pso, (s->programs & (PROG_COROT | PROG_SVK)) ? "compute_forces_solids"
+                                                                                     : "compute_forces_fluids");
+}
+
+extern "C" void step_forward_device_cuda(psdata_cuda pso) { call_for_all_particles_device_cuda(pso, "step_forward"); }
+
+extern "C" void populate_position_cuboid_device_cuda(psdata_cuda pso, float x1, float y1, float z1, float x2,
+                                                     float y2, float z2, unsigned xs, unsigned ys, unsigned zs) {
+    with_store(pso, "populate_position_cuboid", false, [&](Store *s) {
+        const float c1[3] = {x1, y1, z1}, c2[3] = {x2, y2, z2};
+        const unsigned sz[3] = {xs, ys, zs};
+        if (xs == 0 || ys == 0 || zs == 0) return true;
+        sph_launch_populate_cuboid(s->L, c1, c2, sz);
+        return true;
+    });
+}
+
+extern "C" void rotate_particles_device_cuda(psdata_cuda pso, float ax, float ay, float az) {
+    with_store(pso, "rotate_particles", false, [&](Store *s) {
+        sph_launch_rotate_particles(s->L, ax, ay, az);
+        return true;
+    });
+}
+
+static bool body_ok(Store *s, unsigned body, const char *what) {
+    if (!(s->programs & PROG_RIGIDBODY)) {
+        sph_set_error("%s: the store's program lacks rigidbody.cl", what);
+        return false;
+    }
+    if (body >= s->desc.body_capacity) {
+        sph_set_error("%s: body %u beyond the store's %u bodies", what, body, s->desc.body_capacity);
+        return false;
+    }
+    return true;
+}
+
+// particle_system_host.c:562-574
+extern "C" void set_body_position_device_cuda(psdata_cuda pso, unsigned body, float *position) {
+    with_store(pso, "set_body_position", false, [&](Store *s) {
+        if (!body_ok(s, body, "set_body_position")) return false;
+        sph_launch_set_body_position(s->L, body, position);
+        return true;
+    });
+}
+
+// particle_system_host.c:576-588
+extern "C" void set_body_rotation_device_cuda(psdata_cuda pso, unsigned body, float *euler) {
+    with_store(pso, "set_body_rotation", false, [&](Store *s) {
+        if (!body_ok(s, body, "set_body_rotation")) return false;
+        sph_launch_set_body_rotation(s->L, body, euler);
+        return true;
+    });
+}
+
+extern "C" int sph_synchronize(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_synchronize");
+    if (!s) return -1;
+    cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) sph_set_error("sph_synchronize: %s", cudaGetErrorString(e));
+    return (int)e;
+}
+
+extern "C" int sph_update(psdata_cuda pso, unsigned num_steps) {
+    Store *s = store_of(pso, "sph_update");
+    if (!s) return -1;
+    if (s->material < 0) {
+        sph_set_error("sph_update: the store's program has no substep recipe (needs fluids, "
+                      "solid_corotation or solid_svk)");
+        return -1;
+    }
+    if (!s->step_graph) {
+        cudaGraph_t g = nullptr;
+        if (!cuda_ok(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture")) return -1;
+        sph_launch_substep(s->L, (SphMaterial)s->material);
+        cudaError_t le = cudaGetLastError();
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            sph_set_error("sph_update capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
+            if (g) cudaGraphDestroy(g);
+            return -1;
+        }
+        cudaError_t ie = cudaGraphInstantiate(&s->step_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (!cuda_ok(ie, "cudaGraphInstantiate")) {
+            s->step_graph = nullptr;
+            return -1;
+        }
+    }
+    for (unsigned k = 0; k < num_steps; ++k)
+        if (!cuda_ok(cudaGraphLaunch(s->step_graph, s->stream), "cudaGraphLaunch")) return -1;
+    return 0;
+}
+
+extern "C" unsigned sph_status(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_status");
+    if (!s) return 0xFFFFFFFFu;
+    unsigned v = 0;
+    if (!cuda_ok(cudaMemcpyAsync(&v, s->desc.status, 4, cudaMemcpyDeviceToHost, s->stream), "sph_status") ||
+        !cuda_ok(cudaStreamSynchronize(s->stream), "sph_status"))
+        return 0xFFFFFFFFu;
+    return v;
+}
+
+extern "C" void sph_clear_status(psdata_cuda pso) {
+    with_store(pso, "sph_clear_status", false, [&](Store *s) {
+        return cuda_ok(cudaMemsetAsync(s->desc.status, 0, 4, s->stream), "sph_clear_status");
+    });
+}
+
+// ---- the reference's names -------------------------------------------------
+
+extern "C" void init_opencl(void) { init_cuda(); }
+extern "C" void terminate_opencl(void) { terminate_cuda(); }
+extern "C" psdata_opencl create_psdata_opencl(psdata *data, const char *file_list) {
+    return create_psdata_cuda(data, file_list);
+}
+extern "C" void free_psdata_opencl(psdata_opencl *pso) { free_psdata_cuda(pso); }
+extern "C" void populate_position_cuboid_device_opencl(psdata_opencl pso, float x1, float y1, float z1, float x2,
+                                                       float y2, float z2, unsigned xs, unsigned ys, unsigned zs) {
+    populate_position_cuboid_device_cuda(pso, x1, y1, z1, x2, y2, z2, xs, ys, zs);
+}
+extern "C" void rotate_particles_device_opencl(psdata_opencl pso, float ax, float ay, float az) {
+    rotate_particles_device_cuda(pso, ax, ay, az);
+}
+extern "C" void call_for_all_particles_device_opencl(psdata_opencl pso, const char *kernel_name) {
+    call_for_all_particles_device_cuda(pso, kernel_name);
+}
+extern "C" void compute_particle_bins_device_opencl(psdata_opencl pso) { compute_particle_bins_device_cuda(pso); }
+extern "C" void compute_density_device_opencl(psdata_opencl pso) { compute_density_device_cuda(pso); }
+extern "C" void compute_forces_device_opencl(psdata_opencl pso) { compute_forces_device_cuda(pso); }
+extern "C" void step_forward_device_opencl(psdata_opencl pso) { step_forward_device_cuda(pso); }
+extern "C" void set_body_position_device_opencl(psdata_opencl pso, unsigned body, float *position) {
+    set_body_position_device_cuda(pso, body, position);
+}
+extern "C" void set_body_rotation_device_opencl(psdata_opencl pso, unsigned body, float *euler) {
+    set_body_rotation_device_cuda(pso, body, euler);
+}

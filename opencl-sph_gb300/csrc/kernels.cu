@@ -1,0 +1,153 @@
+// kernels.cu -- the sm_103a kernels of the per-substep particle pipeline
+// and the host functions that enqueue them (see launch.h).
+#include <stdio.h>
+
+#include "kernels_fluid.cuh"
+#include "kernels_grid.cuh"
+#include "kernels_solid.cuh"
+#include "launch.h"
+
+static inline unsigned grid_for(const BlockMap &m, unsigned cap) {
+    unsigned g = m.num < cap ? m.num : cap;
+    return g ? g : 1;
+}
+
+cudaError_t sph_check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) sph_set_error("%s: %s", what, cudaGetErrorString(e));
+    return e;
+}
+
+void sph_launch_find_bins(const Launch &L) {
+    k_bin_count<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, 0);
+}
+
+void sph_launch_zero_cells(const Launch &L) {
+    k_zero_cells<<<grid_for(L.cells, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.cells);
+}
+
+void sph_launch_count(const Launch &L) {
+    k_count_only<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+}
+
+void sph_launch_scan(const Launch &L) {
+    k_scan_tiles<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
+    unsigned g = L.num_scenes < L.grid_cap ? L.num_scenes : L.grid_cap;
+    k_scan_sums<<<g ? g : 1, 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
+    k_scan_add<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
+}
+
+void sph_launch_insert(const Launch &L) {
+    k_scatter<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+    k_sort_cells<<<grid_for(L.cells, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.cells);
+    // crowded cells are rare; a small fixed grid walks the queue
+    k_sort_big_cells<<<32, 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
+}
+
+void sph_launch_bins(const Launch &L) {
+    sph_launch_zero_cells(L);
+    k_bin_count<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, 1);
+    sph_launch_scan(L);
+    sph_launch_insert(L);
+}
+
+void sph_launch_gather(const Launch &L, bool vel, bool dens) {
+    k_gather<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, vel ? 1 : 0,
+                                                                          dens ? 1 : 0);
+}
+
+void sph_launch_density(const Launch &L, bool original) {
+    k_density<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles,
+                                                                                      original ? 1 : 0);
+}
+
+void sph_launch_forces_fluids(const Launch &L, bool fuse_step) {
+    k_forces_fluids<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+        L.scenes, L.pair_particles, fuse_step ? 1 : 0);
+}
+
+void sph_launch_step_forward(const Launch &L) {
+    k_step_forward<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+}
+
+void sph_launch_plane_constraints(const Launch &L) {
+    k_plane_constraints<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+}
+
+void sph_launch_init_original_position(const Launch &L) {
+    k_init_original_position<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+}
+
+void sph_launch_rotations_and_strains(const Launch &L) {
+    k_rotations_and_strains<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+        L.scenes, L.pair_particles);
+}
+
+void sph_launch_stresses(const Launch &L, bool corot) {
+    if (corot)
+        k_stresses_corot<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+    else
+        k_stresses_svk<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+}
+
+void sph_launch_deformations(const Launch &L) {
+    k_deformations<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(L.scenes,
+                                                                                           L.pair_particles);
+}
+
+void sph_launch_forces_solids(const Launch &L, bool corot) {
+    if (corot)
+        k_forces_solids<true><<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+            L.scenes, L.pair_particles);
+    else
+        k_forces_solids<false><<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+            L.scenes, L.pair_particles);
+}
+
+void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]) {
+    float3 p = make_float3(pos[0], pos[1], pos[2]);
+    k_set_body_position<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, body, p);
+    k_store_body_vec<<<1, 32, 0, L.stream>>>(L.scenes, 0, body, p);
+}
+
+void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]) {
+    float3 e = make_float3(euler[0], euler[1], euler[2]);
+    k_set_body_rotation<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, body);
+    k_store_body_vec<<<1, 32, 0, L.stream>>>(L.scenes, 1, body, e);
+}
+
+void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]) {
+    dim3 block(8, 8, 4);
+    dim3 grid((size[0] + 7) / 8, (size[1] + 7) / 8, (size[2] + 3) / 4);
+    k_populate_cuboid<<<grid, block, 0, L.stream>>>(L.scenes, make_float3(c1[0], c1[1], c1[2]),
+                                                    make_float3(c2[0], c2[1], c2[2]), make_uint3(size[0], size[1], size[2]));
+}
+
+void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az) {
+    k_rotate_particles<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, ax, ay, az);
+}
+
+// The substep recipes a reference driver issues by name:
+//   fluids: compute_particle_bins, compute_density, compute_forces_fluids,
+//           step_forward (src/mex/simstep_fluid.c:18-23)
+//   corotational solid: bins, compute_density,
+//           compute_rotations_and_strains, compute_stresses,
+//           compute_forces_solids, step_forward (scripts/sph/systems.py:194-204)
+//   SVK solid: the same with compute_deformations (systems.py:225-235)
+// Positions do not move between the bins and the integrator, so the sorted
+// copies are gathered once; for fluids the integrator is fused into the
+// force pass.
+void sph_launch_substep(const Launch &L, SphMaterial mat) {
+    sph_launch_bins(L);
+    sph_launch_gather(L, mat == MAT_FLUID, false);
+    sph_launch_density(L, false);
+    if (mat == MAT_FLUID) {
+        sph_launch_forces_fluids(L, true);
+        return;
+    }
+    if (mat == MAT_COROT) sph_launch_rotations_and_strains(L);
+    else sph_launch_deformations(L);
+    sph_launch_stresses(L, mat == MAT_COROT);
+    sph_launch_forces_solids(L, mat == MAT_COROT);
+    sph_launch_step_forward(L);
+}

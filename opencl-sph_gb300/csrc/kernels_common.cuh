@@ -1,0 +1,172 @@
+// kernels_common.cuh -- device helpers shared by every sm_103a kernel of the
+// pipeline: scene/block-map iteration, IEEE-exact distance tests, Kahan
+// sums, the 27-cell neighbour walk and the symmetry-plane images.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sph_internal.h"
+
+#define SPH_FULL_MASK 0xffffffffu
+
+// Iterate the virtual blocks of a segment-aware launch.  Inside the body,
+// `S` is the block's scene and `item` this thread's item index in it.
+#define SPH_FOR_WORK(map)                                                      \
+    for (unsigned vb_ = blockIdx.x; vb_ < (map).num; vb_ += gridDim.x) {       \
+        const BlockWork bw_ = (map).work[vb_];                                 \
+        const SceneDesc &S = scenes[bw_.scene];                                \
+        const unsigned item = bw_.first + threadIdx.x;
+#define SPH_END_WORK }
+
+// Active particle count, clamped to the store's capacity so that a bad `n`
+// written from the host can never index past the fields.
+__device__ __forceinline__ unsigned active_count(const SceneDesc &S) {
+    unsigned n = *S.n;
+    return n < S.pnum ? n : S.pnum;
+}
+
+// ---- IEEE-exact helpers (no FMA contraction) --------------------------------
+// These reproduce the oracle's individually rounded float operations so that
+// cell indices and neighbour decisions are bit-identical.
+
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) {
+    return make_float3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+// (x*x + y*y) + z*z, the order OpenCL's length()/dot() are restated in
+__device__ __forceinline__ float norm2(float3 d) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+// v - (2n) * dot(n, v - p): a mirror image across a symmetry plane
+__device__ __forceinline__ float3 reflect3(float3 v, float3 p, float3 n) {
+    float d = dot3(n, sub3(v, p));
+    float3 tn = make_float3(2.f * n.x, 2.f * n.y, 2.f * n.z);
+    return make_float3(__fsub_rn(v.x, __fmul_rn(tn.x, d)), __fsub_rn(v.y, __fmul_rn(tn.y, d)),
+                       __fsub_rn(v.z, __fmul_rn(tn.z, d)));
+}
+
+// Squared-distance bounds equivalent to the reference's tests on
+// dist = sqrt(r2) (correctly rounded):
+//   r2 <= lt  <=>  dist <  h        r2 <= le  <=>  dist <= h
+struct DistBounds {
+    float lt, le;
+};
+__device__ __forceinline__ float next_up(float x) { return __uint_as_float(__float_as_uint(x) + 1u); }
+__device__ __forceinline__ float next_down(float x) { return __uint_as_float(__float_as_uint(x) - 1u); }
+__device__ __forceinline__ DistBounds dist_bounds(float h) {
+    DistBounds b;
+    float x = __fmul_rn(h, h);
+    // largest x with sqrt_rn(x) < h
+    float lt = x;
+    for (int k = 0; k < 6 && lt > 0.f && __fsqrt_rn(lt) >= h; ++k) lt = next_down(lt);
+    for (int k = 0; k < 6 && __fsqrt_rn(next_up(lt)) < h; ++k) lt = next_up(lt);
+    // largest x with sqrt_rn(x) <= h
+    float le = x;
+    for (int k = 0; k < 6 && le > 0.f && __fsqrt_rn(le) > h; ++k) le = next_down(le);
+    for (int k = 0; k < 6 && __fsqrt_rn(next_up(le)) <= h; ++k) le = next_up(le);
+    b.lt = lt;
+    b.le = le;
+    return b;
+}
+
+// Kahan-compensated float accumulator.
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        float y = __fsub_rn(x, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+struct Kahan3 {
+    Kahan x, y, z;
+    __device__ __forceinline__ void add(float3 v) { x.add(v.x); y.add(v.y); z.add(v.z); }
+    __device__ __forceinline__ float3 get() const { return make_float3(x.s, y.s, z.s); }
+};
+
+__device__ __forceinline__ float3 ld3(const float *p, size_t i) {
+    return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+}
+__device__ __forceinline__ void st3(float *p, size_t i, float3 v) {
+    p[3 * i] = v.x;
+    p[3 * i + 1] = v.y;
+    p[3 * i + 2] = v.z;
+}
+__device__ __forceinline__ float3 xyz(float4 v) { return make_float3(v.x, v.y, v.z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return make_float3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return make_float3(a.x * s, a.y * s, a.z * s); }
+
+// ---- cell walk ----------------------------------------------------------------
+
+// FOR_PARTICLES_IN_RANGE (common.cl:49-68) on the cell-sorted order: the 27
+// cells are visited z, y, x as in the reference, and because cells x-1..x+1
+// of one (z, y) row are consecutive in the sort, each row is one contiguous
+// range [celloffset[first], celloffset[last] + gridcount[last]).  `f(kk)` is
+// called for every sorted neighbour index kk in the reference's order.
+template <class F>
+__device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned cell, F &&f) {
+    const unsigned R0 = S.gridres[0], R1 = S.gridres[1], R2 = S.gridres[2];
+    const unsigned layer = R0 * R1;
+    const unsigned cz = cell / layer;
+    const unsigned rem = cell - cz * layer;
+    const unsigned cy = rem / R0;
+    const unsigned cx = rem - cy * R0;
+    const unsigned x0 = cx > 0 ? cx - 1 : 0;
+    const unsigned x1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
+    const unsigned *__restrict__ off = S.celloffset;
+    const unsigned *__restrict__ cnt = S.gridcount;
+    for (int dz = -1; dz <= 1; ++dz) {
+        int z = (int)cz + dz;
+        if (z < 0 || z >= (int)R2) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+            int y = (int)cy + dy;
+            if (y < 0 || y >= (int)R1) continue;
+            unsigned row = (unsigned)z * layer + (unsigned)y * R0;
+            unsigned b = __ldg(off + row + x0);
+            unsigned e = __ldg(off + row + x1) + __ldg(cnt + row + x1);
+            if (e > S.pnum) e = S.pnum;  // only reachable with inconsistent host-written tables
+            for (unsigned kk = b; kk < e; ++kk) f(kk);
+        }
+    }
+}
+
+// ---- symmetry planes (the SYMMETRY blocks, e.g. common.cl:647-686) ----------
+
+#define SPH_MAX_PLANES 8
+
+struct Planes {
+    float3 p[SPH_MAX_PLANES], n[SPH_MAX_PLANES];
+    unsigned count;
+    unsigned imask;  // planes that i itself passes (|n.(x_i - p)| <= h)
+};
+
+__device__ __forceinline__ void load_planes(const SceneDesc &S, float3 ipos, float h, Planes &P) {
+    P.count = S.num_symmetry_planes < SPH_MAX_PLANES ? S.num_symmetry_planes : SPH_MAX_PLANES;
+    P.imask = 0;
+    for (unsigned k = 0; k < P.count; ++k) {
+        const float *pl = S.symmetry_planes + 6 * k;
+        P.p[k] = make_float3(pl[0], pl[1], pl[2]);
+        P.n[k] = make_float3(pl[3], pl[4], pl[5]);
+        // a zero normal makes jplane_dist 0 < 1e-5 for every j: never live
+        bool live = !(P.n[k].x == 0.f && P.n[k].y == 0.f && P.n[k].z == 0.f);
+        if (live && !(fabsf(dot3(P.n[k], sub3(ipos, P.p[k]))) > h)) P.imask |= 1u << k;
+    }
+}
+
+// Planes of the i-live set that j also passes (|n.(x_j - p)| in [1e-5, h]).
+__device__ __forceinline__ unsigned plane_jmask(const Planes &P, float3 jpos, float h) {
+    unsigned m = 0;
+    for (unsigned k = 0; k < P.count; ++k) {
+        if (!(P.imask & (1u << k))) continue;
+        float jd = fabsf(dot3(P.n[k], sub3(jpos, P.p[k])));
+        if (!(jd > h) && !((double)jd < 1.0e-5)) m |= 1u << k;
+    }
+    return m;
+}

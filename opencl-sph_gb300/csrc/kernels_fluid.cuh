@@ -1,0 +1,211 @@
+// kernels_fluid.cuh -- per-particle pair passes for density and WCSPH
+// forces, the symplectic-Euler integrator and plane constraints (sm_103a).
+//
+// Pair passes run one thread per cell-sorted particle k (i =
+// cellparticles[k]) so a warp covers a few neighbouring cells and shares
+// their neighbour rows in L1; neighbours are streamed from the float4
+// copies built by k_gather.  Sums are Kahan-compensated FP32.
+#pragma once
+
+#include "kernels_common.cuh"
+
+#define SPH_PI_F 3.1415926535f
+
+// compute_density (common.cl:610-690) and compute_original_density
+// (solids.cl:99-170): rho_i = m * sum_j W_poly6(|x_j - x_i|), j = i
+// included, plus mirror images across the symmetry planes.  With
+// `original` the result goes to density0 and no neighbour count is kept.
+__global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original) {
+    SPH_FOR_WORK(map)
+    const unsigned n = active_count(S);
+    if (item < n) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const float h = *S.h;
+        const DistBounds B = dist_bounds(h);
+        const float h2 = h * h;
+        const float3 ipos = xyz(S.spos[k]);
+        Planes P;
+        load_planes(S, ipos, h, P);
+        Kahan rho;
+        unsigned count = 0;
+        const float4 *__restrict__ spos = S.spos;
+        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+            const float3 jpos = xyz(spos[kk]);
+            const float r2 = norm2(sub3(jpos, ipos));
+            if (r2 <= B.le) {
+                float d = fmaxf(h2 - r2, 0.f);
+                rho.add(d * d * d);
+                count += r2 <= B.lt;
+            }
+            if (P.imask) {
+                unsigned jm = plane_jmask(P, jpos, h);
+                // subsets of jm in increasing order: the reference's
+                // plane_bits order restricted to the subsets it keeps
+                for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                    float3 ref = jpos;
+                    for (unsigned s = 0; s < P.count; ++s)
+                        if (bits & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
+                    float m2 = norm2(sub3(ref, ipos));
+                    if (m2 <= B.lt) {
+                        float d = fmaxf(h2 - m2, 0.f);
+                        rho.add(d * d * d);
+                        ++count;
+                    }
+                }
+            }
+        });
+        // poly6 normalisation 315 / (64 pi h^9), applied once
+        const float h3 = h2 * h;
+        const float coef = 315.0f / (64.0f * SPH_PI_F * h3 * h3 * h3);
+        const float value = rho.s * coef * (*S.mass);
+        if (original) {
+            S.density0[i] = value;
+        } else {
+            S.density[i] = value;
+            S.num_neighbours[i] = count;
+            S.sdens[k] = value;
+        }
+    }
+    SPH_END_WORK
+}
+
+// APPLY_CUBE_BOUNDS(ipos, f, -2.0, 2.0) (common.cl:37-43): a repulsive
+// band 0.2 wide inside [-2, 2]^3; the bounds are double literals, so the
+// tests and the update are evaluated in double as in the source.
+__device__ __forceinline__ float cube_bound(float p, float f) {
+    const double mn = -2.0, mx = 2.0, band = (double)0.2f;
+    double dp = (double)p;
+    if (dp < mn + band) return (float)((double)f + (1.0 / (-(mn) + dp) - 5.0));
+    if (dp > mx - band) return (float)((double)f - (1.0 / (mx - dp) - 5.0));
+    return f;
+}
+
+// compute_forces_fluids (kernels/fluids.cl:1-63): pressure
+// p = (rho - rho0) * stiffness, spiky-gradient pressure and Laplacian
+// viscosity pair terms divided by rho_i rho_j, times the mass, plus the
+// cube band.  `fuse_step` also integrates particle i (step_forward) from
+// the sorted copies, which no other thread reads afterwards.
+__device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p);
+
+__global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
+    SPH_FOR_WORK(map)
+    const unsigned n = active_count(S);
+    if (item < n) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const float h = *S.h;
+        const DistBounds B = dist_bounds(h);
+        const float rho0 = *S.restdens, stiff = *S.stiffness, visc = *S.viscosity;
+        const float h3 = h * h * h;
+        const float kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
+        const float3 ipos = xyz(S.spos[k]);
+        const float3 ivel = xyz(S.svel[k]);
+        const float rhoi = S.sdens[k];
+        const float pi = (rhoi - rho0) * stiff;
+        Kahan3 f;
+        const float4 *__restrict__ spos = S.spos;
+        const float4 *__restrict__ svel = S.svel;
+        const float *__restrict__ sdens = S.sdens;
+        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+            if (kk == k) return;
+            const float3 d = sub3(xyz(spos[kk]), ipos);
+            const float r2 = norm2(d);
+            if (!(r2 <= B.le)) return;
+            const float rinv = rsqrtf(r2);
+            const float dist = r2 * rinv;
+            const float din = h - dist;
+            const float rhoj = sdens[kk];
+            const float pj = (rhoj - rho0) * stiff;
+            const float inv_didj = 1.0f / (rhoi * rhoj);
+            const float vterm = visc * din * kv;
+            const float pterm = -(pi + pj) * 0.5f * rinv * din * din * kv;
+            const float3 rv = xyz(svel[kk]) - ivel;
+            f.add(make_float3((d.x * pterm + rv.x * vterm) * inv_didj, (d.y * pterm + rv.y * vterm) * inv_didj,
+                              (d.z * pterm + rv.z * vterm) * inv_didj));
+        });
+        const float m = *S.mass;
+        float3 fi = f.get() * m;
+        fi.x = cube_bound(ipos.x, fi.x);
+        fi.y = cube_bound(ipos.y, fi.y);
+        fi.z = cube_bound(ipos.z, fi.z);
+        st3(S.force, i, fi);
+        if (fuse_step) integrate(S, i, fi, ivel, ipos);
+    }
+    SPH_END_WORK
+}
+
+// step_forward (common.cl:691-722): a = f/m + g, v += dt a, x += dt v;
+// particles of a fixed (non-dynamic) body are skipped.  An optional
+// `wallbounds` field (extension) mirrors particles that leave the box back
+// inside and reverses their normal velocity.
+__device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p) {
+    if (S.body_number) {
+        // a body number beyond body_dynamic's size is treated as dynamic
+        unsigned b = S.body_number[i];
+        if (b > 0 && b <= S.body_capacity && !S.body_dynamic[b - 1]) return;
+    }
+    const float m = *S.mass, dt = *S.timestep;
+    const float3 g = make_float3(S.gravity[0], S.gravity[1], S.gravity[2]);
+    const float3 a = make_float3(f.x / m + g.x, f.y / m + g.y, f.z / m + g.z);
+    st3(S.acceleration, i, a);
+    float3 vn = make_float3(v.x + dt * a.x, v.y + dt * a.y, v.z + dt * a.z);
+    float3 pn = make_float3(p.x + dt * vn.x, p.y + dt * vn.y, p.z + dt * vn.z);
+    if (S.wallbounds) {
+        float *pc = &pn.x, *vc = &vn.x;
+        for (int a2 = 0; a2 < 3; ++a2) {
+            float lo = S.wallbounds[2 * a2], hi = S.wallbounds[2 * a2 + 1];
+            if (pc[a2] < lo) {
+                pc[a2] = lo + (lo - pc[a2]);
+                vc[a2] = -vc[a2];
+            } else if (pc[a2] > hi) {
+                pc[a2] = hi - (pc[a2] - hi);
+                vc[a2] = -vc[a2];
+            }
+        }
+    }
+    if (!(isfinite(pn.x) && isfinite(pn.y) && isfinite(pn.z))) atomicOr(S.status, (unsigned)STATUS_NONFINITE);
+    st3(S.position, i, pn);
+    st3(S.velocity, i, vn);
+}
+
+__global__ void k_step_forward(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned i = item;
+        integrate(S, i, ld3(S.force, i), ld3(S.velocity, i), ld3(S.position, i));
+    }
+    SPH_END_WORK
+}
+
+// apply_plane_constraints (kernels/constraints.cl:1-30): project masked
+// particles onto each of their planes and remove the normal velocity.
+__global__ void k_plane_constraints(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned i = item;
+        const unsigned mask = S.plane_constraints_particles[i];
+        if (mask) {
+            float3 p = ld3(S.position, i), v = ld3(S.velocity, i);
+            for (unsigned c = 0; c < S.num_plane_constraints && c < 32; ++c) {
+                if (!(mask & (1u << c))) continue;
+                const float *pl = S.plane_constraints + 6 * c;
+                float3 pt = make_float3(pl[0], pl[1], pl[2]), nm = make_float3(pl[3], pl[4], pl[5]);
+                float dp = dot3(nm, sub3(p, pt));
+                p = make_float3(p.x - dp * nm.x, p.y - dp * nm.y, p.z - dp * nm.z);
+                float dv = dot3(nm, v);
+                v = make_float3(v.x - dv * nm.x, v.y - dv * nm.y, v.z - dv * nm.z);
+            }
+            st3(S.position, i, p);
+            st3(S.velocity, i, v);
+        }
+    }
+    SPH_END_WORK
+}
+
+// init_original_position (solids.cl:84-95)
+__global__ void k_init_original_position(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) st3(S.originalpos, item, ld3(S.position, item));
+    SPH_END_WORK
+}

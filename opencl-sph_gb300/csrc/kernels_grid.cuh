@@ -1,0 +1,272 @@
+// kernels_grid.cuh -- neighbour grid on sm_103a: cell hash, counting sort
+// with warp-aggregated atomics, segmented exclusive scan, scatter and a
+// deterministic per-cell order (ascending particle index), plus the gathers
+// that build the cell-sorted float4 copies the pair kernels stream.
+//
+// Replaces find_particle_bins, zero_gridcount, count_particles_in_bins,
+// prefix_sum, copy_celloffset_to_backup and insert_particles_in_bin_array
+// (kernels/common.cl:372-529).  Output fields gridcell, gridcount,
+// celloffset and cellparticles have the reference's meaning and layout; the
+// order inside a cell is ascending particle index (the reference's is the
+// atomic race order).
+#pragma once
+
+#include "kernels_common.cuh"
+
+// find_particle_bins (common.cl:372-391) fused with count_particles_in_bins
+// (:401-408).  The cell coordinate is clamp((uint)((p-b0)/(b1-b0)*R), 0,
+// R-1) with each float operation individually rounded and a saturating
+// conversion.  Lanes of a warp that hit the same cell combine into one
+// atomicAdd; each particle keeps its arrival slot within the cell.
+__global__ void k_bin_count(const SceneDesc *__restrict__ scenes, BlockMap map, int do_count) {
+    SPH_FOR_WORK(map)
+    const unsigned n = active_count(S);
+    const bool valid = item < n;
+    const unsigned lanes = __ballot_sync(SPH_FULL_MASK, valid);
+    if (valid) {
+        const float *gb = S.gridbounds;
+        float3 p = ld3(S.position, item);
+        float q[3] = {p.x, p.y, p.z};
+        unsigned c[3];
+        bool outside = false;
+        for (int a = 0; a < 3; ++a) {
+            float lo = gb[2 * a], hi = gb[2 * a + 1];
+            float r = (float)S.gridres[a];
+            float v = __fmul_rn(__fdiv_rn(__fsub_rn(q[a], lo), __fsub_rn(hi, lo)), r);
+            unsigned u = __float2uint_rz(v);  // saturating: negative and NaN -> 0
+            if (u > S.gridres[a] - 1) u = S.gridres[a] - 1;
+            outside |= !(v >= 0.f && v < r);
+            c[a] = u;
+        }
+        const unsigned cell = c[2] * S.gridres[0] * S.gridres[1] + c[1] * S.gridres[0] + c[0];
+        S.gridcell[item] = cell;
+        if (outside) atomicOr(S.status, (unsigned)STATUS_OUTSIDE_GRID);
+        if (do_count) {
+            const unsigned peers = __match_any_sync(lanes, cell);
+            const unsigned lane = threadIdx.x & 31u;
+            const unsigned leader = __ffs(peers) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(S.gridcount + cell, (unsigned)__popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            S.slot[item] = base + __popc(peers & ((1u << lane) - 1u));
+        }
+    }
+    SPH_END_WORK
+}
+
+// zero_gridcount (common.cl:392-400) for every scene of the launch, plus
+// the crowded-cell queue counter.
+__global__ void k_zero_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < S.num_cells) S.gridcount[item] = 0u;
+    if (item == 0) S.big_cells[0] = 0u;
+    SPH_END_WORK
+}
+
+// count_particles_in_bins alone, for a driver that calls the reference's
+// kernels one by one (gridcell already computed).
+__global__ void k_count_only(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    const unsigned n = active_count(S);
+    const bool valid = item < n;
+    const unsigned lanes = __ballot_sync(SPH_FULL_MASK, valid);
+    if (valid) {
+        unsigned cell = S.gridcell[item];
+        if (cell >= S.num_cells) cell = S.num_cells - 1;  // host-written garbage
+        const unsigned peers = __match_any_sync(lanes, cell);
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(S.gridcount + cell, (unsigned)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        S.slot[item] = base + __popc(peers & ((1u << lane) - 1u));
+    }
+    SPH_END_WORK
+}
+
+// ---- segmented exclusive scan of gridcount -> celloffset (prefix_sum,
+// common.cl:409-515, restated as a correct three-phase scan) -----------------
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive
+// prefix and writes the block total to *total.
+__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *total) {
+    __shared__ unsigned warp_sums[32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    unsigned x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned y = __shfl_up_sync(SPH_FULL_MASK, x, o);
+        if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    const unsigned nw = blockDim.x >> 5;
+    if (warp == 0) {
+        unsigned w = lane < nw ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(SPH_FULL_MASK, w, o);
+            if (lane >= (unsigned)o) w += y;
+        }
+        if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    unsigned before = warp ? warp_sums[warp - 1] : 0u;
+    *total = warp_sums[nw - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+// Phase 1: each block scans SPH_SCAN_TILE cells locally.
+__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_tiles(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
+        const BlockWork bw = map.work[vb];
+        const SceneDesc &S = scenes[bw.scene];
+        const unsigned per = SPH_SCAN_TILE / SPH_SCAN_THREADS;
+        const unsigned c0 = bw.first + threadIdx.x * per;
+        unsigned v[SPH_SCAN_TILE / SPH_SCAN_THREADS];
+        unsigned sum = 0;
+        for (unsigned k = 0; k < per; ++k) {
+            unsigned c = c0 + k;
+            v[k] = c < S.num_cells ? S.gridcount[c] : 0u;
+            sum += v[k];
+        }
+        unsigned total;
+        unsigned run = block_exclusive_scan(sum, &total);
+        for (unsigned k = 0; k < per; ++k) {
+            unsigned c = c0 + k;
+            if (c < S.num_cells) S.celloffset[c] = run;
+            run += v[k];
+        }
+        if (threadIdx.x == 0) S.scan_sums[bw.first / SPH_SCAN_TILE] = total;
+    }
+}
+
+// Phase 2: one block per scene scans that scene's tile totals in place.
+__global__ void __launch_bounds__(1024) k_scan_sums(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
+    for (unsigned s = blockIdx.x; s < num_scenes; s += gridDim.x) {
+        const SceneDesc &S = scenes[s];
+        unsigned carry = 0;
+        for (unsigned base = 0; base < S.num_scan_blocks; base += blockDim.x) {
+            unsigned i = base + threadIdx.x;
+            unsigned v = i < S.num_scan_blocks ? S.scan_sums[i] : 0u;
+            unsigned total;
+            unsigned ex = block_exclusive_scan(v, &total);
+            if (i < S.num_scan_blocks) S.scan_sums[i] = carry + ex;
+            carry += total;
+        }
+    }
+}
+
+// Phase 3: add each tile's prefix.
+__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_add(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
+        const BlockWork bw = map.work[vb];
+        const SceneDesc &S = scenes[bw.scene];
+        const unsigned add = S.scan_sums[bw.first / SPH_SCAN_TILE];
+        if (add == 0) continue;
+        for (unsigned c = bw.first + threadIdx.x; c < bw.first + SPH_SCAN_TILE && c < S.num_cells; c += blockDim.x)
+            S.celloffset[c] += add;
+    }
+}
+
+// insert_particles_in_bin_array (common.cl:523-529) without atomics: each
+// particle goes to celloffset[cell] + its arrival slot.
+__global__ void k_scatter(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned cell = S.gridcell[item];
+        if (cell < S.num_cells) {
+            const unsigned dst = S.celloffset[cell] + S.slot[item];
+            if (dst < S.pnum) S.cellparticles[dst] = item;
+        }
+    }
+    SPH_END_WORK
+}
+
+// Canonical order inside each cell: ascending particle index.  Cells of up
+// to SPH_SMALL_CELL particles are insertion-sorted by one thread; larger
+// cells are queued for k_sort_big_cells.
+__global__ void k_sort_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < S.num_cells) {
+        const unsigned cnt = S.gridcount[item];
+        const unsigned off = S.celloffset[item];
+        if (off > S.pnum || cnt > S.pnum - off) {
+            // inconsistent tables (only from host-written garbage): leave it
+        } else if (cnt > SPH_SMALL_CELL) {
+            unsigned k = atomicAdd(S.big_cells, 1u);
+            S.big_cells[1 + k] = item;
+        } else if (cnt > 1) {
+            unsigned *seg = S.cellparticles + off;
+            unsigned v[SPH_SMALL_CELL];
+            for (unsigned a = 0; a < cnt; ++a) {
+                unsigned x = seg[a];
+                unsigned b = a;
+                while (b > 0 && v[b - 1] > x) {
+                    v[b] = v[b - 1];
+                    --b;
+                }
+                v[b] = x;
+            }
+            for (unsigned a = 0; a < cnt; ++a) seg[a] = v[a];
+        }
+    }
+    SPH_END_WORK
+}
+
+// Fallback for crowded cells (e.g. particles clamped into an edge cell):
+// one block bitonic-sorts each queued cell, padded to a power of two, in a
+// scratch region of the sorted-position buffer ([2*off, 2*off + L) of its
+// words, which cannot overlap another cell's region since L < 2*count).
+__global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
+    for (unsigned s = 0; s < num_scenes; ++s) {
+        const SceneDesc &S = scenes[s];
+        const unsigned nbig = S.big_cells[0];
+        for (unsigned b = blockIdx.x; b < nbig; b += gridDim.x) {
+            const unsigned cell = S.big_cells[1 + b];
+            const unsigned off = S.celloffset[cell], cnt = S.gridcount[cell];
+            if (off > S.pnum || cnt > S.pnum - off) continue;
+            unsigned L = 1;
+            while (L < cnt) L <<= 1;
+            unsigned *buf = reinterpret_cast<unsigned *>(S.spos) + 2u * off;
+            unsigned *seg = S.cellparticles + off;
+            for (unsigned t = threadIdx.x; t < L; t += blockDim.x) buf[t] = t < cnt ? seg[t] : 0xffffffffu;
+            __syncthreads();
+            for (unsigned k = 2; k <= L; k <<= 1) {
+                for (unsigned j = k >> 1; j > 0; j >>= 1) {
+                    for (unsigned t = threadIdx.x; t < L; t += blockDim.x) {
+                        unsigned u = t ^ j;
+                        if (u > t) {
+                            unsigned a = buf[t], c = buf[u];
+                            bool up = (t & k) == 0;
+                            if ((a > c) == up) {
+                                buf[t] = c;
+                                buf[u] = a;
+                            }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            for (unsigned t = threadIdx.x; t < cnt; t += blockDim.x) seg[t] = buf[t];
+            __syncthreads();
+        }
+    }
+}
+
+// Cell-sorted copies: spos[k] = position[cellparticles[k]] (and velocity,
+// density when asked).  Gathers once so the pair loops stream float4s.
+__global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int with_vel, int with_dens) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        unsigned i = S.cellparticles[item];
+        if (i >= S.pnum) i = 0;  // host-written garbage
+        float3 p = ld3(S.position, i);
+        S.spos[item] = make_float4(p.x, p.y, p.z, 0.f);
+        if (with_vel) {
+            float3 v = ld3(S.velocity, i);
+            S.svel[item] = make_float4(v.x, v.y, v.z, 0.f);
+        }
+        if (with_dens) S.sdens[item] = S.density[i];
+    }
+    SPH_END_WORK
+}

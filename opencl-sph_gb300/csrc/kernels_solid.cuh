@@ -1,0 +1,562 @@
+// kernels_solid.cuh -- elastic solids on sm_103a: the corotational linear
+// model (kernels/solid_corotation.cl) with its polar decomposition in FP64,
+// the St. Venant-Kirchhoff model (kernels/solid_svk.cl), the shared solid
+// force pass, kinematic bodies (kernels/rigidbody.cl) and the scene-init
+// kernels of common.cl.
+//
+// The 3x3 eigen-solver keeps the reference's scheme (common.cl:101-305):
+// eight Givens rotations, each zeroing the largest remaining off-diagonal
+// of the symmetric matrix.  The rotation for a pivot (a = off-diagonal,
+// b, c = its diagonal pair) is the one with tan(2 theta) = 2a / (b - c) and
+// |theta| <= pi/4, computed with Rutishauser's algebraic form
+// t = sign(tau) / (|tau| + sqrt(1 + tau^2)), tau = (b - c) / (2a),
+// cos = 1/sqrt(1 + t^2), sin = t cos, instead of atan/cos/sin.  A zero
+// pivot gives the identity (the reference evaluates atan(0/0) = NaN when
+// b == c there).
+#pragma once
+
+#include "kernels_common.cuh"
+
+#ifndef SPH_PI_F
+#define SPH_PI_F 3.1415926535f
+#endif
+
+template <typename T>
+__device__ __forceinline__ void givens_rotate(const T in[6], const T pin[9], unsigned off, T o[6], T pout[9]) {
+    // index sets of common.cl:95-99 for off-diagonal 3 (xy), 4 (xz), 5 (yz)
+    unsigned xx, yy, ee, ex, ey;
+    if (off == 3) { xx = 0; yy = 1; ee = 2; ex = 4; ey = 5; }
+    else if (off == 4) { xx = 0; yy = 2; ee = 1; ex = 3; ey = 5; }
+    else { xx = 1; yy = 2; ee = 0; ex = 3; ey = 4; }
+    const T a = in[off], b = in[xx], c = in[yy];
+    T cs = 1, sn = 0;
+    if (a != T(0)) {
+        T tau = (b - c) / (T(2) * a);
+        T t = copysign(T(1), tau) / (fabs(tau) + sqrt(T(1) + tau * tau));
+        cs = T(1) / sqrt(T(1) + t * t);
+        sn = t * cs;
+    }
+    const T c2 = cs * cs, s2 = sn * sn, csn = cs * sn;
+    o[xx] = b * c2 + c * s2 + T(2) * a * csn;
+    o[off] = -b * csn + c * csn + a * (c2 - s2);
+    o[yy] = b * s2 + c * c2 - T(2) * a * csn;
+    o[ee] = in[ee];
+    o[ex] = in[ex] * cs + in[ey] * sn;
+    o[ey] = -in[ex] * sn + in[ey] * cs;
+    for (unsigned r = 0; r < 3; ++r) {
+        pout[3 * r + xx] = pin[3 * r + xx] * cs + pin[3 * r + yy] * sn;
+        pout[3 * r + yy] = -pin[3 * r + xx] * sn + pin[3 * r + yy] * cs;
+        pout[3 * r + ee] = pin[3 * r + ee];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ unsigned max_offdiag(const T t[6]) {
+    T m = 0;
+    unsigned im = 0;
+    for (unsigned k = 0; k < 3; ++k) {
+        T v = fabs(t[3 + k]);
+        if (v > m) { m = v; im = k; }
+    }
+    return im + 3;
+}
+
+// jacobi(i, 0, 8, ...) of common.cl:257-295
+template <typename T>
+__device__ void jacobi8(const T in[6], T eig[3], T p[9]) {
+    T p2[9], t[6], t2[6];
+    for (int k = 0; k < 9; ++k) p[k] = (k % 4 == 0) ? T(1) : T(0);
+    for (int k = 0; k < 6; ++k) t[k] = in[k];
+    unsigned im = max_offdiag(t);
+    for (int it = 0; it < 4; ++it) {
+        givens_rotate(t, p, im, t2, p2);
+        im = max_offdiag(t2);
+        givens_rotate(t2, p2, im, t, p);
+        im = max_offdiag(t);
+    }
+    for (int k = 0; k < 3; ++k) eig[k] = t[k];
+}
+
+// P diag(d) P^T as a symmetric 6-vector (multiplyBothSides, common.cl:169-186)
+template <typename T>
+__device__ __forceinline__ void p_d_pt(const T d[3], const T p[9], T out[6]) {
+    auto e = [&](int r, int c) { return p[3 * r] * d[0] * p[3 * c] + p[3 * r + 1] * d[1] * p[3 * c + 1] + p[3 * r + 2] * d[2] * p[3 * c + 2]; };
+    out[0] = e(0, 0); out[1] = e(1, 1); out[2] = e(2, 2);
+    out[3] = e(0, 1); out[4] = e(0, 2); out[5] = e(1, 2);
+}
+// A S with S symmetric (multiplyAS, common.cl:187-199)
+template <typename T>
+__device__ __forceinline__ void mul_as(const T a[9], const T s[6], T out[9]) {
+    const T S9[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[3 * r + c] = a[3 * r] * S9[c] + a[3 * r + 1] * S9[3 + c] + a[3 * r + 2] * S9[6 + c];
+}
+
+// getR (common.cl:306-331) in FP64: R = A (A^T A)^(-1/2).
+__device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
+    double A[9];
+    for (int k = 0; k < 9; ++k) A[k] = (double)apq[k];
+    double s[6];
+    s[0] = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+    s[1] = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+    s[2] = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+    s[3] = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+    s[4] = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+    s[5] = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+    double eig[3], P[9], tmp[6], R[9];
+    jacobi8(s, eig, P);
+    for (int k = 0; k < 3; ++k) eig[k] = 1.0 / sqrt(eig[k]);
+    p_d_pt(eig, P, tmp);
+    mul_as(A, tmp, R);
+    for (int k = 0; k < 9; ++k) r[k] = (float)R[k];
+}
+
+// jacobiInvert (common.cl:296-305) in FP32
+__device__ void sym_inverse(const float m[6], float out[6]) {
+    float eig[3], P[9];
+    jacobi8(m, eig, P);
+    for (int k = 0; k < 3; ++k) eig[k] = 1.0f / eig[k];
+    p_d_pt(eig, P, out);
+}
+
+__device__ __forceinline__ float3 mat_vec(const float m[9], float3 v) {
+    return make_float3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+                       m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+__device__ __forceinline__ float3 mat_t_vec(const float m[9], float3 v) {
+    return make_float3(m[0] * v.x + m[3] * v.y + m[6] * v.z, m[1] * v.x + m[4] * v.y + m[7] * v.z,
+                       m[2] * v.x + m[5] * v.y + m[8] * v.z);
+}
+__device__ __forceinline__ float3 sym_vec(const float s[6], float3 v) {
+    return make_float3(s[0] * v.x + s[3] * v.y + s[4] * v.z, s[3] * v.x + s[1] * v.y + s[5] * v.z,
+                       s[4] * v.x + s[5] * v.y + s[2] * v.z);
+}
+__device__ __forceinline__ void add_outer(float3 a, float3 b, float m[9]) {
+    m[0] += a.x * b.x; m[1] += a.x * b.y; m[2] += a.x * b.z;
+    m[3] += a.y * b.x; m[4] += a.y * b.y; m[5] += a.y * b.z;
+    m[6] += a.z * b.x; m[7] += a.z * b.y; m[8] += a.z * b.z;
+}
+
+// Spiky gradient dir(d) * -45/(pi h^6) * (h - |d|)^2, zero beyond h
+// (applyKernelGradient, common.cl:81-87); kv = 45/(pi h^6).
+__device__ __forceinline__ float3 spiky_grad(float3 d, float h, float kv, float le) {
+    float r2 = norm2(d);
+    if (!(r2 <= le) || r2 == 0.f) return make_float3(0.f, 0.f, 0.f);
+    float rinv = rsqrtf(r2);
+    float din = h - r2 * rinv;
+    float s = -kv * din * din * rinv;
+    return d * s;
+}
+
+struct SolidConsts {
+    float h, h2, le, lt, kv, coef, mass;
+};
+__device__ __forceinline__ SolidConsts solid_consts(const SceneDesc &S) {
+    SolidConsts c;
+    c.h = *S.h;
+    c.h2 = c.h * c.h;
+    DistBounds b = dist_bounds(c.h);
+    c.le = b.le;
+    c.lt = b.lt;
+    float h3 = c.h2 * c.h;
+    c.kv = 45.0f / (SPH_PI_F * h3 * h3);
+    c.coef = 315.0f / (64.0f * SPH_PI_F * h3 * h3 * h3);
+    c.mass = *S.mass;
+    return c;
+}
+
+// Images of j (and optionally of x0_j and x0_i) across the planes of `bits`.
+__device__ __forceinline__ float3 reflect_bits(const Planes &P, unsigned bits, float3 v) {
+    for (unsigned s = 0; s < P.count; ++s)
+        if (bits & (1u << s)) v = reflect3(v, P.p[s], P.n[s]);
+    return v;
+}
+
+// compute_rotations_and_strains (solid_corotation.cl:28-195): pass 1 sums
+// Apq = sum W(|p|) p q^T (+ images), R = polar(Apq) in FP64, pass 2 sums
+// D = sum (R^T p - q) m / rho0_i (x) gradW(-q) (+ images), strain =
+// sym(D).  Body particles keep their rotation and strain.
+__global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        if (!(S.body_number && S.body_number[i] > 0)) {
+            const SolidConsts C = solid_consts(S);
+            const float3 ipos = xyz(S.spos[k]);
+            const float3 ipos0 = ld3(S.originalpos, i);
+            Planes P;
+            load_planes(S, ipos, C.h, P);
+            const unsigned cell = S.gridcell[i];
+            float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for_each_neighbour(S, cell, [&](unsigned kk) {
+                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+                const float3 jpos = xyz(S.spos[kk]);
+                const float3 jpos0 = ld3(S.originalpos, j);
+                if (j != i) {
+                    float3 p = sub3(jpos, ipos);
+                    float r2 = norm2(p);
+                    if (r2 <= C.le) {
+                        float d = fmaxf(C.h2 - r2, 0.f);
+                        add_outer(p * (d * d * d), sub3(jpos0, ipos0), apq);
+                    }
+                }
+                if (P.imask) {
+                    unsigned jm = plane_jmask(P, jpos, C.h);
+                    for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                        float3 p = sub3(reflect_bits(P, bits, jpos), ipos);
+                        float r2 = norm2(p);
+                        if (r2 <= C.lt) {
+                            float d = fmaxf(C.h2 - r2, 0.f);
+                            add_outer(p * (d * d * d), sub3(reflect_bits(P, bits, jpos0), ipos0), apq);
+                        }
+                    }
+                }
+            });
+            for (int c = 0; c < 9; ++c) apq[c] *= C.coef;
+            float R[9];
+            polar_rotation_fp64(apq, R);
+            for (int c = 0; c < 9; ++c) {
+                S.apq_temp[9 * (size_t)i + c] = apq[c];
+                S.intermediate[9 * (size_t)i + c] = apq[c];
+                S.rotation[9 * (size_t)i + c] = R[c];
+            }
+            const float scale = C.mass / S.density0[i];
+            float D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            for_each_neighbour(S, cell, [&](unsigned kk) {
+                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+                const float3 jpos = xyz(S.spos[kk]);
+                const float3 jpos0 = ld3(S.originalpos, j);
+                if (j != i) {
+                    float3 q = sub3(jpos0, ipos0);
+                    float3 g = spiky_grad(-q, C.h, C.kv, C.le);
+                    if (g.x != 0.f || g.y != 0.f || g.z != 0.f) {
+                        float3 u = mat_t_vec(R, sub3(jpos, ipos)) - q;
+                        add_outer(u * scale, g, D);
+                    }
+                }
+                if (P.imask) {
+                    unsigned jm = plane_jmask(P, jpos, C.h);
+                    for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                        float3 p = mat_t_vec(R, sub3(reflect_bits(P, bits, jpos), ipos));
+                        if (norm2(p) <= C.lt) {
+                            float3 q = sub3(reflect_bits(P, bits, jpos0), ipos0);
+                            add_outer((p - q) * scale, spiky_grad(-q, C.h, C.kv, C.le), D);
+                        }
+                    }
+                }
+            });
+            float *st = S.strain + 6 * (size_t)i;
+            st[0] = D[0];
+            st[1] = D[4];
+            st[2] = D[8];
+            st[3] = 0.5f * (D[1] + D[3]);
+            st[4] = 0.5f * (D[2] + D[6]);
+            st[5] = 0.5f * (D[5] + D[7]);
+        }
+    }
+    SPH_END_WORK
+}
+
+// compute_stresses, corotational (solid_corotation.cl:9-26,197-208):
+// isotropic Hooke's law with the Lame constants.
+__global__ void k_stresses_corot(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const float E = *S.youngs_modulus, nu = *S.poisson;
+        const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
+        const float mu = E / 2.0f / (1.0f + nu);
+        const float *e = S.strain + 6 * (size_t)item;
+        float *o = S.stress + 6 * (size_t)item;
+        const float tr = e[0] + e[1] + e[2];
+        o[0] = lam * tr + 2.0f * mu * e[0];
+        o[1] = lam * tr + 2.0f * mu * e[1];
+        o[2] = lam * tr + 2.0f * mu * e[2];
+        o[3] = 2.0f * mu * e[3];
+        o[4] = 2.0f * mu * e[4];
+        o[5] = 2.0f * mu * e[5];
+    }
+    SPH_END_WORK
+}
+
+// compute_deformations (solid_svk.cl:82-175): F = Apq Aqq^-1.  The poly6
+// normalisation cancels in the product and is left out.
+__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float3 ipos = xyz(S.spos[k]);
+        const float3 ipos0 = ld3(S.originalpos, i);
+        Planes P;
+        load_planes(S, ipos, C.h, P);
+        float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        float aqq[6] = {0, 0, 0, 0, 0, 0};
+        auto contrib = [&](float3 p, float3 q, float w) {
+            add_outer(p * w, q, apq);
+            float3 wq = q * w;
+            aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
+            aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
+            aqq[2] += wq.z * q.z;
+        };
+        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+            const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+            const float3 jpos = xyz(S.spos[kk]);
+            const float3 jpos0 = ld3(S.originalpos, j);
+            if (j != i) {
+                float3 p = sub3(jpos, ipos);
+                float r2 = norm2(p);
+                if (r2 <= C.le) {
+                    float d = fmaxf(C.h2 - r2, 0.f);
+                    contrib(p, sub3(jpos0, ipos0), d * d * d);
+                }
+            }
+            if (P.imask) {
+                unsigned jm = plane_jmask(P, jpos, C.h);
+                for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                    float3 p = sub3(reflect_bits(P, bits, jpos), ipos);
+                    float r2 = norm2(p);
+                    if (r2 <= C.lt) {
+                        float d = fmaxf(C.h2 - r2, 0.f);
+                        contrib(p, sub3(reflect_bits(P, bits, jpos0), ipos0), d * d * d);
+                    }
+                }
+            }
+        });
+        float inv[6];
+        sym_inverse(aqq, inv);
+        float F[9];
+        mul_as(apq, inv, F);
+        for (int c = 0; c < 9; ++c) S.deformation[9 * (size_t)i + c] = F[c];
+    }
+    SPH_END_WORK
+}
+
+// compute_stresses, SVK (solid_svk.cl:1-80): E = (F^T F - I)/2,
+// S = lambda tr(E) I + 2 mu E, sigma = F S F^T / det F.
+__global__ void k_stresses_svk(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const float E = *S.youngs_modulus, nu = *S.poisson;
+        const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
+        const float mu = E / 2.0f / (1.0f + nu);
+        const float *F = S.deformation + 9 * (size_t)item;
+        float f[9];
+        for (int c = 0; c < 9; ++c) f[c] = F[c];
+        auto ftf = [&](int r, int c) { return f[r] * f[c] + f[3 + r] * f[3 + c] + f[6 + r] * f[6 + c]; };
+        float g[6] = {0.5f * ftf(0, 0) - 0.5f, 0.5f * ftf(1, 1) - 0.5f, 0.5f * ftf(2, 2) - 0.5f,
+                      0.5f * ftf(0, 1), 0.5f * ftf(0, 2), 0.5f * ftf(1, 2)};
+        const float first = lam * (g[0] + g[1] + g[2]);
+        float sv[6] = {first + 2.0f * mu * g[0], first + 2.0f * mu * g[1], first + 2.0f * mu * g[2],
+                       2.0f * mu * g[3], 2.0f * mu * g[4], 2.0f * mu * g[5]};
+        float fs[9];
+        mul_as(f, sv, fs);
+        const float det = f[0] * (f[4] * f[8] - f[5] * f[7]) - f[1] * (f[3] * f[8] - f[5] * f[6]) +
+                          f[2] * (f[3] * f[7] - f[4] * f[6]);
+        const float rdet = 1.0f / det;
+        auto cau = [&](int r, int c) { return (fs[3 * r] * f[3 * c] + fs[3 * r + 1] * f[3 * c + 1] + fs[3 * r + 2] * f[3 * c + 2]) * rdet; };
+        float *o = S.stress + 6 * (size_t)item;
+        o[0] = cau(0, 0);
+        o[1] = cau(1, 1);
+        o[2] = cau(2, 2);
+        o[3] = cau(0, 1);
+        o[4] = cau(0, 2);
+        o[5] = cau(1, 2);
+    }
+    SPH_END_WORK
+}
+
+// compute_forces_solids (solid_corotation.cl:215-403 when COROT,
+// solid_svk.cl:182-367 otherwise): elastic pair forces from the stresses
+// in the rest configuration, rotated by R_i / R_j for the corotational
+// model, plus Laplacian viscosity; symmetry images; the force, its elastic
+// and viscous parts and the test-axis cut-off force are all written.
+template <bool COROT>
+__global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float3 ipos = xyz(S.spos[k]);
+        const float3 ivel = ld3(S.velocity, i);
+        const float3 ipos0 = ld3(S.originalpos, i);
+        float si[6], Ri[9];
+        for (int c = 0; c < 6; ++c) si[c] = S.stress[6 * (size_t)i + c];
+        if (COROT)
+            for (int c = 0; c < 9; ++c) Ri[c] = S.rotation[9 * (size_t)i + c];
+        const float rho0i = S.density0[i];
+        Planes P;
+        load_planes(S, ipos, C.h, P);
+        Kahan3 fe_s, fv_s, fec_s, fvc_s;
+        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+            const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+            const float3 jpos = xyz(S.spos[kk]);
+            const float3 jpos0 = ld3(S.originalpos, j);
+            const float3 x = sub3(ipos0, jpos0);
+            const bool direct = j != i && (norm2(x) <= C.le || norm2(sub3(jpos, ipos)) <= C.le);
+            unsigned jm = 0;
+            if (P.imask) jm = plane_jmask(P, jpos, C.h);
+            if (!direct && !jm) return;
+            const float3 jvel = ld3(S.velocity, j);
+            const float vivj = C.mass * C.mass / rho0i / S.density0[j];
+            const float mrj = C.mass / S.density[j];
+            float sj[6], Rj[9];
+            for (int c = 0; c < 6; ++c) sj[c] = S.stress[6 * (size_t)j + c];
+            if (COROT)
+                for (int c = 0; c < 9; ++c) Rj[c] = S.rotation[9 * (size_t)j + c];
+            if (direct) {
+                const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
+                const float3 f_ji = sym_vec(si, gx) * (-vivj);
+                const float3 f_ij = S.body_number[j] > 0 ? -f_ji : sym_vec(sj, -gx) * (-vivj);
+                const float3 fe = COROT ? mat_vec(Rj, f_ij) - mat_vec(Ri, f_ji) : f_ij - f_ji;
+                const float r2 = norm2(sub3(jpos, ipos));
+                const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
+                const float3 fv = (jvel - ivel) * (mrj * lap);
+                fe_s.add(fe);
+                fv_s.add(fv);
+                fec_s.add(fe);
+                fvc_s.add(fv);
+            }
+            for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                const float3 rp = reflect_bits(P, bits, jpos);
+                const float3 rp0 = reflect_bits(P, bits, jpos0);
+                const float3 rip0 = reflect_bits(P, bits, ipos0);
+                const float3 xm = sub3(ipos0, rp0);
+                const float3 refx = sub3(rip0, jpos0);
+                const float3 f_ji = sym_vec(si, spiky_grad(xm, C.h, C.kv, C.le)) * (-vivj);
+                float3 f_ij = sym_vec(sj, spiky_grad(-refx, C.h, C.kv, C.le)) * (-vivj);
+                if (COROT) f_ij = mat_vec(Rj, f_ij);
+                // reflect back across the subset's planes, highest first; the
+                // last normal used (the lowest plane's) also mirrors j's
+                // velocity, as in the source
+                float3 nlast = make_float3(0.f, 0.f, 0.f);
+                for (int s = (int)P.count - 1; s >= 0; --s) {
+                    if (!(bits & (1u << s))) continue;
+                    nlast = P.n[s];
+                    f_ij = f_ij - nlast * (2.f * dot3(nlast, f_ij));
+                }
+                const float3 fe = COROT ? f_ij - mat_vec(Ri, f_ji) : f_ij - f_ji;
+                const float3 refvel = jvel - nlast * (2.f * dot3(nlast, jvel));
+                const float r2 = norm2(sub3(rp, ipos));
+                const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
+                const float3 fv = (refvel - ivel) * (mrj * lap);
+                fe_s.add(fe);
+                fv_s.add(fv);
+                if (!(bits & 1u)) {
+                    fec_s.add(fe);
+                    fvc_s.add(fv);
+                }
+            }
+        });
+        const float visc = *S.viscosity;
+        const float3 fe = fe_s.get() * 0.5f, fv = fv_s.get() * visc;
+        st3(S.force, i, fe + fv);
+        st3(S.force_elastic, i, fe);
+        st3(S.force_viscous, i, fv);
+        st3(S.cutoff_force, i, fec_s.get() * 0.5f + fvc_s.get() * visc);
+    }
+    SPH_END_WORK
+}
+
+// ---- kinematic bodies (kernels/rigidbody.cl) --------------------------------
+
+// set_body_position (rigidbody.cl:1-33): translate the body's particles to
+// the new pose and give them velocity (new - old) / dt.  Every particle
+// reads the old pose; k_store_body_vec records the new one afterwards.
+__global__ void k_set_body_position(const SceneDesc *__restrict__ scenes, BlockMap map, unsigned body, float3 np) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S) && body < *S.body_count && body < S.body_capacity && S.body_number[item] == body + 1) {
+        const float3 old = ld3(S.body_position, body);
+        const float dt = *S.timestep;
+        st3(S.position, item, ld3(S.position, item) - old + np);
+        const float3 dv = np - old;
+        st3(S.velocity, item, make_float3(dv.x / dt, dv.y / dt, dv.z / dt));
+    }
+    SPH_END_WORK
+}
+
+// get_matrix_from_euler, XYX (rigidbody.cl:35-68)
+__device__ void euler_xyx(float3 e, float out[9]) {
+    float cx = cosf(e.x), sx = sinf(e.x), cy = cosf(e.y), sy = sinf(e.y), cx2 = cosf(e.z), sx2 = sinf(e.z);
+    const float rx[9] = {1, 0, 0, 0, cx, -sx, 0, sx, cx};
+    const float ry[9] = {cy, 0, -sy, 0, 1, 0, sy, 0, cy};
+    const float rx2[9] = {1, 0, 0, 0, cx2, -sx2, 0, sx2, cx2};
+    float ryx[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) ryx[3 * r + c] = ry[3 * r] * rx[c] + ry[3 * r + 1] * rx[3 + c] + ry[3 * r + 2] * rx[6 + c];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[3 * r + c] = rx2[3 * r] * ryx[c] + rx2[3 * r + 1] * ryx[3 + c] + rx2[3 * r + 2] * ryx[6 + c];
+}
+
+// set_body_rotation (rigidbody.cl:70-120).  As in the source, the matrix
+// applied is built from the body's stored Euler angles and the particle's
+// rotation field; the new angles are only recorded (by k_store_body_vec).
+__global__ void k_set_body_rotation(const SceneDesc *__restrict__ scenes, BlockMap map, unsigned body) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S) && body < *S.body_count && body < S.body_capacity && S.body_number[item] == body + 1) {
+        float b[9];
+        euler_xyx(ld3(S.body_euler_rotation, body), b);
+        float *pr = S.rotation + 9 * (size_t)item;
+        float prot[9], t2[9], t3[9];
+        for (int c = 0; c < 9; ++c) prot[c] = pr[c];
+        // t2 = b^T prot
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) t2[3 * r + c] = b[r] * prot[c] + b[3 + r] * prot[3 + c] + b[6 + r] * prot[6 + c];
+        const float3 rpos = mat_vec(t2, ld3(S.position, item));
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) t3[3 * r + c] = t2[3 * r] * prot[c] + t2[3 * r + 1] * prot[3 + c] + t2[3 * r + 2] * prot[6 + c];
+        for (int c = 0; c < 9; ++c) pr[c] = t3[c];
+        st3(S.position, item, rpos);
+    }
+    SPH_END_WORK
+}
+
+// Records the body's new pose (which == 0) or Euler angles (which == 1)
+// after the particle update, as particle 0 does in the source.
+__global__ void k_store_body_vec(const SceneDesc *__restrict__ scenes, int which, unsigned body, float3 v) {
+    const SceneDesc &S = scenes[0];
+    if (threadIdx.x == 0 && blockIdx.x == 0 && body < *S.body_count && body < S.body_capacity)
+        st3(which == 0 ? S.body_position : S.body_euler_rotation, body, v);
+}
+
+// ---- scene init (common.cl:533-604) ------------------------------------------
+
+// populate_position_cuboid: a size.x x size.y x size.z lattice spanning
+// corner1..corner2; sets n as the reference does.
+__global__ void k_populate_cuboid(const SceneDesc *__restrict__ scenes, float3 c1, float3 c2, uint3 size) {
+    const SceneDesc &S = scenes[0];
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned j = blockIdx.y * blockDim.y + threadIdx.y;
+    const unsigned k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= size.x || j >= size.y || k >= size.z) return;
+    const unsigned p = i + size.x * j + size.x * size.y * k;
+    if (p >= S.pnum) return;
+    unsigned *n = const_cast<unsigned *>(S.n);
+    if (p == S.pnum - 1) *n = S.pnum;
+    else if (i == size.x - 1 && j == size.y - 1 && k == size.z - 1) *n = size.x * size.y * size.z;
+    float3 q = make_float3(((float)i / (float)(size.x - 1)) * (c2.x - c1.x) + c1.x,
+                           ((float)j / (float)(size.y - 1)) * (c2.y - c1.y) + c1.y,
+                           ((float)k / (float)(size.z - 1)) * (c2.z - c1.z) + c1.z);
+    st3(S.position, p, q);
+}
+
+// rotate_particles: positions rotated by Rx(ax) Ry(ay) Rz(az) with the
+// source's sign conventions.
+__global__ void k_rotate_particles(const SceneDesc *__restrict__ scenes, BlockMap map, float ax, float ay, float az) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) {
+        float cx = cosf(ax), sx = sinf(ax), cy = cosf(ay), sy = sinf(ay), cz = cosf(az), sz = sinf(az);
+        const float rx[9] = {1, 0, 0, 0, cx, -sx, 0, sx, cx};
+        const float ry[9] = {cy, 0, -sy, 0, 1, 0, sy, 0, cy};
+        const float rz[9] = {cz, -sz, 0, sz, cz, 0, 0, 0, 1};
+        float ryz[9], r[9];
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) ryz[3 * a + c] = ry[3 * a] * rz[c] + ry[3 * a + 1] * rz[3 + c] + ry[3 * a + 2] * rz[6 + c];
+        for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) r[3 * a + c] = rx[3 * a] * ryz[c] + rx[3 * a + 1] * ryz[3 + c] + rx[3 * a + 2] * ryz[6 + c];
+        st3(S.position, item, mat_vec(r, ld3(S.position, item)));
+    }
+    SPH_END_WORK
+}

@@ -1,0 +1,57 @@
+// launch.h -- host-side entry points that enqueue the sm_103a kernels of
+// the pipeline on a stream.  Every function works on a table of scenes
+// (one for the drop-in store, many for a batch) through segment-aware
+// block maps; none allocates memory or synchronises.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sph_internal.h"
+
+struct Launch {
+    const SceneDesc *scenes;  // device table
+    unsigned num_scenes;
+    BlockMap particles;       // `block` items per entry
+    BlockMap cells;           // `block` cells per entry
+    BlockMap scan;            // SPH_SCAN_TILE cells per entry
+    unsigned block;           // threads per block for particle/cell kernels
+    unsigned pair_block;      // threads per block for the pair kernels
+    BlockMap pair_particles;  // `pair_block` items per entry
+    unsigned grid_cap;        // upper bound on blocks per launch (persistent loop)
+    cudaStream_t stream;
+};
+
+enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2 };
+
+// Neighbour grid, the reference's kernels one by one.
+void sph_launch_find_bins(const Launch &L);
+void sph_launch_zero_cells(const Launch &L);
+void sph_launch_count(const Launch &L);
+void sph_launch_scan(const Launch &L);
+void sph_launch_insert(const Launch &L);  // scatter + per-cell ordering
+// All of compute_particle_bins: zero, bin+count, scan, insert.
+void sph_launch_bins(const Launch &L);
+// Cell-sorted copies (positions; velocities and densities on request).
+void sph_launch_gather(const Launch &L, bool vel, bool dens);
+
+void sph_launch_density(const Launch &L, bool original);
+void sph_launch_forces_fluids(const Launch &L, bool fuse_step);
+void sph_launch_step_forward(const Launch &L);
+void sph_launch_plane_constraints(const Launch &L);
+void sph_launch_init_original_position(const Launch &L);
+void sph_launch_rotations_and_strains(const Launch &L);
+void sph_launch_stresses(const Launch &L, bool corot);
+void sph_launch_deformations(const Launch &L);
+void sph_launch_forces_solids(const Launch &L, bool corot);
+void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
+void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
+void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);
+void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
+
+// One substep of a material's recipe for every scene of the launch.  All
+// scenes of L must share the material (batches launch one Launch per
+// material group).
+void sph_launch_substep(const Launch &L, SphMaterial mat);
+
+// cudaGetLastError() after the enqueues above; records and returns it.
+cudaError_t sph_check_launch(const char *what);

@@ -1,0 +1,100 @@
+// sph_internal.h -- definitions shared by the host driver and the CUDA
+// kernels of libsph_gb300.so (not part of the public ABI).
+#pragma once
+
+#include <stdint.h>
+
+#include <vector_types.h>  // float4 (CUDA runtime headers)
+
+// ---- errors ---------------------------------------------------------------
+
+// Records a message for sph_last_error() (printf-style).
+void sph_set_error(const char *fmt, ...);
+// Aborts when abort-on-error is on (the reference's ASSERT behaviour).
+void sph_fail();
+
+// ---- materials ------------------------------------------------------------
+
+// Kernel files named in a conf's $opencl_kernel_files list
+// (src/opencl/particle_system_host.c:221-272 loads kernels/<name>.cl).
+enum SphProgram : unsigned {
+    PROG_COMMON = 1u << 0,            // kernels/common.cl
+    PROG_FLUIDS = 1u << 1,            // kernels/fluids.cl
+    PROG_SOLIDS = 1u << 2,            // kernels/solids.cl
+    PROG_COROT = 1u << 3,             // kernels/solid_corotation.cl
+    PROG_SVK = 1u << 4,               // kernels/solid_svk.cl
+    PROG_CONSTRAINTS = 1u << 5,       // kernels/constraints.cl
+    PROG_RIGIDBODY = 1u << 6,         // kernels/rigidbody.cl
+};
+
+// Device status word bits (sph_status()).
+enum SphStatus : unsigned {
+    STATUS_NONFINITE = 1u << 0,       // a non-finite position was written
+    STATUS_OUTSIDE_GRID = 1u << 1,    // a particle was binned outside gridbounds
+};
+
+// Cells with more particles than this are ordered by the block-wide
+// fallback sort instead of the per-cell insertion sort.
+#define SPH_SMALL_CELL 32
+
+// ---- one scene on the device ----------------------------------------------
+//
+// Pointers into the scene's device copy of its psdata blob (fields the
+// program does not use may be null) plus the scratch the GB300 pipeline
+// keeps beside it.  Scalars are read through their device pointers at run
+// time, as the reference's USE_FIELD_FIRST_VALUE does, so a host-to-device
+// sync of a scalar takes effect at the next launch.
+struct SceneDesc {
+    // scalars (device pointers)
+    const unsigned *n;
+    const float *mass, *timestep, *h, *restdens, *stiffness, *viscosity;
+    const float *youngs_modulus, *poisson;
+    const float *gravity, *gridbounds;
+    const float *wallbounds;  // optional reflective box (extension)
+    // particle fields
+    float *position, *velocity, *acceleration, *force;
+    float *density, *density0, *originalpos;
+    float *rotation, *strain, *stress, *apq_temp, *intermediate, *deformation;
+    float *cutoff_force, *force_elastic, *force_viscous;
+    unsigned *num_neighbours;
+    // neighbour grid fields
+    unsigned *gridcell, *gridcount, *celloffset, *cellparticles;
+    // planes and bodies
+    const float *symmetry_planes, *plane_constraints;
+    const unsigned *plane_constraints_particles;
+    const unsigned *body_number, *body_dynamic, *body_count;
+    float *body_position, *body_euler_rotation;
+    // shape, fixed when the store is created
+    unsigned pnum;
+    unsigned gridres[3];
+    unsigned num_cells;
+    unsigned num_symmetry_planes;
+    unsigned num_plane_constraints;
+    unsigned body_capacity;
+    unsigned programs;        // SphProgram bits
+    unsigned jacobi_guard;    // 1: Givens angle 0 when the pivot is exactly 0
+    // scratch (device)
+    unsigned *slot;           // per particle: arrival slot within its cell
+    float4 *spos;             // cell-sorted (x, y, z, 0) positions
+    float4 *svel;             // cell-sorted velocities
+    float *sdens;             // cell-sorted densities
+    unsigned *scan_sums;      // this scene's scan partial sums
+    unsigned num_scan_blocks;
+    unsigned *big_cells;      // [0] = count, [1..] = cells above SPH_SMALL_CELL
+    unsigned *status;         // SphStatus bits
+};
+
+// Block map entry: block b of a launch works on `scene`, items
+// [first, first + block size).
+struct BlockWork {
+    unsigned scene;
+    unsigned first;
+};
+
+struct BlockMap {
+    const BlockWork *work;
+    unsigned num;
+};
+
+#define SPH_SCAN_TILE 2048      // cells per scan block (256 threads x 8)
+#define SPH_SCAN_THREADS 256

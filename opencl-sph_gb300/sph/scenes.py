@@ -1,0 +1,209 @@
+"""Seeded synthetic scenes in the reference's store format.
+
+Each builder returns a :class:`Scene`: the $psdata_specification text, the
+$opencl_kernel_files list, and initial field values.  The scenes are the
+workloads of the benchmark (all synthetic; no dataset is involved):
+
+* :func:`wcsph_block` -- WCSPH fluid lattice in the corner of a box (the
+  8,000-particle dam break at 20^3, and the 1,048,576-particle 128^3 block);
+* :func:`solid_lattice` -- corotational or St. Venant-Kirchhoff solid
+  lattice with clamped layers (the 10x10x40 beam);
+* :func:`batch_mix` -- many uneven scenes, 60% fluid / 25% corotational /
+  15% SVK, particle counts log-uniform.
+
+Lattices are x-fastest, so particle order follows the grid's cell order.
+"""
+import math
+
+import numpy as np
+
+FLUID_KERNELS = "common, fluids"
+COROT_KERNELS = "common, solids, solid_corotation, constraints, rigidbody"
+SVK_KERNELS = "common, solids, solid_svk, constraints, rigidbody"
+
+
+def _fmt(v):
+    if isinstance(v, (list, tuple, np.ndarray)):
+        return ", ".join(_fmt(x) for x in np.ravel(v))
+    if isinstance(v, (int, np.integer)):
+        return str(int(v))
+    return repr(float(v))
+
+
+class Scene(object):
+    """A store specification plus initial values."""
+
+    def __init__(self, name, material, kernel_files, entries, init, n):
+        self.name = name
+        self.material = material          # 'fluid' | 'corot' | 'svk'
+        self.kernel_files = kernel_files
+        self.entries = entries            # (name, dims, type, value or None)
+        self.init = init                  # field -> array (set after build)
+        self.n = n
+
+    @property
+    def spec(self):
+        lines = []
+        for name, dims, typ, val in self.entries:
+            line = "%s | %s | %s" % (name, dims, typ)
+            if val is not None:
+                line += " | " + _fmt(val)
+            lines.append(line)
+        return "\n".join(lines) + "\n"
+
+    def param(self, name):
+        for n, _, _, v in self.entries:
+            if n == name:
+                return v
+        raise KeyError(name)
+
+    def to_double(self):
+        """The same scene with every float field declared double (the FP64
+        run that errors are reported against)."""
+        ents = [(n, d, "double" if t == "float" else t, v) for n, d, t, v in self.entries]
+        return Scene(self.name + "-fp64", self.material, self.kernel_files, ents, self.init, self.n)
+
+    def system(self):
+        """A ParticleSystem on the device with the initial values uploaded."""
+        from .systems import ParticleSystem
+        ps = ParticleSystem(spec=self.spec, kernel_files=self.kernel_files)
+        ps.set_fields(True, **self.init)
+        ps.sync_host_to_device()
+        return ps
+
+
+def lattice(nx, ny, nz, spacing, origin=(0.0, 0.0, 0.0), jitter=0.0, rng=None):
+    """x-fastest (nx*ny*nz, 3) lattice at `spacing` from `origin`, each
+    coordinate jittered uniformly in [-jitter, jitter]."""
+    i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    p = np.stack([i.T.ravel(), j.T.ravel(), k.T.ravel()], axis=1).astype(np.float64) * spacing
+    p += np.asarray(origin, dtype=np.float64)
+    if jitter:
+        rng = rng if rng is not None else np.random.default_rng(0)
+        p += rng.uniform(-jitter, jitter, size=p.shape)
+    return p.astype(np.float32)
+
+
+def _common_entries(pnum, mass, dt, h, gravity, gridbounds, nplanes=0, body_count=1):
+    return [
+        ("pnum", "1", "unsigned int", pnum),
+        ("n", "1", "unsigned int", None),
+        ("mass", "1", "float", mass),
+        ("timestep", "1", "float", dt),
+        ("smoothingradius", "1", "float", h),
+        ("gravity", "3", "float", list(gravity)),
+        ("position", "3, pnum", "float", None),
+        ("posnext", "3, pnum", "float", None),
+        ("velocity", "3, pnum", "float", None),
+        ("veleval", "3, pnum", "float", None),
+        ("acceleration", "3, pnum", "float", None),
+        ("force", "3, pnum", "float", None),
+        ("density", "pnum", "float", None),
+        ("num_neighbours", "pnum", "unsigned int", None),
+        ("gridbounds", "2, 3", "float", list(gridbounds)),
+        ("symmetry_planes", "3, 2, %d" % nplanes, "float", None),
+        ("body_number", "pnum", "unsigned int", None),
+        ("body_count", "1", "unsigned int", body_count),
+        ("body_dynamic", "body_count", "unsigned int", None),
+    ]
+
+
+def wcsph_block(nx=20, ny=20, nz=20, spacing=0.01, h=0.02, box=(0.0, 0.4), jitter=1e-4, seed=0,
+                restdens=1000.0, stiffness=3.0, viscosity=0.2, gravity=(0.0, -9.8, 0.0), dt=1e-4,
+                mass=None, walls=True, pnum=None, name=None):
+    """WCSPH fluid lattice in the low corner of the cube box^3 (the dam
+    break).  `walls` adds the reflective-box extension at the box faces."""
+    rng = np.random.default_rng(seed)
+    pos = lattice(nx, ny, nz, spacing, origin=(box[0] + spacing / 2,) * 3, jitter=jitter, rng=rng)
+    n = pos.shape[0]
+    pnum = pnum or n
+    if mass is None:
+        mass = restdens * spacing ** 3
+    gb = [box[0], box[1]] * 3
+    entries = _common_entries(pnum, mass, dt, h, gravity, gb)
+    entries += [("restdens", "1", "float", restdens), ("stiffness", "1", "float", stiffness),
+                ("viscosity", "1", "float", viscosity)]
+    if walls:
+        entries.append(("wallbounds", "6", "float", gb))
+    return Scene(name or "wcsph-%d" % n, "fluid", FLUID_KERNELS, entries, {"position": pos, "n": n}, n)
+
+
+def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", youngs_modulus=1e5,
+                  poisson=0.3, density=1000.0, viscosity=6e-5, gravity=(0.0, -9.8, 0.0), dt=5e-5,
+                  clamp_layers=2, jitter=0.0, seed=0, margin=None, name=None):
+    """Elastic lattice whose first `clamp_layers` layers along z belong to
+    body 1, a fixed (non-dynamic) body: the clamped beam."""
+    rng = np.random.default_rng(seed)
+    pos = lattice(nx, ny, nz, spacing, jitter=jitter, rng=rng)
+    n = pos.shape[0]
+    ext = np.array([nx, ny, nz]) * spacing
+    m = margin if margin is not None else 4 * h
+    sag = max(ext) + m  # room to bend under gravity along -y
+    gb = [-m, ext[0] + m, -sag, ext[1] + m, -m, ext[2] + m]
+    entries = _common_entries(n, density * spacing ** 3, dt, h, gravity, gb, nplanes=0, body_count=1)
+    entries += [
+        ("originalpos", "3, pnum", "float", None),
+        ("density0", "pnum", "float", None),
+        ("stress", "6, pnum", "float", None),
+        ("rotation", "3, 3, pnum", "float", None),
+        ("viscosity", "1", "float", viscosity),
+        ("youngs_modulus", "1", "float", youngs_modulus),
+        ("poisson", "1", "float", poisson),
+        ("plane_constraints", "3, 2, 0", "float", None),
+        ("plane_constraints_particles", "pnum", "unsigned int", None),
+        ("cutoff_force", "3, pnum", "float", None),
+        ("force_elastic", "3, pnum", "float", None),
+        ("force_viscous", "3, pnum", "float", None),
+        ("padding", "pnum", "unsigned int", None),
+        ("body_position", "3, body_count", "float", None),
+        ("body_euler_rotation", "3, body_count", "float", None),
+    ]
+    if material == "corot":
+        entries += [("strain", "6, pnum", "float", None), ("apq_temp", "3, 3, pnum", "float", None),
+                    ("intermediate", "3, 3, pnum", "float", None)]
+        kernels = COROT_KERNELS
+    else:
+        entries += [("deformation", "3, 3, pnum", "float", None)]
+        kernels = SVK_KERNELS
+    layer = nx * ny
+    body = np.zeros(n, dtype=np.uint32)
+    body[: clamp_layers * layer] = 1
+    rot = np.tile(np.eye(3, dtype=np.float32), (n, 1, 1))
+    init = {"position": pos, "n": n, "body_number": body, "rotation": rot, "body_dynamic": np.zeros(1, np.uint32)}
+    return Scene(name or "%s-%d" % (material, n), material, kernels, entries, init, n)
+
+
+def _dims_for(n_target, aspect=(1.0, 1.0, 1.0)):
+    a = np.asarray(aspect, dtype=np.float64)
+    s = (n_target / np.prod(a)) ** (1.0 / 3.0)
+    d = np.maximum(2, np.round(a * s)).astype(int)
+    return int(d[0]), int(d[1]), int(d[2])
+
+
+def batch_mix(count=256, seed=0, n_range=(1000, 65536), mix=(0.6, 0.25, 0.15), e_range=(1e4, 1e6),
+              nu_range=(0.25, 0.45), spacing=0.01, h=0.02, dt_fluid=1e-4, dt_solid=5e-5, jitter=1e-4):
+    """`count` independent scenes: particle counts log-uniform in n_range,
+    material drawn with probabilities `mix` (fluid, corotational, SVK),
+    Young's modulus log-uniform in e_range, Poisson ratio uniform in
+    nu_range; seeded lattice jitter."""
+    rng = np.random.default_rng(seed)
+    scenes = []
+    for s in range(count):
+        n_target = math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))
+        kind = rng.choice(3, p=np.asarray(mix) / np.sum(mix))
+        sub = int(rng.integers(1 << 30))
+        if kind == 0:
+            nx, ny, nz = _dims_for(n_target, (1.0, 0.5, 1.0))
+            ext = max(nx, nz) * spacing
+            box_hi = 2.0 * ext + 4 * h
+            scenes.append(wcsph_block(nx, ny, nz, spacing=spacing, h=h, box=(0.0, box_hi), jitter=jitter,
+                                      seed=sub, dt=dt_fluid, name="b%03d-fluid" % s))
+        else:
+            nx, ny, nz = _dims_for(n_target, (1.0, 1.0, 2.0))
+            E = math.exp(rng.uniform(math.log(e_range[0]), math.log(e_range[1])))
+            nu = rng.uniform(*nu_range)
+            mat = "corot" if kind == 1 else "svk"
+            scenes.append(solid_lattice(nx, ny, nz, spacing=spacing, h=h, material=mat, youngs_modulus=E,
+                                        poisson=nu, dt=dt_solid, clamp_layers=1, jitter=jitter, seed=sub,
+                                        name="b%03d-%s" % (s, mat)))
+    return scenes

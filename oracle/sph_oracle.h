@@ -1,0 +1,98 @@
+/*
+ * sph_oracle.h -- CPU restatement of the opencl-sph per-substep particle
+ * pipeline, used ONLY as a test oracle and as the timed CPU baseline.
+ *
+ * This is test infrastructure: the product library never links, loads or
+ * calls anything here. Every function restates one reference kernel
+ * (the kernels/ OpenCL files of tauroid/opencl-sph) and cites the lines it
+ * follows.
+ *
+ * The state struct is a flat table of field pointers laid out exactly like
+ * the reference's psdata fields (AoS float[3] vectors, row-major 3x3
+ * matrices, symmetric tensors as [xx,yy,zz,xy,xz,yz]); a field that a
+ * kernel does not use may be NULL.  Two instantiations exist: _f32 (REAL =
+ * float, the reference precision) and _f64 (REAL = double, the FP64 run
+ * that errors are reported against).
+ *
+ * Deviations from the OpenCL source, all deliberate and shared with the
+ * CUDA path:
+ *   - float->uint conversion in find_particle_bins saturates (negative and
+ *     NaN -> 0), the GPU's conversion rule; C leaves it undefined.
+ *   - prefix_sum is a correct serial exclusive scan (the reference's
+ *     cross-work-group fix-up is racy, common.cl:501-514).
+ *   - insert_particles_in_bin_array is a stable scatter: particles of one
+ *     cell appear in ascending index order (the reference's order is the
+ *     nondeterministic atomic_inc order, common.cl:528).
+ *   - set_body_position / set_body_rotation read the old body pose for
+ *     every particle before it is overwritten (the reference relies on an
+ *     unsynchronised global barrier, rigidbody.cl:13-17,30-32).
+ *   - jacobi_guard != 0 defines the Givens angle as 0 when the pivot
+ *     off-diagonal is exactly 0 (the reference evaluates atan(0/0) = NaN
+ *     there when the two diagonal entries are equal, common.cl:124).
+ */
+#ifndef SPH_ORACLE_H_
+#define SPH_ORACLE_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ORACLE_STATE_FIELDS(REAL)                                          \
+    unsigned int n;                 /* active particles */                     \
+    unsigned int gridres[3];                                                   \
+    REAL mass, timestep, smoothingradius;                                      \
+    REAL restdens, stiffness, viscosity;                                       \
+    REAL youngs_modulus, poisson;                                              \
+    REAL gravity[3];                                                           \
+    REAL gridbounds[6];                                                        \
+    unsigned int num_symmetry_planes;   REAL *symmetry_planes;   /* [P][2][3] */\
+    unsigned int num_plane_constraints; REAL *plane_constraints; /* [P][2][3] */\
+    unsigned int *plane_constraints_particles;                                 \
+    unsigned int body_count;                                                   \
+    unsigned int *body_number, *body_dynamic;                                  \
+    REAL *body_position, *body_euler_rotation;                                 \
+    REAL *position, *velocity, *acceleration, *force;                          \
+    REAL *density, *density0, *originalpos;                                    \
+    REAL *rotation, *strain, *stress, *apq_temp, *intermediate, *deformation;  \
+    REAL *cutoff_force, *force_elastic, *force_viscous;                        \
+    unsigned int *num_neighbours;                                              \
+    unsigned int *gridcell, *gridcount, *celloffset, *cellparticles;           \
+    /* optional reflective box (extension, not in the reference): */          \
+    unsigned int has_wallbounds; REAL wallbounds[6];                           \
+    int jacobi_guard;                                                          \
+    int nthreads;
+
+typedef struct { SPH_ORACLE_STATE_FIELDS(float)  } sph_oracle_state_f32;
+typedef struct { SPH_ORACLE_STATE_FIELDS(double) } sph_oracle_state_f64;
+
+#define SPH_ORACLE_DECLARE(SFX, REAL)                                                \
+    void oracle_find_particle_bins##SFX(sph_oracle_state##SFX *s);             \
+    void oracle_sort_particles##SFX(sph_oracle_state##SFX *s);                 \
+    void oracle_compute_particle_bins##SFX(sph_oracle_state##SFX *s);          \
+    void oracle_init_original_position##SFX(sph_oracle_state##SFX *s);         \
+    void oracle_compute_original_density##SFX(sph_oracle_state##SFX *s);       \
+    void oracle_compute_density##SFX(sph_oracle_state##SFX *s);                \
+    void oracle_compute_forces_fluids##SFX(sph_oracle_state##SFX *s);          \
+    void oracle_compute_rotations_and_strains##SFX(sph_oracle_state##SFX *s);  \
+    void oracle_compute_stresses_corot##SFX(sph_oracle_state##SFX *s);         \
+    void oracle_compute_forces_solids_corot##SFX(sph_oracle_state##SFX *s);    \
+    void oracle_compute_deformations##SFX(sph_oracle_state##SFX *s);           \
+    void oracle_compute_stresses_svk##SFX(sph_oracle_state##SFX *s);           \
+    void oracle_compute_forces_solids_svk##SFX(sph_oracle_state##SFX *s);      \
+    void oracle_step_forward##SFX(sph_oracle_state##SFX *s);                   \
+    void oracle_apply_plane_constraints##SFX(sph_oracle_state##SFX *s);        \
+    void oracle_set_body_position##SFX(sph_oracle_state##SFX *s,               \
+                                       unsigned int body, const REAL *pos);   \
+    void oracle_set_body_rotation##SFX(sph_oracle_state##SFX *s,               \
+                                       unsigned int body, const REAL *euler); \
+    void oracle_get_r##SFX(const REAL *apq, REAL *r, int guard);             \
+    void oracle_jacobi_invert##SFX(const REAL *m6, REAL *out6, int guard);
+
+SPH_ORACLE_DECLARE(_f32, float)
+SPH_ORACLE_DECLARE(_f64, double)
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
