@@ -201,6 +201,18 @@ int sph_update(psdata_cuda pso, unsigned int num_steps);
  * outside the grid bounds (and clamped into an edge cell). */
 unsigned int sph_status(psdata_cuda pso);
 void sph_clear_status(psdata_cuda pso);
+/* The store's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or timing events with the store's kernels. */
+void *sph_stream(psdata_cuda pso);
+/* Kernel launches in one sph_update substep of this store (the kernel
+ * nodes of its CUDA graph; 0 before the first sph_update). */
+unsigned int sph_graph_kernel_count(psdata_cuda pso);
+/* Runs `reps` substeps of the store's recipe as individual launches (the
+ * kernels sph_update's graph holds) with CUDA events between phases, and
+ * writes each phase's mean device time in ms and its name.  Returns the
+ * number of phases (at most max_phases), or -1 on failure. */
+int sph_profile_substep(psdata_cuda pso, unsigned int reps, float *phase_ms, const char **phase_names,
+                        unsigned int max_phases);
 /* Library and device description (static string). */
 const char *sph_version(void);
 

@@ -80,6 +80,7 @@ struct Store {
     SceneDesc *d_desc = nullptr;
     Launch L{};
     cudaGraphExec_t step_graph = nullptr;
+    unsigned graph_kernels = 0;
 };
 
 std::mutex g_stores_mu;
@@ -499,6 +500,15 @@ extern "C" int sph_update(psdata_cuda pso, unsigned num_steps) {
             if (g) cudaGraphDestroy(g);
             return -1;
         }
+        size_t nn = 0;
+        cudaGraphGetNodes(g, nullptr, &nn);
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (nn) cudaGraphGetNodes(g, nodes.data(), &nn);
+        s->graph_kernels = 0;
+        for (size_t k = 0; k < nn; ++k) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++s->graph_kernels;
+        }
         cudaError_t ie = cudaGraphInstantiate(&s->step_graph, g, 0);
         cudaGraphDestroy(g);
         if (!cuda_ok(ie, "cudaGraphInstantiate")) {
@@ -509,6 +519,69 @@ extern "C" int sph_update(psdata_cuda pso, unsigned num_steps) {
     for (unsigned k = 0; k < num_steps; ++k)
         if (!cuda_ok(cudaGraphLaunch(s->step_graph, s->stream), "cudaGraphLaunch")) return -1;
     return 0;
+}
+
+namespace {
+struct ProfileCtx {
+    cudaStream_t stream;
+    std::vector<cudaEvent_t> events;
+    std::vector<const char *> names;
+    bool ok = true;
+};
+void profile_mark(void *p, const char *name) {
+    ProfileCtx *c = static_cast<ProfileCtx *>(p);
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { c->ok = false; return; }
+    cudaEventRecord(e, c->stream);
+    c->events.push_back(e);
+    c->names.push_back(name);
+}
+}  // namespace
+
+extern "C" int sph_profile_substep(psdata_cuda pso, unsigned reps, float *phase_ms, const char **phase_names,
+                                   unsigned max_phases) {
+    Store *s = store_of(pso, "sph_profile_substep");
+    if (!s) return -1;
+    if (s->material < 0) {
+        sph_set_error("sph_profile_substep: no substep recipe for this store's program");
+        return -1;
+    }
+    std::vector<double> acc;
+    std::vector<const char *> names;
+    for (unsigned r = 0; r < reps; ++r) {
+        ProfileCtx c;
+        c.stream = s->stream;
+        sph_launch_substep(s->L, (SphMaterial)s->material, profile_mark, &c);
+        bool ok = c.ok && sph_check_launch("sph_profile_substep") == cudaSuccess &&
+                  cuda_ok(cudaStreamSynchronize(s->stream), "sph_profile_substep");
+        if (ok && acc.empty()) {
+            acc.assign(c.events.size() - 1, 0.0);
+            names.assign(c.names.begin(), c.names.end() - 1);
+        }
+        for (size_t k = 0; ok && k + 1 < c.events.size(); ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, c.events[k], c.events[k + 1]);
+            acc[k] += ms;
+        }
+        for (cudaEvent_t e : c.events) cudaEventDestroy(e);
+        if (!ok) return -1;
+    }
+    unsigned np = (unsigned)acc.size() < max_phases ? (unsigned)acc.size() : max_phases;
+    for (unsigned k = 0; k < np; ++k) {
+        phase_ms[k] = reps ? (float)(acc[k] / reps) : 0.f;
+        if (phase_names) phase_names[k] = names[k];
+    }
+    return (int)np;
+}
+
+extern "C" void *sph_stream(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_stream");
+    return s ? (void *)s->stream : nullptr;
+}
+
+extern "C" unsigned sph_graph_kernel_count(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_graph_kernel_count");
+    return s ? s->graph_kernels : 0u;
 }
 
 extern "C" unsigned sph_status(psdata_cuda pso) {

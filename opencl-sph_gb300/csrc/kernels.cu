@@ -137,17 +137,39 @@ void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az) 
 // Positions do not move between the bins and the integrator, so the sorted
 // copies are gathered once; for fluids the integrator is fused into the
 // force pass.
-void sph_launch_substep(const Launch &L, SphMaterial mat) {
-    sph_launch_bins(L);
+void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *ctx) {
+    auto phase = [&](const char *name) {
+        if (mark) mark(ctx, name);
+    };
+    phase("bin_count");
+    sph_launch_zero_cells(L);
+    k_bin_count<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, 1);
+    phase("scan");
+    sph_launch_scan(L);
+    phase("insert");
+    sph_launch_insert(L);
+    phase("gather");
     sph_launch_gather(L, mat == MAT_FLUID, false);
+    phase("density");
     sph_launch_density(L, false);
     if (mat == MAT_FLUID) {
+        phase("forces_fluids+step");
         sph_launch_forces_fluids(L, true);
+        phase(nullptr);
         return;
     }
-    if (mat == MAT_COROT) sph_launch_rotations_and_strains(L);
-    else sph_launch_deformations(L);
+    if (mat == MAT_COROT) {
+        phase("rotations_and_strains");
+        sph_launch_rotations_and_strains(L);
+    } else {
+        phase("deformations");
+        sph_launch_deformations(L);
+    }
+    phase("stresses");
     sph_launch_stresses(L, mat == MAT_COROT);
+    phase("forces_solids");
     sph_launch_forces_solids(L, mat == MAT_COROT);
+    phase("step_forward");
     sph_launch_step_forward(L);
+    phase(nullptr);
 }

@@ -50,8 +50,10 @@ void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
 
 // One substep of a material's recipe for every scene of the launch.  All
 // scenes of L must share the material (batches launch one Launch per
-// material group).
-void sph_launch_substep(const Launch &L, SphMaterial mat);
+// material group).  `mark`, when given, is called with each phase's name
+// before the phase is enqueued and with nullptr after the last one.
+typedef void (*PhaseMark)(void *ctx, const char *phase);
+void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark = nullptr, void *ctx = nullptr);
 
 // cudaGetLastError() after the enqueues above; records and returns it.
 cudaError_t sph_check_launch(const char *what);

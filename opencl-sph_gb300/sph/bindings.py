@@ -193,6 +193,9 @@ _SIGS = {
     "sph_status": ([psdata_cuda], c_uint),
     "sph_clear_status": ([psdata_cuda], None),
     "sph_version": ([], c_char_p),
+    "sph_stream": ([psdata_cuda], c_void_p),
+    "sph_graph_kernel_count": ([psdata_cuda], c_uint),
+    "sph_profile_substep": ([psdata_cuda, c_uint, POINTER(c_float), POINTER(c_char_p), c_uint], c_int),
 }
 
 for _n, (_a, _r) in _SIGS.items():

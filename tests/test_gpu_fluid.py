@@ -1,0 +1,172 @@
+"""GPU parity: neighbour grid, density, WCSPH forces, integration.
+
+Each test runs the CUDA path through the C ABI and the CPU oracle
+(oracle/sph_oracle.c, itself pinned bit-exact to the reference's kernels)
+on the same store.  Tolerances:
+  - integer and index outputs (gridcell, gridcount, celloffset,
+    cellparticles, num_neighbours): bit-exact;
+  - density: max |d| <= 1e-5 of max |rho| (poly6 evaluated from r^2 and
+    summed with Kahan compensation, the oracle sums pow() terms plainly);
+  - forces: max |d| <= 1e-4 of max |f| on identical inputs;
+  - positions after N substeps: relative L2 error <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from helpers import max_rel, oracle_of, rel_err
+from sph import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def _bins_equal(ps, orc, n):
+    ps.sync_device_to_host()
+    cell, count, off, parts = ps.get_fields("gridcell", "gridcount", "celloffset", "cellparticles")
+    orc.call("compute_particle_bins")
+    assert np.array_equal(cell[:n], orc.a["gridcell"][:n])
+    assert np.array_equal(count.ravel(), orc.a["gridcount"])
+    assert np.array_equal(off.ravel(), orc.a["celloffset"])
+    assert np.array_equal(parts[:n], orc.a["cellparticles"][:n])
+
+
+@pytest.mark.parametrize("jitter", [0.0, 1e-4, 3e-3])
+def test_bins_bitexact(jitter):
+    sc = scenes.wcsph_block(13, 9, 11, jitter=jitter, seed=11)
+    ps = sc.system()
+    orc = oracle_of(ps)
+    ps.compute_particle_bins()
+    _bins_equal(ps, orc, sc.n)
+    assert ps.status() == 0
+    ps.close()
+
+
+def test_bins_outside_grid_and_crowded_cells():
+    """Particles outside gridbounds clamp into edge cells (status bit 1);
+    a cell with more than 32 particles takes the block-sort path."""
+    sc = scenes.wcsph_block(10, 10, 10, jitter=1e-4, seed=3)
+    pos = sc.init["position"].copy()
+    rng = np.random.default_rng(5)
+    pos[:40] = rng.uniform(-0.3, -0.01, size=(40, 3))           # below the box: corner cell
+    pos[40:140] = 0.105 + rng.uniform(0, 0.004, size=(100, 3))  # 100 in one cell
+    pos[140:180] = rng.uniform(0.45, 0.9, size=(40, 3))         # above the box
+    ps = sc.system()
+    ps.set_fields(position=pos)
+    orc = oracle_of(ps)
+    ps.compute_particle_bins()
+    _bins_equal(ps, orc, sc.n)
+    assert ps.status() & 2
+    ps.close()
+
+
+@pytest.mark.parametrize("n_active", [0, 1, 777])
+def test_bins_ragged_n(n_active):
+    sc = scenes.wcsph_block(10, 10, 10, jitter=1e-4, seed=9)
+    ps = sc.system()
+    ps.set_fields(n=n_active)
+    orc = oracle_of(ps)
+    ps.compute_particle_bins()
+    _bins_equal(ps, orc, n_active)
+    ps.call_for_all_particles("compute_density")
+    ps.sync_device_to_host()
+    orc.call("compute_density")
+    assert np.array_equal(ps.get_fields("num_neighbours")[0][:n_active], orc.a["num_neighbours"][:n_active])
+    ps.close()
+
+
+def test_reference_kernel_sequence_equals_fused_bins():
+    """find_particle_bins, zero_gridcount, count_particles_in_bins,
+    prefix_sum, copy_celloffset_to_backup, insert_particles_in_bin_array
+    called by name give compute_particle_bins' tables."""
+    sc = scenes.wcsph_block(9, 9, 9, jitter=2e-3, seed=2)
+    ps = sc.system()
+    orc = oracle_of(ps)
+    for k in ["find_particle_bins", "zero_gridcount", "count_particles_in_bins", "prefix_sum",
+              "copy_celloffset_to_backup", "insert_particles_in_bin_array"]:
+        ps.call_for_all_particles(k)
+    _bins_equal(ps, orc, sc.n)
+    ps.close()
+
+
+def test_density_and_neighbour_sets():
+    sc = scenes.wcsph_block(14, 12, 10, jitter=2e-3, seed=4)
+    ps = sc.system()
+    orc = oracle_of(ps)
+    ps.compute_particle_bins()
+    ps.call_for_all_particles("compute_density")
+    ps.sync_device_to_host()
+    orc.call("compute_particle_bins")
+    orc.call("compute_density")
+    n = sc.n
+    nn, rho = ps.get_fields("num_neighbours", "density")
+    assert np.array_equal(nn[:n], orc.a["num_neighbours"][:n])
+    assert max_rel(rho[:n], orc.a["density"][:n]) <= 1e-5
+
+
+def test_forces_on_identical_inputs():
+    sc = scenes.wcsph_block(12, 12, 12, jitter=1e-3, seed=6)
+    ps = sc.system()
+    rng = np.random.default_rng(1)
+    ps.set_fields(velocity=rng.normal(0, 0.05, size=(sc.n, 3)).astype(np.float32))
+    orc = oracle_of(ps)
+    orc.call("compute_particle_bins")
+    orc.call("compute_density")
+    ps.compute_particle_bins()
+    ps.set_fields(density=orc.a["density"])  # the oracle's density as input
+    ps.call_for_all_particles("compute_forces_fluids")
+    orc.call("compute_forces_fluids")
+    ps.sync_device_to_host()
+    f = ps.get_fields("force")[0][: sc.n]
+    assert max_rel(f, orc.a["force"][: sc.n]) <= 1e-4
+    ps.close()
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_trajectory_named_and_fused(walls):
+    """N substeps through the reference's kernel names and through the
+    CUDA-graph substep agree with the oracle."""
+    sc = scenes.wcsph_block(12, 10, 12, jitter=1e-4, seed=8, walls=walls)
+    steps = 40
+    a = sc.system()
+    b = sc.system()
+    orc = oracle_of(a)
+    for _ in range(steps):
+        a.compute_particle_bins()
+        for k in ["compute_density", "compute_forces_fluids", "step_forward"]:
+            a.call_for_all_particles(k)
+    b.update_fused(steps)
+    orc.run("fluid", steps)
+    a.sync_device_to_host()
+    b.sync_device_to_host()
+    n = sc.n
+    pa = a.get_fields("position")[0][:n]
+    pb = b.get_fields("position")[0][:n]
+    assert np.array_equal(pa, pb), "named and fused paths differ"
+    assert rel_err(pa, orc.a["position"][:n]) <= 1e-5
+    assert np.array_equal(a.get_fields("num_neighbours")[0][:n], orc.a["num_neighbours"][:n])
+    a.close()
+    b.close()
+
+
+def test_error_vs_fp64_run():
+    """FP32 GPU trajectory against the all-FP64 oracle run of the scene."""
+    sc = scenes.wcsph_block(10, 10, 10, jitter=1e-4, seed=12)
+    ps = sc.system()
+    o64 = oracle_of(ps, prec="f64")
+    steps = 100
+    ps.update_fused(steps)
+    o64.run("fluid", steps)
+    ps.sync_device_to_host()
+    err = rel_err(ps.get_fields("position")[0][: sc.n], o64.a["position"][: sc.n])
+    assert err <= 1e-4
+    ps.close()
+
+
+def test_status_nonfinite():
+    sc = scenes.wcsph_block(8, 8, 8, jitter=1e-4, seed=1)
+    ps = sc.system()
+    pos = sc.init["position"].copy()
+    pos[5] = np.nan
+    ps.set_fields(position=pos)
+    ps.update_fused(1)
+    assert ps.status() & 1
+    ps.close()
