@@ -4,8 +4,8 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
 
 Workloads (seeded synthetic scenes; sph/scenes.py):
-  wcsph-1m   1,048,576-particle WCSPH block (128^3 lattice, spacing 0.005 m,
-             h = 0.01 m, +-5e-5 m jitter) in a [0,1]^3 box, dt = 2e-5 s: the
+  wcsph-1m   1,048,576-particle WCSPH slab (128 x 64 x 128 lattice, spacing
+             0.005 m, h = 0.01 m, +-5e-5 m jitter) in a [0,1]^3 box, dt = 2e-5 s: the
              plain single-scene drop-in path, one CUDA-graph substep per step
              (default)
   dam-8k     8,000-particle WCSPH dam break (20^3 at 0.01 m, h = 0.02 m) in
@@ -68,9 +68,11 @@ PHASE_BYTES = {
 def workload(name, seed):
     from sph import scenes
     if name == "wcsph-1m":
-        return scenes.wcsph_block(128, 128, 128, spacing=0.005, h=0.01, box=(0.0, 1.0), jitter=5e-5, seed=seed,
+        # 1,048,576 particles (the configuration's count; a 128^3 lattice
+        # would hold 2,097,152) as a 128 x 64 x 128 slab, 64 layers high
+        return scenes.wcsph_block(128, 64, 128, spacing=0.005, h=0.01, box=(0.0, 1.0), jitter=5e-5, seed=seed,
                                   dt=2e-5, walls=True, name="wcsph-1m"), \
-            "1,048,576-particle WCSPH block, 128^3 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s"
+            "1,048,576-particle WCSPH slab, 128x64x128 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s"
     if name == "dam-8k":
         return scenes.wcsph_block(20, 20, 20, seed=seed, name="dam-8k"), \
             "8,000-particle WCSPH dam break, 20^3 at 0.01 m, h=0.02 m, [0,0.4]^3 box, dt=1e-4 s"
@@ -267,7 +269,10 @@ def run_e2e(ps, scene, steps, torch):
     from sph import bindings as bnd
     size = bnd.psdata_data_size(ps.psdata)
     cudart = torch.cuda.cudart()
-    registered = cudart.cudaHostRegister(ps.psdata.data, size, 0) == 0
+    try:
+        registered = int(cudart.cudaHostRegister(ps.psdata.data, size, 0)) == 0
+    except Exception:
+        registered = False
     names_in = ("gravity", "timestep")
     t0 = time.perf_counter()
     for _ in range(steps):

@@ -213,6 +213,40 @@ unsigned int sph_graph_kernel_count(psdata_cuda pso);
  * number of phases (at most max_phases), or -1 on failure. */
 int sph_profile_substep(psdata_cuda pso, unsigned int reps, float *phase_ms, const char **phase_names,
                         unsigned int max_phases);
+/* ---- NEW: batched and served forms ---------------------------------------
+ * A batch holds many independent scenes resident on the device and
+ * advances all of them together: every phase of the substep is one
+ * segment-aware launch over all scenes (blocks map to (scene, first item)),
+ * the material phases of fluid, corotational and SVK scenes run as
+ * parallel branches, and the whole substep is one CUDA graph, recaptured
+ * only when scenes are added or removed.  Scenes keep the psdata layout of
+ * their host store; each scene's result is independent of the others in
+ * the batch (the same kernels, order and arithmetic as alone). */
+typedef struct sph_batch sph_batch;
+sph_batch *sph_batch_create(void);
+void sph_batch_free(sph_batch *batch);
+/* Device bytes a scene will hold once added (blob + scratch). */
+size_t sph_scene_bytes(psdata *scene, const char *file_list);
+/* Uploads a scene (its current host values) and, for solids, runs the
+ * setup of scripts/sph/systems.py:185-192.  Returns its id (>= 0) or -1. */
+int sph_batch_add(sph_batch *batch, psdata *scene, const char *file_list);
+/* Releases a scene's device memory (stream-ordered). */
+int sph_batch_remove(sph_batch *batch, int id);
+/* Advances every scene of the batch by num_steps substeps. */
+int sph_batch_step(sph_batch *batch, unsigned int num_steps);
+/* Copies a scene's device store into `out` (same layout as when added). */
+int sph_batch_read(sph_batch *batch, int id, psdata *out);
+int sph_batch_synchronize(sph_batch *batch);
+/* Device bytes held by the batch's scenes and tables. */
+size_t sph_batch_bytes(sph_batch *batch);
+unsigned int sph_batch_size(sph_batch *batch);
+/* Launch shape: threads per block for particle/cell kernels and for pair
+ * kernels, and the persistent-grid cap (0: one block per work item). */
+int sph_batch_tune(sph_batch *batch, unsigned int block, unsigned int pair_block, unsigned int grid_cap);
+unsigned int sph_batch_kernel_count(sph_batch *batch);
+void *sph_batch_stream(sph_batch *batch);
+unsigned int sph_batch_status(sph_batch *batch, int id);
+
 /* Library and device description (static string). */
 const char *sph_version(void);
 

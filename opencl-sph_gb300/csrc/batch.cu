@@ -1,0 +1,424 @@
+// batch.cu -- the batched form: many independent scenes resident on the
+// device, advanced together by segment-aware launches captured in one
+// CUDA graph per substep (see the sph_batch_* declarations in sph_gb300.h).
+//
+// Memory is stream-ordered (cudaMallocAsync/cudaFreeAsync on the batch's
+// stream), so adding or retiring a scene never synchronises the device and
+// work already queued keeps running: this is what lets the serving loop
+// admit requests while others are on the GPU.
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "launch.h"
+#include "sph_gb300.h"
+#include "sph_internal.h"
+#include "store.h"
+
+namespace {
+
+struct BatchScene {
+    unsigned programs = 0;
+    int material = -1;
+    char *mem = nullptr;     // blob followed by scratch
+    size_t bytes = 0;
+    size_t blob_size = 0;
+    SceneDesc desc{};
+};
+
+bool ok(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    sph_set_error("%s: %s", what, cudaGetErrorString(e));
+    return false;
+}
+
+struct GroupLaunch {
+    Launch L{};
+    bool present = false;
+};
+
+}  // namespace
+
+struct sph_batch {
+    cudaStream_t stream = nullptr;
+    cudaStream_t side[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
+    std::vector<BatchScene *> slots;
+    bool dirty = true;
+    char *tables = nullptr;  // scene table + block maps
+    size_t table_bytes = 0;
+    Launch all{};
+    GroupLaunch group[3];    // by SphMaterial
+    cudaGraphExec_t graph = nullptr;
+    unsigned graph_kernels = 0;
+    unsigned block = 256, pair_block = 128, grid_cap = 0;
+    size_t bytes = 0;
+};
+
+namespace {
+
+unsigned cap_of(const sph_batch *b) { return b->grid_cap ? b->grid_cap : (1u << 30); }
+
+// Uploads a table of scenes and its maps into one stream-ordered buffer.
+struct TableBuild {
+    std::vector<char> host;
+    size_t add(const void *p, size_t n) {
+        size_t o = host.size();
+        size_t pad = Arena::align(n);
+        host.resize(o + pad, 0);
+        if (n) memcpy(host.data() + o, p, n);
+        return o;
+    }
+};
+
+BlockMap map_at(char *base, size_t off, const std::vector<BlockWork> &v) {
+    return {reinterpret_cast<const BlockWork *>(base + off), (unsigned)v.size()};
+}
+
+void release_graph(sph_batch *b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_kernels = 0;
+}
+
+// Runs the solid setup (init_original_position, compute_particle_bins,
+// compute_original_density) for one freshly added scene.
+bool solid_setup(sph_batch *b, BatchScene *sc) {
+    std::vector<SceneDesc> one(1, sc->desc);
+    HostMaps m;
+    sph_build_maps(one, {0u}, b->block, b->pair_block, &m);
+    TableBuild t;
+    size_t o_d = t.add(&sc->desc, sizeof(SceneDesc));
+    size_t o_p = t.add(m.particles.data(), m.particles.size() * sizeof(BlockWork));
+    size_t o_pp = t.add(m.pair_particles.data(), m.pair_particles.size() * sizeof(BlockWork));
+    size_t o_c = t.add(m.cells.data(), m.cells.size() * sizeof(BlockWork));
+    size_t o_s = t.add(m.scan.data(), m.scan.size() * sizeof(BlockWork));
+    char *d = nullptr;
+    if (!ok(cudaMallocAsync(&d, t.host.size(), b->stream), "cudaMallocAsync(setup)")) return false;
+    if (!ok(cudaMemcpyAsync(d, t.host.data(), t.host.size(), cudaMemcpyHostToDevice, b->stream), "setup upload"))
+        return false;
+    Launch L{};
+    L.scenes = reinterpret_cast<SceneDesc *>(d + o_d);
+    L.num_scenes = 1;
+    L.particles = map_at(d, o_p, m.particles);
+    L.pair_particles = map_at(d, o_pp, m.pair_particles);
+    L.cells = map_at(d, o_c, m.cells);
+    L.scan = map_at(d, o_s, m.scan);
+    L.block = b->block;
+    L.pair_block = b->pair_block;
+    L.grid_cap = cap_of(b);
+    L.stream = b->stream;
+    sph_launch_init_original_position(L);
+    sph_launch_bins(L);
+    sph_launch_gather(L, false, false);
+    sph_launch_density(L, true);
+    bool good = sph_check_launch("sph_batch_add(setup)") == cudaSuccess;
+    // the host copy must outlive the asynchronous upload
+    good = ok(cudaStreamSynchronize(b->stream), "sph_batch_add(setup)") && good;
+    cudaFreeAsync(d, b->stream);
+    return good;
+}
+
+bool rebuild(sph_batch *b) {
+    // the previous graph may still be running: let it finish before its
+    // executable and tables go away
+    if (b->graph && !ok(cudaStreamSynchronize(b->stream), "batch rebuild")) return false;
+    release_graph(b);
+    std::vector<unsigned> ids;
+    std::vector<SceneDesc> descs;
+    for (unsigned i = 0; i < b->slots.size(); ++i)
+        if (b->slots[i]) {
+            ids.push_back(i);
+            descs.push_back(b->slots[i]->desc);
+        }
+    if (b->tables) cudaFreeAsync(b->tables, b->stream);
+    b->tables = nullptr;
+    b->table_bytes = 0;
+    b->dirty = false;
+    if (descs.empty()) return true;
+    std::vector<unsigned> idx(descs.size()), by_mat[3];
+    for (unsigned k = 0; k < descs.size(); ++k) {
+        idx[k] = k;
+        by_mat[b->slots[ids[k]]->material].push_back(k);
+    }
+    HostMaps all, g[3];
+    sph_build_maps(descs, idx, b->block, b->pair_block, &all);
+    for (int m = 0; m < 3; ++m) sph_build_maps(descs, by_mat[m], b->block, b->pair_block, &g[m]);
+    TableBuild t;
+    size_t o_d = t.add(descs.data(), descs.size() * sizeof(SceneDesc));
+    size_t o_p = t.add(all.particles.data(), all.particles.size() * sizeof(BlockWork));
+    size_t o_pp = t.add(all.pair_particles.data(), all.pair_particles.size() * sizeof(BlockWork));
+    size_t o_c = t.add(all.cells.data(), all.cells.size() * sizeof(BlockWork));
+    size_t o_s = t.add(all.scan.data(), all.scan.size() * sizeof(BlockWork));
+    size_t o_gp[3], o_gpp[3];
+    for (int m = 0; m < 3; ++m) {
+        o_gp[m] = t.add(g[m].particles.data(), g[m].particles.size() * sizeof(BlockWork));
+        o_gpp[m] = t.add(g[m].pair_particles.data(), g[m].pair_particles.size() * sizeof(BlockWork));
+    }
+    if (!ok(cudaMallocAsync(&b->tables, t.host.size(), b->stream), "cudaMallocAsync(batch tables)")) return false;
+    b->table_bytes = t.host.size();
+    if (!ok(cudaMemcpyAsync(b->tables, t.host.data(), t.host.size(), cudaMemcpyHostToDevice, b->stream),
+            "batch tables upload") ||
+        !ok(cudaStreamSynchronize(b->stream), "batch tables upload"))
+        return false;
+    char *d = b->tables;
+    Launch &A = b->all;
+    A = Launch{};
+    A.scenes = reinterpret_cast<SceneDesc *>(d + o_d);
+    A.num_scenes = (unsigned)descs.size();
+    A.particles = map_at(d, o_p, all.particles);
+    A.pair_particles = map_at(d, o_pp, all.pair_particles);
+    A.cells = map_at(d, o_c, all.cells);
+    A.scan = map_at(d, o_s, all.scan);
+    A.block = b->block;
+    A.pair_block = b->pair_block;
+    A.grid_cap = cap_of(b);
+    A.stream = b->stream;
+    cudaStream_t streams[3] = {b->stream, b->side[0], b->side[1]};
+    for (int m = 0; m < 3; ++m) {
+        GroupLaunch &G = b->group[m];
+        G.present = !by_mat[m].empty();
+        G.L = A;
+        G.L.particles = map_at(d, o_gp[m], g[m].particles);
+        G.L.pair_particles = map_at(d, o_gpp[m], g[m].pair_particles);
+        G.L.stream = streams[m];
+    }
+    // capture one substep: shared phases on the batch stream, then one
+    // branch per material present, joined back
+    cudaGraph_t graph = nullptr;
+    if (!ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture")) return false;
+    sph_launch_bins(A);
+    sph_launch_gather(A, true, false);
+    sph_launch_density(A, false);
+    cudaEventRecord(b->fork, b->stream);
+    for (int m = 0; m < 3; ++m) {
+        GroupLaunch &G = b->group[m];
+        if (!G.present) continue;
+        if (m > 0) cudaStreamWaitEvent(G.L.stream, b->fork, 0);
+        if (m == MAT_FLUID) {
+            sph_launch_forces_fluids(G.L, true);
+        } else {
+            if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L);
+            else sph_launch_deformations(G.L);
+            sph_launch_stresses(G.L, m == MAT_COROT);
+            sph_launch_forces_solids(G.L, m == MAT_COROT);
+            sph_launch_step_forward(G.L);
+        }
+        if (m > 0) {
+            cudaEventRecord(b->join[m - 1], G.L.stream);
+            cudaStreamWaitEvent(b->stream, b->join[m - 1], 0);
+        }
+    }
+    cudaError_t le = cudaGetLastError();
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        sph_set_error("batch capture: %s", cudaGetErrorString(le != cudaSuccess ? le : ce));
+        if (graph) cudaGraphDestroy(graph);
+        return false;
+    }
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (nn) cudaGraphGetNodes(graph, nodes.data(), &nn);
+    for (size_t k = 0; k < nn; ++k) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nodes[k], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++b->graph_kernels;
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (!ok(ie, "batch graph instantiate")) {
+        b->graph = nullptr;
+        return false;
+    }
+    return true;
+}
+
+BatchScene *scene_of(sph_batch *b, int id, const char *what) {
+    if (!b || id < 0 || (size_t)id >= b->slots.size() || !b->slots[id]) {
+        sph_set_error("%s: no scene %d in the batch", what, id);
+        return nullptr;
+    }
+    return b->slots[id];
+}
+
+}  // namespace
+
+extern "C" sph_batch *sph_batch_create(void) {
+    sph_batch *b = new sph_batch();
+    bool good = ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "sph_batch_create") &&
+                ok(cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking), "sph_batch_create") &&
+                ok(cudaStreamCreateWithFlags(&b->side[1], cudaStreamNonBlocking), "sph_batch_create") &&
+                ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "sph_batch_create") &&
+                ok(cudaEventCreateWithFlags(&b->join[0], cudaEventDisableTiming), "sph_batch_create") &&
+                ok(cudaEventCreateWithFlags(&b->join[1], cudaEventDisableTiming), "sph_batch_create");
+    if (!good) {
+        sph_batch_free(b);
+        return nullptr;
+    }
+    return b;
+}
+
+extern "C" void sph_batch_free(sph_batch *b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    release_graph(b);
+    for (BatchScene *s : b->slots)
+        if (s) {
+            if (s->mem) cudaFreeAsync(s->mem, b->stream);
+            delete s;
+        }
+    if (b->tables) cudaFreeAsync(b->tables, b->stream);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (cudaEvent_t e : {b->fork, b->join[0], b->join[1]})
+        if (e) cudaEventDestroy(e);
+    for (cudaStream_t s : {b->stream, b->side[0], b->side[1]})
+        if (s) cudaStreamDestroy(s);
+    delete b;
+}
+
+extern "C" size_t sph_scene_bytes(psdata *scene, const char *file_list) {
+    std::string err;
+    unsigned programs = scene ? sph_parse_programs(file_list, &err) : 0;
+    SceneDesc d;
+    if (!programs || !sph_resolve_scene(*scene, nullptr, programs, &d, &err)) {
+        sph_set_error("sph_scene_bytes: %s", err.c_str());
+        return 0;
+    }
+    return Arena::align(psdata_data_size(*scene)) + sph_scratch_bytes(d);
+}
+
+extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list) {
+    if (!b || !scene) {
+        sph_set_error("sph_batch_add: null batch or scene");
+        return -1;
+    }
+    std::string err;
+    unsigned programs = sph_parse_programs(file_list, &err);
+    SceneDesc probe;
+    if (!programs || !sph_resolve_scene(*scene, nullptr, programs, &probe, &err)) {
+        sph_set_error("sph_batch_add: %s", err.c_str());
+        return -1;
+    }
+    int material = sph_material_of(programs);
+    if (material < 0) {
+        sph_set_error("sph_batch_add: the program has no substep recipe (needs fluids, solid_corotation or solid_svk)");
+        return -1;
+    }
+    BatchScene *sc = new BatchScene();
+    sc->programs = programs;
+    sc->material = material;
+    sc->blob_size = psdata_data_size(*scene);
+    size_t o_scratch = Arena::align(sc->blob_size);
+    sc->bytes = o_scratch + sph_scratch_bytes(probe);
+    if (!ok(cudaMallocAsync(&sc->mem, sc->bytes, b->stream), "cudaMallocAsync(scene)")) {
+        delete sc;
+        return -1;
+    }
+    sph_resolve_scene(*scene, sc->mem, programs, &sc->desc, &err);
+    sph_place_scratch(&sc->desc, sc->mem + o_scratch);
+    bool good = ok(cudaMemcpyAsync(sc->mem, scene->data, sc->blob_size, cudaMemcpyHostToDevice, b->stream),
+                   "sph_batch_add upload") &&
+                ok(cudaMemsetAsync(sc->desc.status, 0, 4, b->stream), "sph_batch_add") &&
+                ok(cudaStreamSynchronize(b->stream), "sph_batch_add upload");
+    if (good && material != MAT_FLUID) good = solid_setup(b, sc);
+    if (!good) {
+        cudaFreeAsync(sc->mem, b->stream);
+        delete sc;
+        return -1;
+    }
+    int id = -1;
+    for (size_t i = 0; i < b->slots.size(); ++i)
+        if (!b->slots[i]) {
+            id = (int)i;
+            break;
+        }
+    if (id < 0) {
+        id = (int)b->slots.size();
+        b->slots.push_back(nullptr);
+    }
+    b->slots[id] = sc;
+    b->bytes += sc->bytes;
+    b->dirty = true;
+    return id;
+}
+
+extern "C" int sph_batch_remove(sph_batch *b, int id) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_remove");
+    if (!sc) return -1;
+    cudaFreeAsync(sc->mem, b->stream);
+    b->bytes -= sc->bytes;
+    delete sc;
+    b->slots[id] = nullptr;
+    b->dirty = true;
+    return 0;
+}
+
+extern "C" int sph_batch_step(sph_batch *b, unsigned num_steps) {
+    if (!b) return -1;
+    if (b->dirty && !rebuild(b)) return -1;
+    if (!b->graph) return 0;  // empty batch
+    for (unsigned k = 0; k < num_steps; ++k)
+        if (!ok(cudaGraphLaunch(b->graph, b->stream), "sph_batch_step")) return -1;
+    return 0;
+}
+
+extern "C" int sph_batch_read(sph_batch *b, int id, psdata *out) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_read");
+    if (!sc) return -1;
+    if (!out || psdata_data_size(*out) != sc->blob_size) {
+        sph_set_error("sph_batch_read: the host store's layout differs from the scene's");
+        return -1;
+    }
+    if (!ok(cudaMemcpyAsync(out->data, sc->mem, sc->blob_size, cudaMemcpyDeviceToHost, b->stream), "sph_batch_read") ||
+        !ok(cudaStreamSynchronize(b->stream), "sph_batch_read"))
+        return -1;
+    return 0;
+}
+
+extern "C" int sph_batch_synchronize(sph_batch *b) {
+    if (!b) return -1;
+    return ok(cudaStreamSynchronize(b->stream), "sph_batch_synchronize") ? 0 : -1;
+}
+
+extern "C" size_t sph_batch_bytes(sph_batch *b) { return b ? b->bytes + b->table_bytes : 0; }
+
+extern "C" unsigned sph_batch_size(sph_batch *b) {
+    if (!b) return 0;
+    unsigned n = 0;
+    for (BatchScene *s : b->slots) n += s != nullptr;
+    return n;
+}
+
+extern "C" int sph_batch_tune(sph_batch *b, unsigned block, unsigned pair_block, unsigned grid_cap) {
+    if (!b) return -1;
+    auto valid = [](unsigned t) { return t >= 32 && t <= 1024 && t % 32 == 0; };
+    if (!valid(block) || !valid(pair_block)) {
+        sph_set_error("sph_batch_tune: block sizes must be multiples of 32 in [32, 1024]");
+        return -1;
+    }
+    b->block = block;
+    b->pair_block = pair_block;
+    b->grid_cap = grid_cap;
+    b->dirty = true;
+    return 0;
+}
+
+extern "C" unsigned sph_batch_kernel_count(sph_batch *b) {
+    if (!b) return 0;
+    if (b->dirty && !rebuild(b)) return 0;
+    return b->graph_kernels;
+}
+
+extern "C" void *sph_batch_stream(sph_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+extern "C" unsigned sph_batch_status(sph_batch *b, int id) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_status");
+    if (!sc) return 0xFFFFFFFFu;
+    unsigned v = 0;
+    if (!ok(cudaMemcpyAsync(&v, sc->desc.status, 4, cudaMemcpyDeviceToHost, b->stream), "sph_batch_status") ||
+        !ok(cudaStreamSynchronize(b->stream), "sph_batch_status"))
+        return 0xFFFFFFFFu;
+    return v;
+}

@@ -84,7 +84,8 @@ __device__ __forceinline__ float cube_bound(float p, float f) {
 // compute_forces_fluids (kernels/fluids.cl:1-63): pressure
 // p = (rho - rho0) * stiffness, spiky-gradient pressure and Laplacian
 // viscosity pair terms divided by rho_i rho_j, times the mass, plus the
-// cube band.  `fuse_step` also integrates particle i (step_forward) from
+// cube band.  A pair at exactly zero distance contributes nothing (the
+// reference produces NaN there).  `fuse_step` also integrates particle i (step_forward) from
 // the sorted copies, which no other thread reads afterwards.
 __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p);
 
@@ -111,7 +112,9 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
             if (kk == k) return;
             const float3 d = sub3(xyz(spos[kk]), ipos);
             const float r2 = norm2(d);
-            if (!(r2 <= B.le)) return;
+            // distinct particles at exactly zero distance: no defined
+            // direction (the reference divides by the distance, fluids.cl:48)
+            if (!(r2 <= B.le) || r2 == 0.f) return;
             const float rinv = rsqrtf(r2);
             const float dist = r2 * rinv;
             const float din = h - dist;

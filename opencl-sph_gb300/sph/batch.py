@@ -1,0 +1,117 @@
+"""Batched form: many independent scenes advanced together on the GPU.
+
+A :class:`Batch` keeps each scene's store resident on the device and
+advances all of them with one CUDA graph per substep (libsph_gb300's
+sph_batch_* entry points): every phase is one segment-aware launch over
+all scenes, and the fluid / corotational / SVK material phases run as
+parallel graph branches.  A scene's result does not depend on what else is
+in the batch.
+"""
+import ctypes
+
+import numpy as np
+
+from . import bindings as bnd
+from . import free_data_cpu, init_data_cpu
+
+
+class Scene(object):
+    """A scene resident in a batch: its host store and id."""
+
+    def __init__(self, scene, ps, sid):
+        self.scene = scene
+        self.psdata = ps
+        self.id = sid
+        self.views = bnd.store_views(ps)
+
+
+class Batch(object):
+    def __init__(self):
+        self.handle = bnd.sph_batch_create()
+        if not self.handle:
+            raise bnd.SphError(bnd.last_error())
+        self.scenes = {}
+
+    @staticmethod
+    def host_store(scene):
+        ps = init_data_cpu(scene.spec)
+        v = bnd.store_views(ps)
+        for k, val in scene.init.items():
+            v[k][...] = val
+        return ps
+
+    @staticmethod
+    def scene_bytes(scene, ps=None):
+        own = ps is None
+        ps = ps or Batch.host_store(scene)
+        b = bnd.sph_scene_bytes(ctypes.byref(ps), scene.kernel_files)
+        if own:
+            free_data_cpu(ps)
+        return int(b)
+
+    def add(self, scene, ps=None):
+        """Uploads `scene` (its initial values, or the given host store)."""
+        ps = ps or self.host_store(scene)
+        sid = bnd.sph_batch_add(self.handle, ctypes.byref(ps), scene.kernel_files)
+        if sid < 0:
+            free_data_cpu(ps)
+            raise bnd.SphError(bnd.last_error())
+        self.scenes[sid] = Scene(scene, ps, sid)
+        return sid
+
+    def remove(self, sid):
+        if bnd.sph_batch_remove(self.handle, sid) != 0:
+            raise bnd.SphError(bnd.last_error())
+        free_data_cpu(self.scenes.pop(sid).psdata)
+
+    def step(self, steps=1):
+        if bnd.sph_batch_step(self.handle, steps) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def synchronize(self):
+        if bnd.sph_batch_synchronize(self.handle) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def read(self, sid):
+        """Copies scene `sid` back; returns its host views (name -> array)."""
+        s = self.scenes[sid]
+        if bnd.sph_batch_read(self.handle, sid, ctypes.byref(s.psdata)) != 0:
+            raise bnd.SphError(bnd.last_error())
+        return s.views
+
+    def tune(self, block, pair_block, grid_cap):
+        if bnd.sph_batch_tune(self.handle, block, pair_block, grid_cap) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    @property
+    def bytes(self):
+        return int(bnd.sph_batch_bytes(self.handle))
+
+    @property
+    def kernels_per_step(self):
+        return int(bnd.sph_batch_kernel_count(self.handle))
+
+    @property
+    def stream(self):
+        return bnd.sph_batch_stream(self.handle)
+
+    def status(self, sid):
+        return int(bnd.sph_batch_status(self.handle, sid))
+
+    @property
+    def particles(self):
+        return sum(s.scene.n for s in self.scenes.values())
+
+    def close(self):
+        if self.handle:
+            bnd.sph_batch_free(self.handle)
+            self.handle = None
+        for s in self.scenes.values():
+            free_data_cpu(s.psdata)
+        self.scenes = {}
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

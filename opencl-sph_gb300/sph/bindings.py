@@ -196,6 +196,21 @@ _SIGS = {
     "sph_stream": ([psdata_cuda], c_void_p),
     "sph_graph_kernel_count": ([psdata_cuda], c_uint),
     "sph_profile_substep": ([psdata_cuda, c_uint, POINTER(c_float), POINTER(c_char_p), c_uint], c_int),
+    # batched / served forms (opaque sph_batch*)
+    "sph_batch_create": ([], c_void_p),
+    "sph_batch_free": ([c_void_p], None),
+    "sph_scene_bytes": ([POINTER(psdata), String], c_size_t),
+    "sph_batch_add": ([c_void_p, POINTER(psdata), String], c_int),
+    "sph_batch_remove": ([c_void_p, c_int], c_int),
+    "sph_batch_step": ([c_void_p, c_uint], c_int),
+    "sph_batch_read": ([c_void_p, c_int, POINTER(psdata)], c_int),
+    "sph_batch_synchronize": ([c_void_p], c_int),
+    "sph_batch_bytes": ([c_void_p], c_size_t),
+    "sph_batch_size": ([c_void_p], c_uint),
+    "sph_batch_tune": ([c_void_p, c_uint, c_uint, c_uint], c_int),
+    "sph_batch_kernel_count": ([c_void_p], c_uint),
+    "sph_batch_stream": ([c_void_p], c_void_p),
+    "sph_batch_status": ([c_void_p, c_int], c_uint),
 }
 
 for _n, (_a, _r) in _SIGS.items():

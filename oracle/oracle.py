@@ -60,7 +60,7 @@ def _state_type(real):
         ("deformation", P), ("cutoff_force", P), ("force_elastic", P), ("force_viscous", P),
         ("num_neighbours", U), ("gridcell", U), ("gridcount", U), ("celloffset", U), ("cellparticles", U),
         ("has_wallbounds", c_uint), ("wallbounds", real * 6),
-        ("jacobi_guard", c_int), ("nthreads", c_int),
+        ("guards", c_int), ("nthreads", c_int),
     ]})
 
 
@@ -86,9 +86,11 @@ class OracleScene(object):
                "compute_deformations", "compute_stresses_svk", "compute_forces_solids_svk", "step_forward",
                "apply_plane_constraints"]
 
-    def __init__(self, fields, prec="f32", nthreads=1, jacobi_guard=1):
+    def __init__(self, fields, prec="f32", nthreads=1, guards=3):
         """`fields`: name -> array as given by ParticleSystem.get_fields
-        (scalars as 1-element arrays)."""
+        (scalars as 1-element arrays).  `guards` (see sph_oracle.h): 3
+        defines the two cases where the reference yields NaN, as the CUDA
+        path does; 0 reproduces the reference bit for bit."""
         self.prec = prec
         self.T = np.float32 if prec == "f32" else np.float64
         real = c_float if prec == "f32" else c_double
@@ -147,7 +149,7 @@ class OracleScene(object):
         if "wallbounds" in fields:
             st.has_wallbounds = 1
             st.wallbounds[:] = [float(x) for x in np.ravel(fields["wallbounds"])[:6]]
-        st.jacobi_guard = jacobi_guard
+        st.guards = guards
         st.nthreads = nthreads
         for name, arr in self.a.items():
             ctype = c_uint if arr.dtype == np.uint32 else real

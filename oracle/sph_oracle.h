@@ -26,9 +26,15 @@
  *   - set_body_position / set_body_rotation read the old body pose for
  *     every particle before it is overwritten (the reference relies on an
  *     unsynchronised global barrier, rigidbody.cl:13-17,30-32).
- *   - jacobi_guard != 0 defines the Givens angle as 0 when the pivot
+ *   - guards bit 0 defines the Givens angle as 0 when the pivot
  *     off-diagonal is exactly 0 (the reference evaluates atan(0/0) = NaN
  *     there when the two diagonal entries are equal, common.cl:124).
+ *   - guards bit 1 makes a pair of distinct particles at exactly zero
+ *     distance contribute nothing to the fluid pressure/viscosity force and
+ *     gives a zero spiky gradient at zero distance (the reference divides
+ *     by the distance there, fluids.cl:48 and common.cl:83, producing NaN;
+ *     FP32 WCSPH under tension can merge two particles exactly).
+ * With guards = 0 the oracle reproduces the reference bit for bit.
  */
 #ifndef SPH_ORACLE_H_
 #define SPH_ORACLE_H_
@@ -59,7 +65,7 @@ extern "C" {
     unsigned int *gridcell, *gridcount, *celloffset, *cellparticles;           \
     /* optional reflective box (extension, not in the reference): */          \
     unsigned int has_wallbounds; REAL wallbounds[6];                           \
-    int jacobi_guard;                                                          \
+    int guards; /* bit 0: Givens zero pivot, bit 1: zero-distance pairs */     \
     int nthreads;
 
 typedef struct { SPH_ORACLE_STATE_FIELDS(float)  } sph_oracle_state_f32;

@@ -46,8 +46,9 @@ static inline REAL OF(k_poly6)(REAL dist, REAL h) {
     return (REAL)315.0f / (REAL)64.0f / O_PI / R_POW(h, (REAL)9.0f) *
            R_POW(R_POW(h, (REAL)2.0f) - R_POW(dist, (REAL)2.0f), (REAL)3.0f);
 }
-static inline V3 OF(k_spiky_grad)(V3 d, REAL h) {
+static inline V3 OF(k_spiky_grad)(V3 d, REAL h, int guard) {
     REAL norm = OF(v3_len)(d);
+    if (guard && norm == 0) return OF(v3)(0, 0, 0);
     V3 dir = OF(v3_div)(d, norm);
     if (norm > h) return OF(v3)(0, 0, 0);
     /* direction * -45.0f/PI/pow(h,6) * pow(h - norm, 2), left-associative */
@@ -360,6 +361,7 @@ void OF(oracle_compute_forces_fluids)(OST *s) {
             V3 diff = OF(v3_sub)(jpos, ipos), relvel = OF(v3_sub)(jvel, ivel);
             REAL dist = OF(v3_len)(diff);
             if (dist > h) continue;
+            if ((s->guards & 2) && dist == 0) continue;
             REAL dist_in = h - dist;
             REAL didj = s->density[i] * s->density[j];
             REAL sr6 = R_POW(h, (REAL)6);
@@ -432,7 +434,7 @@ void OF(oracle_compute_rotations_and_strains)(OST *s) {
         REAL *r = s->rotation + 9 * (size_t)i;
         REAL *inter = s->intermediate + 9 * (size_t)i;
         for (int d = 0; d < 9; ++d) inter[d] = apq[d];
-        OF(oracle_get_r)(inter, r, s->jacobi_guard);
+        OF(oracle_get_r)(inter, r, s->guards & 1);
         REAL rt[9], D[9];
         OF(transpose)(r, rt);
         for (int d = 0; d < 9; ++d) D[d] = 0;
@@ -443,7 +445,7 @@ void OF(oracle_compute_rotations_and_strains)(OST *s) {
             V3 q = OF(v3_sub)(jpos0, ipos0);
             V3 u = OF(v3_sub)(p, q);
             if (j != i)
-                OF(add_outer)(OF(v3_div)(OF(v3_mul)(u, mass), s->density0[i]), OF(k_spiky_grad)(OF(v3_neg)(q), h), D);
+                OF(add_outer)(OF(v3_div)(OF(v3_mul)(u, mass), s->density0[i]), OF(k_spiky_grad)(OF(v3_neg)(q), h, s->guards & 2), D);
             for (unsigned bits = 1; bits < (1u << nsp); ++bits) {
                 V3 rp = jpos, rp0 = jpos0;
                 int skip = 0;
@@ -460,7 +462,7 @@ void OF(oracle_compute_rotations_and_strains)(OST *s) {
                 u = OF(v3_sub)(p, q);
                 REAL dist = OF(v3_len)(p);
                 if (dist < h)
-                    OF(add_outer)(OF(v3_div)(OF(v3_mul)(u, mass), s->density0[i]), OF(k_spiky_grad)(OF(v3_neg)(q), h),
+                    OF(add_outer)(OF(v3_div)(OF(v3_mul)(u, mass), s->density0[i]), OF(k_spiky_grad)(OF(v3_neg)(q), h, s->guards & 2),
                                   D);
             }
         })
@@ -523,9 +525,9 @@ static void OF(forces_solids)(OST *s, int corot) {
             const REAL *jst = s->stress + 6 * (size_t)j;
             const REAL *jrot = corot ? s->rotation + 9 * (size_t)j : ident;
             if (j != i) {
-                V3 f_ji = OF(v3_mul)(OF(mul_sv)(ist, OF(k_spiky_grad)(x, h)), -vivj);
+                V3 f_ji = OF(v3_mul)(OF(mul_sv)(ist, OF(k_spiky_grad)(x, h, s->guards & 2)), -vivj);
                 V3 f_ij = s->body_number[j] > 0 ? OF(v3_neg)(f_ji)
-                                                 : OF(v3_mul)(OF(mul_sv)(jst, OF(k_spiky_grad)(OF(v3_neg)(x), h)), -vivj);
+                                                 : OF(v3_mul)(OF(mul_sv)(jst, OF(k_spiky_grad)(OF(v3_neg)(x), h, s->guards & 2)), -vivj);
                 V3 fe = corot ? OF(v3_add)(OF(v3_neg)(OF(mul_mv)(irot, f_ji)), OF(mul_mv)(jrot, f_ij))
                               : OF(v3_add)(OF(v3_neg)(f_ji), f_ij);
                 V3 fv = OF(v3_mul)(OF(v3_mul)(OF(v3_sub)(jvel, ivel), mass / s->density[j]),
@@ -551,8 +553,8 @@ static void OF(forces_solids)(OST *s, int corot) {
                 if (skip) continue;
                 V3 xm = OF(v3_sub)(ipos0, rp0);
                 V3 refx = OF(v3_sub)(rip0, jpos0);
-                V3 f_ji = OF(v3_mul)(OF(mul_sv)(ist, OF(k_spiky_grad)(xm, h)), -vivj);
-                V3 f_ij = OF(v3_mul)(OF(mul_sv)(jst, OF(k_spiky_grad)(OF(v3_neg)(refx), h)), -vivj);
+                V3 f_ji = OF(v3_mul)(OF(mul_sv)(ist, OF(k_spiky_grad)(xm, h, s->guards & 2)), -vivj);
+                V3 f_ij = OF(v3_mul)(OF(mul_sv)(jst, OF(k_spiky_grad)(OF(v3_neg)(refx), h, s->guards & 2)), -vivj);
                 if (corot) f_ij = OF(mul_mv)(jrot, f_ij);
                 /* reflect f_ij back across the subset's planes, highest first;
                  * `normal` ends as the lowest plane's normal (used by refvel) */
@@ -623,7 +625,7 @@ void OF(oracle_compute_deformations)(OST *s) {
             }
         })
         REAL inv[6];
-        OF(oracle_jacobi_invert)(aqq, inv, s->jacobi_guard);
+        OF(oracle_jacobi_invert)(aqq, inv, s->guards & 1);
         OF(mul_as)(apq, inv, s->deformation + 9 * (size_t)i);
     }
 }

@@ -15,9 +15,9 @@ def host_store(scene, **extra):
     return ps, v
 
 
-def oracle_of(system_or_views, prec="f32", nthreads=4, guard=1):
+def oracle_of(system_or_views, prec="f32", nthreads=4, guards=3):
     views = system_or_views if isinstance(system_or_views, dict) else bnd.store_views(system_or_views.psdata)
-    return OracleScene(views, prec, nthreads=nthreads, jacobi_guard=guard)
+    return OracleScene(views, prec, nthreads=nthreads, guards=guards)
 
 
 def rel_err(a, b):

@@ -1,0 +1,133 @@
+"""GPU: the batched and served forms.
+
+A scene advanced inside a batch (any mix of fluid, corotational and SVK
+scenes, added and removed while others run, any launch shape) must give
+bit-identical results to the same scene run alone through the drop-in
+path, which the other GPU tests tie to the oracle.  The serving loop must
+return, for every request, the same result as the request run alone.
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_of, rel_err
+from sph import scenes
+from sph.batch import Batch
+from sph.serving import Server, poisson_requests, release
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(scene, steps):
+    ps = scene.system()
+    if scene.material != "fluid":
+        ps.call_for_all_particles("init_original_position")
+        ps.compute_particle_bins()
+        ps.call_for_all_particles("compute_original_density")
+    ps.update_fused(steps)
+    ps.sync_device_to_host()
+    pos = np.array(ps.get_fields("position")[0][: scene.n])
+    vel = np.array(ps.get_fields("velocity")[0][: scene.n])
+    ps.close()
+    return pos, vel
+
+
+def mix(seed=0):
+    return [
+        scenes.wcsph_block(9, 6, 9, jitter=1e-4, seed=seed + 1, name="f1"),
+        scenes.solid_lattice(5, 5, 9, material="corot", youngs_modulus=3e4, jitter=1e-4, seed=seed + 2,
+                             clamp_layers=1, name="c1"),
+        scenes.wcsph_block(13, 7, 11, jitter=1e-4, seed=seed + 3, name="f2"),
+        scenes.solid_lattice(6, 5, 7, material="svk", youngs_modulus=5e4, poisson=0.35, jitter=1e-4,
+                             seed=seed + 4, clamp_layers=1, name="s1"),
+    ]
+
+
+def test_batch_matches_scenes_alone():
+    scs = mix()
+    steps = 12
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    b.step(steps)
+    for s, sid in zip(scs, ids):
+        v = b.read(sid)
+        pos, vel = alone(s, steps)
+        assert np.array_equal(v["position"][: s.n], pos), s.name
+        assert np.array_equal(v["velocity"][: s.n], vel), s.name
+        assert b.status(sid) == 0
+    b.close()
+
+
+def test_batch_matches_oracle():
+    scs = mix(seed=10)
+    steps = 10
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    orcs = []
+    for s in scs:
+        ps = Batch.host_store(s)
+        from sph import bindings as bnd
+        o = oracle_of(bnd.store_views(ps))
+        if s.material != "fluid":
+            o.setup_solid()
+        orcs.append((o, ps))
+    b.step(steps)
+    for s, sid, (o, ps) in zip(scs, ids, orcs):
+        o.run(s.material, steps)
+        v = b.read(sid)
+        assert rel_err(v["position"][: s.n], o.a["position"][: s.n]) <= 1e-5, s.name
+        assert np.array_equal(v["num_neighbours"][: s.n], o.a["num_neighbours"][: s.n]), s.name
+    b.close()
+
+
+def test_scenes_join_and_leave_while_others_run():
+    a, c, f2, s1 = mix(seed=20)
+    b = Batch()
+    ia = b.add(a)
+    ic = b.add(c)
+    b.step(5)
+    i2 = b.add(f2)          # joins after 5 substeps
+    b.step(4)
+    b.remove(ia)            # leaves after 9
+    is1 = b.add(s1)         # joins after 9
+    b.step(3)
+    assert np.array_equal(b.read(ic)["position"][: c.n], alone(c, 12)[0])
+    assert np.array_equal(b.read(i2)["position"][: f2.n], alone(f2, 7)[0])
+    assert np.array_equal(b.read(is1)["position"][: s1.n], alone(s1, 3)[0])
+    b.close()
+
+
+@pytest.mark.parametrize("shape", [(128, 64, 0), (512, 256, 304), (256, 128, 152)])
+def test_launch_shape_does_not_change_results(shape):
+    scs = mix(seed=30)
+    ref = Batch()
+    ids = [ref.add(s) for s in scs]
+    ref.step(6)
+    want = [np.array(ref.read(i)["position"]) for i in ids]
+    ref.close()
+    b = Batch()
+    b.tune(*shape)
+    ids = [b.add(s) for s in scs]
+    b.step(6)
+    for i, w in zip(ids, want):
+        assert np.array_equal(b.read(i)["position"], w)
+    b.close()
+
+
+def test_served_results_equal_alone():
+    def make(rng, i):
+        kind = i % 3
+        if kind == 0:
+            return scenes.wcsph_block(int(rng.integers(6, 11)), 6, int(rng.integers(6, 11)), seed=i, name="r%d" % i)
+        mat = "corot" if kind == 1 else "svk"
+        return scenes.solid_lattice(5, 5, int(rng.integers(6, 10)), material=mat, seed=i, clamp_layers=1,
+                                    name="r%d" % i)
+    reqs = poisson_requests(rate=200.0, duration=0.06, make_scene=make, steps_range=(3, 17), seed=4)
+    assert len(reqs) >= 6
+    srv = Server(budget_bytes=40e6, max_chunk=4)
+    stats = srv.run(reqs, realtime=False)
+    assert stats["requests"] == len(reqs) and stats["p99_s"] >= stats["p50_s"] > 0
+    for r in reqs:
+        pos, vel = alone(r.scene, r.steps)
+        assert np.array_equal(r.result["position"], pos), r.scene.name
+        assert np.array_equal(r.result["velocity"], vel), r.scene.name
+    release(reqs)

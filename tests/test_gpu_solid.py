@@ -3,10 +3,11 @@ planes, plane constraints and kinematic bodies.
 
 Kernels are compared one at a time on identical inputs (the oracle's
 fields are uploaded first), then whole trajectories.  Tolerances, relative
-to the largest magnitude of the compared field:
-  - rotation R (GPU polar decomposition in FP64, oracle in FP32): 1e-4;
-  - strain, deformation, stress, forces: 1e-3 (small differences of
-    nearly equal neighbour sums);
+to the largest magnitude of the compared field (measured errors on a
+GB300 are 2-5x below them):
+  - rotation R (GPU polar decomposition in FP64, oracle in FP32),
+    deformation, stress, forces: 2e-5;
+  - strain (a small difference of nearly equal neighbour sums): 5e-5;
   - positions after N substeps: relative L2 error 1e-5.
 Neighbour counts stay bit-exact.
 """
@@ -88,22 +89,22 @@ def test_solid_kernels(material, planes):
     ps.sync_device_to_host()
     if material == "corot":
         soft = ps.get_fields("body_number")[0][:n] == 0
-        assert max_rel(ps.get_fields("rotation")[0][:n][soft], orc.a["rotation"][:n][soft]) <= 1e-4
-        assert max_rel(ps.get_fields("strain")[0][:n][soft], orc.a["strain"][:n][soft]) <= 1e-3
+        assert max_rel(ps.get_fields("rotation")[0][:n][soft], orc.a["rotation"][:n][soft]) <= 2e-5
+        assert max_rel(ps.get_fields("strain")[0][:n][soft], orc.a["strain"][:n][soft]) <= 5e-5
     else:
-        assert max_rel(ps.get_fields("deformation")[0][:n], orc.a["deformation"][:n]) <= 1e-3
+        assert max_rel(ps.get_fields("deformation")[0][:n], orc.a["deformation"][:n]) <= 2e-5
     _upload(ps, orc)
     ps.call_for_all_particles("compute_stresses")
     orc.call(k2)
     ps.sync_device_to_host()
-    assert max_rel(ps.get_fields("stress")[0][:n], orc.a["stress"][:n]) <= 1e-4
+    assert max_rel(ps.get_fields("stress")[0][:n], orc.a["stress"][:n]) <= 2e-5
     _upload(ps, orc)
     ps.compute_particle_bins()
     ps.call_for_all_particles("compute_forces_solids")
     orc.call(k3)
     ps.sync_device_to_host()
     for f in ["force", "force_elastic", "force_viscous", "cutoff_force"]:
-        assert max_rel(ps.get_fields(f)[0][:n], orc.a[f][:n]) <= 1e-3, f
+        assert max_rel(ps.get_fields(f)[0][:n], orc.a[f][:n]) <= 2e-5, f
     ps.close()
 
 

@@ -67,7 +67,7 @@ def test_oracle_reproduces_reference_kernels(case, prec):
     if prec == "f64":
         spec = spec.replace("| float", "| double")
     solid = mat != "fluid"
-    orc = OracleScene(fields_of(g, prec, "init", spec), prec, jacobi_guard=0)
+    orc = OracleScene(fields_of(g, prec, "init", spec), prec, guards=0)
     n = orc.n
     if solid:
         orc.setup_solid()
@@ -98,7 +98,7 @@ def test_oracle_bodies_and_constraints(prec):
     spec = str(g["spec"])
     if prec == "f64":
         spec = spec.replace("| float", "| double")
-    orc = OracleScene(fields_of(g, prec, "body_init", spec), prec, jacobi_guard=0)
+    orc = OracleScene(fields_of(g, prec, "body_init", spec), prec, guards=0)
     orc.set_body_position(0, [0.02, 0.0, 0.05])
     for f in ("position", "velocity", "body_position"):
         check(orc.a[f], g["%s/set_body_position/%s" % (prec, f)].reshape(orc.a[f].shape), "set_body_position " + f)
@@ -167,7 +167,7 @@ def test_oracle_matches_compiled_reference_live():
         pytest.skip("oracle/_ref not built on this machine")
     sc = scenes.wcsph_block(9, 8, 7, jitter=3e-3, seed=21, walls=False)
     ps, v = host_store(sc)
-    orc = OracleScene(v, "f32", jacobi_guard=0)
+    orc = OracleScene(v, "f32", guards=0)
     rs = ref.RefStore(sc.spec)
     for k in ("position", "n"):
         rs.view(k)[...] = v[k]
@@ -179,4 +179,18 @@ def test_oracle_matches_compiled_reference_live():
     for k in ("position", "velocity", "density", "num_neighbours", "cellparticles"):
         assert np.array_equal(rs.view(k)[: sc.n], orc.a[k][: sc.n].reshape(rs.view(k)[: sc.n].shape)), k
     rs.free()
+    free_data_cpu(ps)
+
+
+def test_zero_distance_guard():
+    sc = scenes.wcsph_block(5, 5, 5, jitter=1e-4, seed=2, walls=False)
+    pos = sc.init["position"].copy()
+    pos[10] = pos[11]
+    ps, v = host_store(sc, position=pos)
+    for guards, finite in ((3, True), (0, False)):
+        orc = OracleScene(v, "f32", guards=guards)
+        orc.call("compute_particle_bins")
+        orc.call("compute_density")
+        orc.call("compute_forces_fluids")
+        assert np.isfinite(orc.a["force"][: sc.n]).all() == finite
     free_data_cpu(ps)
