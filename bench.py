@@ -69,10 +69,16 @@ def workload(name, seed):
     from sph import scenes
     if name == "wcsph-1m":
         # 1,048,576 particles (the configuration's count; a 128^3 lattice
-        # would hold 2,097,152) as a 128 x 64 x 128 slab, 64 layers high
+        # would hold 2,097,152) as a 128 x 64 x 128 slab, 64 layers high.
+        # The reference's fluid force omits the neighbour mass
+        # (fluids.cl:43-56), so stiffness and viscosity act per unit particle
+        # mass: at 1/8 of the dam break's particle mass they are scaled by
+        # 1/8 to keep its sound speed and viscous time (unscaled, the slab
+        # blows up within ten substeps).
         return scenes.wcsph_block(128, 64, 128, spacing=0.005, h=0.01, box=(0.0, 1.0), jitter=5e-5, seed=seed,
-                                  dt=2e-5, walls=True, name="wcsph-1m"), \
-            "1,048,576-particle WCSPH slab, 128x64x128 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s"
+                                  dt=2e-5, walls=True, stiffness=0.375, viscosity=0.025, name="wcsph-1m"), \
+            ("1,048,576-particle WCSPH slab, 128x64x128 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s, "
+             "stiffness 0.375, viscosity 0.025 (the dam break's 3 and 0.2 scaled by the 1/8 particle mass)")
     if name == "dam-8k":
         return scenes.wcsph_block(20, 20, 20, seed=seed, name="dam-8k"), \
             "8,000-particle WCSPH dam break, 20^3 at 0.01 m, h=0.02 m, [0,0.4]^3 box, dt=1e-4 s"

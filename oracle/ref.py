@@ -80,11 +80,22 @@ def layout(ps):
 
 
 class RefStore(object):
-    """A store built by the reference's own builder, with NumPy views."""
+    """A store built by the reference's own builder, with NumPy views.
+
+    Where libref_psdata.so was not built (a machine without the reference
+    checkout), the product's builder makes the store instead; its layout is
+    pinned to the reference builder's by tests/test_psdata.py."""
 
     def __init__(self, spec):
         self.ps = psdata()
-        psdata_lib().build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
+        self._own = available("psdata")
+        if self._own:
+            psdata_lib().build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
+        else:
+            from sph import bindings as bnd
+            lib = bnd.library
+            lib.build_psdata_from_string.argtypes = [POINTER(psdata), c_char_p]
+            lib.build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
         self.layout = layout(self.ps)
         self.size = self.layout["data_offsets"][-1] + self.layout["data_sizes"][-1]
 
@@ -112,7 +123,12 @@ class RefStore(object):
 
     def free(self):
         if self.ps.num_fields:
-            psdata_lib().free_psdata(ctypes.byref(self.ps))
+            if self._own:
+                psdata_lib().free_psdata(ctypes.byref(self.ps))
+            else:
+                from sph import bindings as bnd
+                bnd.library.free_psdata.argtypes = [POINTER(psdata)]
+                bnd.library.free_psdata(ctypes.byref(self.ps))
             self.ps.num_fields = 0
 
 
