@@ -247,6 +247,29 @@ unsigned int sph_batch_kernel_count(sph_batch *batch);
 void *sph_batch_stream(sph_batch *batch);
 unsigned int sph_batch_status(sph_batch *batch, int id);
 
+/* ---- NEW: neighbour grid without allocation -------------------------------
+ * No counterpart in the reference.  compute_particle_bins for callers that
+ * cannot allocate device memory (inside a CUDA graph capture, in an engine
+ * that owns all device memory through its own pool, or in a real-time loop
+ * that cannot afford cudaMalloc's implicit synchronisation).  The caller
+ * passes device buffers: positions (AoS float[3] x n), gridbounds (6
+ * floats), and the outputs gridcell[n], gridcount[rx*ry*rz],
+ * celloffset[rx*ry*rz], cellparticles[n], with the meanings and layout of
+ * the store fields of the same names.  The scratch is a fixed file-scope
+ * device array (about 12.3 MB, held by every GPU that loads the library),
+ * so n <= SPH_NOALLOC_MAX_PARTICLES and rx*ry*rz <= SPH_NOALLOC_MAX_CELLS;
+ * larger sizes return -1 with an error message.  The call allocates
+ * nothing, enqueues on `stream` (a cudaStream_t, NULL for the default
+ * stream) and returns 0.  Calls share the array: calls that overlap on the
+ * GPU race, so order them on one stream.  The first call on a device looks
+ * up the array's address; make it before any stream capture. */
+#define SPH_NOALLOC_MAX_PARTICLES (1u << 20)
+#define SPH_NOALLOC_MAX_CELLS (1u << 22)
+int sph_compute_particle_bins_noalloc(const float *position, unsigned int n, const float *gridbounds,
+                                      unsigned int rx, unsigned int ry, unsigned int rz,
+                                      unsigned int *gridcell, unsigned int *gridcount,
+                                      unsigned int *celloffset, unsigned int *cellparticles, void *stream);
+
 /* Library and device description (static string). */
 const char *sph_version(void);
 

@@ -20,6 +20,7 @@ def declared_functions():
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
         text = re.sub(r"//[^\n]*", " ", text)
+        text = re.sub(r"^\s*#[^\n]*", " ", text, flags=re.M)
         text = re.sub(r"typedef\s+struct\s*\{.*?\}\s*\w+\s*;", " ", text, flags=re.S)
         text = re.sub(r"typedef[^;]*;", " ", text)
         for m in re.finditer(r"([A-Za-z_]\w*)\s*\(([^;{}]*)\)\s*;", text):
