@@ -62,6 +62,11 @@ PHASE_BYTES = {
     "stresses": (48, 0),
     "forces_solids": (160, 8),
     "step_forward": (76, 0),
+    # batched-form phases (bench_batched): the same figures per material
+    "bins": (44, 20),                 # find/count/insert 44 per particle; zero, scan, copy per cell
+    "fluid forces+step": (120, 8),
+    "corotational passes": (452, 24), # rotations_and_strains 168 + stresses 48 + forces 160 + step 76
+    "svk passes": (324, 16),          # deformations 64 + stresses 60 + forces 124 + step 76
 }
 
 
@@ -82,10 +87,27 @@ def workload(name, seed):
     if name == "dam-8k":
         return scenes.wcsph_block(20, 20, 20, seed=seed, name="dam-8k"), \
             "8,000-particle WCSPH dam break, 20^3 at 0.01 m, h=0.02 m, [0,0.4]^3 box, dt=1e-4 s"
+    if name == "batched-256":
+        raise SystemExit("batched-256 has no single scene")
     if name == "beam-4k":
         return scenes.solid_lattice(10, 10, 40, material="corot", seed=seed, name="beam-4k"), \
             "4,000-particle corotational beam 10x10x40 at 0.01 m, E=1e5 Pa, nu=0.3, 2 clamped layers, dt=5e-5 s"
     raise SystemExit("unknown workload " + name)
+
+
+def aggregate_replicas(n_local, steps, seconds_local, world, device="cpu"):
+    """Whole-job throughput of independent replicas: every rank's particles
+    times the substeps, over the slowest rank's time.  Returns (value,
+    max_seconds); needs an initialised process group when world > 1."""
+    if world <= 1:
+        return n_local * steps / seconds_local, seconds_local
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds_local], dtype=torch.float64, device=device)
+    n = torch.tensor([float(n_local)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) * steps / float(t.item()), float(t.item())
 
 
 def dist_env():
@@ -153,27 +175,28 @@ def measured_peak_gbs():
         return 6800.0, "fallback"
 
 
-def setup_store(scene):
-    ps = scene.system()
-    if scene.material in ("corot", "svk"):
-        ps.setup()
-    return ps
-
-
 def _solid_setup(ps):
     ps.call_for_all_particles("init_original_position")
     ps.compute_particle_bins()
     ps.call_for_all_particles("compute_original_density")
 
 
-def run_ours(args, rank, world, local_rank):
-    import torch
-    torch.cuda.set_device(local_rank)
+def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None):
+    """Roofline of the phase that takes longest: its algorithmic bytes (for
+    the particles and cells it processes) over its measured time."""
+    dom = max(phases, key=phases.get)
+    bp, bc = PHASE_BYTES.get(dom, (0, 0))
+    pn, pc = (counts or {}).get(dom, (n, cells))
+    alg = bp * pn + bc * pc
+    achieved = alg / (phases[dom] * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "algorithmic_bytes_per_launch": alg, "phase_ms": phases}
+
+
+def bench_plain(args, scene, torch, world):
+    """The drop-in path on one scene: K CUDA-graph substeps (sph_update)."""
     from sph import bindings as bnd
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    scene, desc = workload(args.workload, args.seed + rank)
     ps = scene.system()
     if scene.material in ("corot", "svk"):
         _solid_setup(ps)
@@ -181,12 +204,9 @@ def run_ours(args, rank, world, local_rank):
     cells = int(np.prod(ps.get_fields("gridres")[0]))
     ext = torch.cuda.ExternalStream(bnd.sph_stream(ps.psdata_opencl))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    # warm-up (also captures the CUDA graph)
     ps.update_fused(max(args.warmup, 1))
     ps.synchronize()
     kernels_per_step = bnd.sph_graph_kernel_count(ps.psdata_opencl)
-
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     clocks = Clocks(torch.cuda.current_device())
@@ -194,7 +214,6 @@ def run_ours(args, rank, world, local_rank):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    t0 = time.perf_counter()
     with torch.cuda.stream(ext):
         for k in range(args.steps):
             flush.zero_()
@@ -202,71 +221,20 @@ def run_ours(args, rank, world, local_rank):
             ps.update_fused(1)
             ends[k].record(ext)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_s = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s = float(t.item())
-    status = ps.status()
-
-    # live per-phase device times of the same kernels (roofline)
+    total_s = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / 1e3
     maxp = 16
     ms = (ctypes.c_float * maxp)()
     names = (ctypes.c_char_p * maxp)()
-    np_ = bnd.sph_profile_substep(ps.psdata_opencl, max(3, min(args.steps, 10)), ms, names, maxp)
-    phases = {names[i].decode(): float(ms[i]) for i in range(np_)}
-
-    # end to end through the C ABI with host buffers (pinned host store)
+    k = bnd.sph_profile_substep(ps.psdata_opencl, max(3, min(args.steps, 10)), ms, names, maxp)
+    phases = {names[i].decode(): float(ms[i]) for i in range(k)}
     e2e = run_e2e(ps, scene, args.steps, torch)
-
-    line = None
-    if rank == 0:
-        peak, peak_kind = measured_peak_gbs()
-        dom = max(phases, key=phases.get)
-        bp, bc = PHASE_BYTES.get(dom, (0, 0))
-        alg_bytes = bp * n + bc * cells
-        achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9
-        step_alg = 0
-        for ph in phases:
-            b = PHASE_BYTES.get(ph, (0, 0))
-            step_alg += b[0] * n + b[1] * cells
-        value = n * args.steps * world / total_s
-        line = {
-            "metric": METRIC,
-            "value": value,
-            "unit": UNIT,
-            "n_gpus": world,
-            "steps": args.steps,
-            "warmup": args.warmup,
-            "ms_per_step": total_s * 1e3 / args.steps,
-            "higher_is_better": True,
-            "scaling": "weak",
-            "vs_baseline": None,
-            "dtype": "f32",
-            "data": "synthetic (seeded lattice scene, seed %d)" % args.seed,
-            "config": {"workload": args.workload + ": " + desc, "particles": n, "cells": cells,
-                       "path": "plain single scene, one CUDA-graph substep per step (sph_update)",
-                       "l2": "flushed between timed steps (256 MB write, outside the timed events)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "clocks": clk,
-            "e2e": e2e,
-            "gpu_launches": kernels_per_step * args.steps,
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
-                         else "fallback", "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         "step_algorithmic_gbs": step_alg / (sum(phases.values()) * 1e-3) / 1e9,
-                         "phase_ms": phases},
-            "wall_s": wall,
-            "status_word": status,
-        }
+    status = ps.status()
     ps.close()
-    return line
+    return {"n": n, "cells": cells, "total_s": total_s, "clocks": clk, "phases": phases, "e2e": e2e,
+            "status": status, "kernels_per_step": kernels_per_step}
 
 
 def run_e2e(ps, scene, steps, torch):
@@ -279,10 +247,9 @@ def run_e2e(ps, scene, steps, torch):
         registered = int(cudart.cudaHostRegister(ps.psdata.data, size, 0)) == 0
     except Exception:
         registered = False
-    names_in = ("gravity", "timestep")
     t0 = time.perf_counter()
     for _ in range(steps):
-        ps.sync_fields_host_to_device(*names_in)
+        ps.sync_fields_host_to_device("gravity", "timestep")
         ps.update_fused(1)
         ps.sync_fields_device_to_host("position")
     el = time.perf_counter() - t0
@@ -290,6 +257,190 @@ def run_e2e(ps, scene, steps, torch):
         cudart.cudaHostUnregister(ps.psdata.data)
     return {"value": scene.n * steps / el, "unit": UNIT, "h2d_bytes_per_step": 12 + 4,
             "d2h_bytes_per_step": 12 * scene.n, "host_memory": "pinned" if registered else "pageable"}
+
+
+def batched_scenes(seed):
+    from sph import scenes
+    return scenes.batch_mix(256, seed=seed)
+
+
+def bench_batched(args, torch, world):
+    """256 uneven scenes (60% WCSPH, 25% corotational, 15% SVK) advanced
+    together: one CUDA graph per substep over all scenes."""
+    from sph.batch import Batch
+    from sph import autotune
+    scs = batched_scenes(args.seed)
+    tuned = None
+    if not args.quick:
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        cands = [(b_, p_, c_) for b_ in (128, 256) for p_ in (64, 128, 256) for c_ in (0, 4 * sms, 8 * sms)]
+        best, best_s, table = autotune.tune(scs, steps=3, cands=cands)
+        default_s = dict(table).get((256, 128, 0))
+        tuned = {"block": best[0], "pair_block": best[1], "grid_cap": best[2], "candidates": len(table),
+                 "best_ms_per_step": best_s * 1e3,
+                 "default_ms_per_step": default_s * 1e3 if default_s else None}
+    b = Batch()
+    if tuned:
+        b.tune(tuned["block"], tuned["pair_block"], tuned["grid_cap"])
+    ids = [b.add(s) for s in scs]
+    n = sum(s.n for s in scs)
+    ext = torch.cuda.ExternalStream(b.stream)
+    b.step(max(args.warmup, 1))
+    b.synchronize()
+    kernels_per_step = b.kernels_per_step
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = Clocks(torch.cuda.current_device())
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(ext):
+        for k in range(args.steps):
+            starts[k].record(ext)
+            b.step(1)
+            ends[k].record(ext)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    total_s = sum(a.elapsed_time(e) for a, e in zip(starts, ends)) / 1e3
+    phases = b.profile(reps=max(3, min(args.steps, 10)))
+    # end to end: per step, one batched substep and every scene's positions
+    # downloaded into its host store
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b.step(1)
+        for sid in ids:
+            b.read_field(sid, "position")
+    e2e_s = time.perf_counter() - t0
+    status = sum(1 for sid in ids if b.status(sid) != 0)
+    cells = 0
+    by_mat = {"fluid": [0, 0], "corot": [0, 0], "svk": [0, 0]}
+    for sid in ids:
+        c = int(np.prod(b.scenes[sid].views["gridres"]))
+        cells += c
+        m = b.scenes[sid].scene.material
+        by_mat[m][0] += b.scenes[sid].scene.n
+        by_mat[m][1] += c
+    counts = {"fluid forces+step": tuple(by_mat["fluid"]), "corotational passes": tuple(by_mat["corot"]),
+              "svk passes": tuple(by_mat["svk"])}
+    b.close()
+    return {"scenes": scs, "n": n, "cells": cells, "counts": counts, "total_s": total_s, "clocks": clk,
+            "phases": phases, "tuned": tuned,
+            "kernels_per_step": kernels_per_step, "status_scenes": status,
+            "e2e": {"value": n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 12 * n, "host_memory": "pageable"}}
+
+
+def bench_plain_loop(scs, steps):
+    """The plain per-scene loop: each scene through the drop-in path, one
+    sph_update substep at a time, scene after scene, waiting for each as the
+    reference's blocking calls do."""
+    systems = []
+    for s in scs:
+        ps = s.system()
+        if s.material in ("corot", "svk"):
+            _solid_setup(ps)
+        ps.update_fused(1)
+        ps.synchronize()
+        systems.append(ps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for ps in systems:
+            ps.update_fused(1)
+            ps.synchronize()
+    el = time.perf_counter() - t0
+    for ps in systems:
+        ps.close()
+    n = sum(s.n for s in scs)
+    return {"value": n * steps / el, "unit": UNIT, "s": el}
+
+
+def plain_step_model(sizes, steps=20):
+    """Measured seconds per drop-in substep for WCSPH scenes of given sizes
+    (for the sequential-server model); returns a log-log interpolator."""
+    from sph import scenes
+    pts = []
+    for n_target in sizes:
+        d = max(2, int(round((n_target / 0.5) ** (1 / 3))))
+        sc = scenes.wcsph_block(d, max(2, d // 2), d, seed=1)
+        ps = sc.system()
+        ps.update_fused(2)
+        ps.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ps.update_fused(1)
+            ps.synchronize()
+        pts.append((sc.n, (time.perf_counter() - t0) / steps))
+        ps.close()
+    xs = np.log([p[0] for p in pts])
+    ys = np.log([p[1] for p in pts])
+    return lambda n: float(np.exp(np.interp(np.log(n), xs, ys)))
+
+
+def bench_served(args):
+    """Poisson arrivals at 50 requests/s; each request a scene of the batched
+    mix with 2,000-262,144 particles (log-uniform) and 100-2,000 substeps
+    (uniform); continuous batching under a 150 GB budget."""
+    import math
+    from sph import scenes
+    from sph.serving import Server, poisson_requests, release, sequential_fifo
+
+    def make(rng, i):
+        n_target = math.exp(rng.uniform(math.log(2000), math.log(262144)))
+        kind = rng.choice(3, p=[0.6, 0.25, 0.15])
+        if kind == 0:
+            d = max(2, int(round((n_target / 0.5) ** (1 / 3))))
+            return scenes.wcsph_block(d, max(2, d // 2), d, seed=i, name="q%d" % i)
+        d = max(2, int(round((n_target / 2.0) ** (1 / 3))))
+        return scenes.solid_lattice(d, d, 2 * d, material="corot" if kind == 1 else "svk",
+                                    youngs_modulus=math.exp(rng.uniform(math.log(1e4), math.log(1e6))),
+                                    poisson=rng.uniform(0.25, 0.45), jitter=1e-4, seed=i, clamp_layers=1,
+                                    name="q%d" % i)
+    reqs = poisson_requests(rate=50.0, duration=args.served_seconds, make_scene=make, steps_range=(100, 2000),
+                            seed=args.seed)
+    srv = Server(budget_bytes=150e9, max_chunk=50, keep_results=False)
+    srv.prepare(reqs)
+    st = srv.run(reqs, realtime=True)
+    model = plain_step_model([2000, 16000, 131072, 262144])
+    seq = sequential_fifo(reqs, lambda r: r.steps * model(r.scene.n))
+    release(reqs)
+    return {"requests": st["requests"], "arrival_rate_per_s": 50.0, "window_s": args.served_seconds,
+            "throughput": st["throughput"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
+            "makespan_s": st["makespan_s"], "peak_resident": st["peak_resident"],
+            "sequential_plain_model": {"throughput": seq["throughput"], "p50_s": seq["p50_s"],
+                                       "p99_s": seq["p99_s"],
+                                       "how": "FIFO queue of one-at-a-time drop-in solves, per-substep times "
+                                              "measured on this GPU at 2k-262k particles"}}
+
+
+def fp64_error_sample(scs, steps):
+    """Relative L2 position error of batched FP32 results against the
+    all-FP64 oracle run, on the smallest scene of each material."""
+    from sph.batch import Batch
+    from sph import bindings as bnd
+    from oracle.oracle import OracleScene
+    picks = {}
+    for s in sorted(scs, key=lambda s: s.n):
+        picks.setdefault(s.material, s)
+    out = {}
+    b = Batch()
+    ids = {m: b.add(s) for m, s in picks.items()}
+    b.step(steps)
+    for m, s in picks.items():
+        host = Batch.host_store(s)
+        o = OracleScene(bnd.store_views(host), "f64", nthreads=os.cpu_count() or 1)
+        if m != "fluid":
+            o.setup_solid()
+        o.run(m, steps)
+        p = b.read(ids[m])["position"][: s.n].astype(np.float64)
+        q = o.a["position"][: s.n]
+        out[m] = {"scene": s.name, "particles": s.n, "rel_l2": float(np.linalg.norm(p - q) / np.linalg.norm(q))}
+        from sph import free_data_cpu
+        free_data_cpu(host)
+    b.close()
+    return {"substeps": steps, "per_material": out}
 
 
 def cpu_sample(scene, material, steps, nthreads, reference):
@@ -326,6 +477,7 @@ def cpu_sample(scene, material, steps, nthreads, reference):
         if material != "fluid":
             for k in ("init_original_position", "compute_particle_bins", "compute_original_density"):
                 rs.call(prog, "f32", k, scene.n, nthreads)
+        closer = rs.free
     else:
         from oracle.oracle import OracleScene
         orc = OracleScene(v, "f32", nthreads=nthreads)
@@ -334,23 +486,107 @@ def cpu_sample(scene, material, steps, nthreads, reference):
 
         def one():
             orc.substep(material)
+        closer = None
     one()  # warm
     t0 = time.perf_counter()
     for _ in range(steps):
         one()
     el = time.perf_counter() - t0
+    if closer:
+        closer()
     free_data_cpu(ps)
-    return scene.n * steps / el, kind, el
+    return scene.n * steps, el, kind
+
+
+def cpu_workload(name, seed, budget_scenes=None):
+    if name == "batched-256":
+        scs = batched_scenes(seed)
+        return scs if budget_scenes is None else scs[:budget_scenes]
+    return [workload(name, seed)[0]]
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    peak, peak_kind = measured_peak_gbs()
+    peak_kind = "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"
+    extra = {}
+    if args.workload == "batched-256":
+        r = bench_batched(args, torch, world)
+        desc = ("256 independent scenes, 60% WCSPH / 25% corotational / 15% SVK, particle counts log-uniform "
+                "in [1,000, 65,536], E log-uniform [1e4, 1e6] Pa, Poisson uniform [0.25, 0.45], 0.01 m "
+                "spacing, h=0.02 m, seeded jitter; one CUDA graph per substep over all scenes")
+        t = r.get("tuned")
+        path = ("batched form (sph_batch_step); launch shape chosen by sph.autotune: block %d, pair block %d, "
+                "grid cap %d" % (t["block"], t["pair_block"], t["grid_cap"]) if t else
+                "batched form (sph_batch_step), launch shape: block 256, pair block 128, no grid cap")
+        if t:
+            extra["autotune"] = t
+        l2 = "working set %.2f GB > L2 (129 MB); no flush needed" % (r["n"] * 300e-9)
+        if rank == 0 and not args.quick:
+            pl = bench_plain_loop(r["scenes"], max(3, args.steps // 4))
+            extra["plain_per_scene"] = {"value": pl["value"], "unit": UNIT,
+                                        "how": "same 256 scenes through the drop-in path, one sph_update "
+                                               "substep per scene per step, waiting for each"}
+            extra["batched_vs_plain"] = (r["n"] * args.steps / r["total_s"]) / pl["value"]
+            extra["fp64_error"] = fp64_error_sample(r["scenes"], 100)
+            extra["served"] = bench_served(args)
+            sc1m, d1m = workload("wcsph-1m", args.seed)
+            p1 = bench_plain(args, sc1m, torch, 1)
+            extra["plain_1m"] = {"workload": "wcsph-1m: " + d1m, "value": p1["n"] * args.steps / p1["total_s"],
+                                 "ms_per_step": p1["total_s"] * 1e3 / args.steps,
+                                 "roofline": _phase_roofline(p1["phases"], p1["n"], p1["cells"], peak, peak_kind),
+                                 "e2e": p1["e2e"]}
+    else:
+        scene, desc = workload(args.workload, args.seed + rank)
+        r = bench_plain(args, scene, torch, world)
+        path = "plain single scene, one CUDA-graph substep per step (sph_update)"
+        l2 = "flushed between timed steps (256 MB write, outside the timed events)"
+    value, total_s = aggregate_replicas(r["n"], args.steps, r["total_s"], world, device="cuda")
+    if rank != 0:
+        return None
+    n = r["n"]
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_s * 1e3 / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded lattice scenes, seed %d)" % args.seed,
+        "config": {"workload": args.workload + ": " + desc, "particles": n, "cells": r["cells"], "path": path,
+                   "l2": l2, "parallelism": "replicas" if world > 1 else "single GPU"},
+        "clocks": r["clocks"],
+        "e2e": r["e2e"],
+        "gpu_launches": r["kernels_per_step"] * args.steps,
+        "roofline": _phase_roofline(r["phases"], n, r["cells"], peak, peak_kind, r.get("counts")),
+    }
+    line.update(extra)
+    return line
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    scene, desc = workload(args.workload, args.seed)
+    scs = cpu_workload(args.workload, args.seed)
     nthreads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        pass
-    value, kind, el = cpu_sample(scene, scene.material, args.steps, nthreads, reference=True)
+    work = 0
+    el = 0.0
+    kind = "port"
+    for s in scs:
+        w, e, kind = cpu_sample(s, s.material, args.steps, nthreads, reference=True)
+        work += w
+        el += e
+    value = work / el
+    desc = args.workload
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -364,10 +600,10 @@ def run_reference(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic (seeded lattice scene, seed %d)" % args.seed,
-        "config": {"workload": args.workload + ": " + desc, "particles": scene.n},
+        "data": "synthetic (seeded lattice scenes, seed %d)" % args.seed,
+        "config": {"workload": desc, "particles": sum(s.n for s in scs), "scenes": len(scs)},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": "%d full substeps of the workload" % args.steps},
+                         "sample": "%d full substeps of every scene of the workload" % args.steps},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -377,11 +613,14 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--workload", default="wcsph-1m")
+    ap.add_argument("--workload", default="batched-256",
+                    choices=["batched-256", "wcsph-1m", "dam-8k", "beam-4k"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=3, help="substeps in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip the plain loop, served, FP64 and 1M extras")
+    ap.add_argument("--served-seconds", type=float, default=8.0, help="arrival window of the served stream")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -394,12 +633,16 @@ def main():
     line = run_ours(args, rank, world, local_rank)
     if line is not None:
         if world == 1 and not args.no_cpu_baseline:
-            scene, _ = workload(args.workload, args.seed)
             nthreads = os.cpu_count() or 1
-            v, kind, el = cpu_sample(scene, scene.material, args.cpu_steps, nthreads, reference=False)
-            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": kind,
-                                    "sample": "%d substeps of the full workload on the C oracle (%.1f s)"
-                                              % (args.cpu_steps, el)}
+            scs = cpu_workload(args.workload, args.seed)
+            work, el = 0, 0.0
+            for s in scs:
+                w, e, kind = cpu_sample(s, s.material, args.cpu_steps, nthreads, reference=False)
+                work += w
+                el += e
+            line["cpu_baseline"] = {"value": work / el, "unit": UNIT, "cores": nthreads, "kind": "port",
+                                    "sample": "%d substeps of every scene of the workload on the C oracle "
+                                              "(%.1f s)" % (args.cpu_steps, el)}
         print(json.dumps(line), flush=True)
     return 0
 

@@ -236,12 +236,20 @@ int sph_batch_remove(sph_batch *batch, int id);
 int sph_batch_step(sph_batch *batch, unsigned int num_steps);
 /* Copies a scene's device store into `out` (same layout as when added). */
 int sph_batch_read(sph_batch *batch, int id, psdata *out);
+/* Copies one named field of a scene into the same field of `out`. */
+int sph_batch_read_field(sph_batch *batch, int id, const char *field, psdata *out);
+/* Runs `reps` substeps of the batch as individual launches with CUDA events
+ * between phases (material branches one after another) and writes each
+ * phase's mean device time in ms and its name; returns the phase count. */
+int sph_batch_profile(sph_batch *batch, unsigned int reps, float *phase_ms, const char **phase_names,
+                      unsigned int max_phases);
 int sph_batch_synchronize(sph_batch *batch);
 /* Device bytes held by the batch's scenes and tables. */
 size_t sph_batch_bytes(sph_batch *batch);
 unsigned int sph_batch_size(sph_batch *batch);
-/* Launch shape: threads per block for particle/cell kernels and for pair
- * kernels, and the persistent-grid cap (0: one block per work item). */
+/* Launch shape: threads per block for particle/cell kernels (32..1024) and
+ * for pair kernels (32..512), multiples of 32, and the persistent-grid cap
+ * (0: one block per work item). */
 int sph_batch_tune(sph_batch *batch, unsigned int block, unsigned int pair_block, unsigned int grid_cap);
 unsigned int sph_batch_kernel_count(sph_batch *batch);
 void *sph_batch_stream(sph_batch *batch);

@@ -191,14 +191,14 @@ bool rebuild(sph_batch *b) {
     if (!ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture")) return false;
     sph_launch_bins(A);
     sph_launch_gather(A, true, false);
-    sph_launch_density(A, false);
+    sph_launch_density(A, false, true);  // masks for the fluid scenes only
     cudaEventRecord(b->fork, b->stream);
     for (int m = 0; m < 3; ++m) {
         GroupLaunch &G = b->group[m];
         if (!G.present) continue;
         if (m > 0) cudaStreamWaitEvent(G.L.stream, b->fork, 0);
         if (m == MAT_FLUID) {
-            sph_launch_forces_fluids(G.L, true);
+            sph_launch_forces_fluids(G.L, true, true);
         } else {
             if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L);
             else sph_launch_deformations(G.L);
@@ -247,7 +247,8 @@ BatchScene *scene_of(sph_batch *b, int id, const char *what) {
 
 extern "C" sph_batch *sph_batch_create(void) {
     sph_batch *b = new sph_batch();
-    bool good = ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "sph_batch_create") &&
+    bool good = ok(sph_prepare_kernels(), "sph_batch_create") &&
+                ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "sph_batch_create") &&
                 ok(cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking), "sph_batch_create") &&
                 ok(cudaStreamCreateWithFlags(&b->side[1], cudaStreamNonBlocking), "sph_batch_create") &&
                 ok(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "sph_batch_create") &&
@@ -377,6 +378,92 @@ extern "C" int sph_batch_read(sph_batch *b, int id, psdata *out) {
     return 0;
 }
 
+extern "C" int sph_batch_read_field(sph_batch *b, int id, const char *field, psdata *out) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_read_field");
+    if (!sc) return -1;
+    int f = out && field ? get_field_psdata(*out, field) : -1;
+    if (f < 0 || psdata_data_size(*out) != sc->blob_size) {
+        sph_set_error("sph_batch_read_field: no field '%s' in a store of the scene's layout", field ? field : "");
+        return -1;
+    }
+    size_t off = out->data_offsets[f], sz = out->data_sizes[f];
+    if (!ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost, b->stream),
+            "sph_batch_read_field") ||
+        !ok(cudaStreamSynchronize(b->stream), "sph_batch_read_field"))
+        return -1;
+    return 0;
+}
+
+namespace {
+struct PhaseLog {
+    cudaStream_t stream;
+    std::vector<cudaEvent_t> events;
+    std::vector<const char *> names;
+    void mark(const char *name) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return;
+        cudaEventRecord(e, stream);
+        events.push_back(e);
+        names.push_back(name);
+    }
+};
+}  // namespace
+
+extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, const char **phase_names,
+                                 unsigned max_phases) {
+    if (!b) return -1;
+    if (b->dirty && !rebuild(b)) return -1;
+    if (!b->graph) return 0;
+    static const char *kMat[3] = {"fluid forces+step", "corotational passes", "svk passes"};
+    std::vector<double> acc;
+    std::vector<const char *> names;
+    for (unsigned r = 0; r < reps; ++r) {
+        PhaseLog log{b->stream};
+        Launch A = b->all;
+        log.mark("bins");
+        sph_launch_bins(A);
+        log.mark("gather");
+        sph_launch_gather(A, true, false);
+        log.mark("density");
+        sph_launch_density(A, false, true);
+        for (int m = 0; m < 3; ++m) {
+            if (!b->group[m].present) continue;
+            Launch G = b->group[m].L;
+            G.stream = b->stream;
+            log.mark(kMat[m]);
+            if (m == MAT_FLUID) {
+                sph_launch_forces_fluids(G, true, true);
+            } else {
+                if (m == MAT_COROT) sph_launch_rotations_and_strains(G);
+                else sph_launch_deformations(G);
+                sph_launch_stresses(G, m == MAT_COROT);
+                sph_launch_forces_solids(G, m == MAT_COROT);
+                sph_launch_step_forward(G);
+            }
+        }
+        log.mark(nullptr);
+        bool good = sph_check_launch("sph_batch_profile") == cudaSuccess &&
+                    ok(cudaStreamSynchronize(b->stream), "sph_batch_profile");
+        if (good && acc.empty()) {
+            acc.assign(log.events.size() - 1, 0.0);
+            names.assign(log.names.begin(), log.names.end() - 1);
+        }
+        for (size_t k = 0; good && k + 1 < log.events.size() && k < acc.size(); ++k) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, log.events[k], log.events[k + 1]);
+            acc[k] += ms;
+        }
+        for (cudaEvent_t e : log.events) cudaEventDestroy(e);
+        if (!good) return -1;
+    }
+    unsigned np = (unsigned)acc.size() < max_phases ? (unsigned)acc.size() : max_phases;
+    for (unsigned k = 0; k < np; ++k) {
+        phase_ms[k] = reps ? (float)(acc[k] / reps) : 0.f;
+        if (phase_names) phase_names[k] = names[k];
+    }
+    return (int)np;
+}
+
 extern "C" int sph_batch_synchronize(sph_batch *b) {
     if (!b) return -1;
     return ok(cudaStreamSynchronize(b->stream), "sph_batch_synchronize") ? 0 : -1;
@@ -393,9 +480,9 @@ extern "C" unsigned sph_batch_size(sph_batch *b) {
 
 extern "C" int sph_batch_tune(sph_batch *b, unsigned block, unsigned pair_block, unsigned grid_cap) {
     if (!b) return -1;
-    auto valid = [](unsigned t) { return t >= 32 && t <= 1024 && t % 32 == 0; };
-    if (!valid(block) || !valid(pair_block)) {
-        sph_set_error("sph_batch_tune: block sizes must be multiples of 32 in [32, 1024]");
+    auto valid = [](unsigned t, unsigned hi) { return t >= 32 && t <= hi && t % 32 == 0; };
+    if (!valid(block, 1024) || !valid(pair_block, 512)) {
+        sph_set_error("sph_batch_tune: block sizes must be multiples of 32, at most 1024 (512 for pair kernels)");
         return -1;
     }
     b->block = block;

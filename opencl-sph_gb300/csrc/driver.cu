@@ -137,7 +137,8 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     size_t o_sm = o_cm + Arena::align(maps.cells.size() * sizeof(BlockWork));
     size_t total = o_sm + Arena::align(maps.scan.size() * sizeof(BlockWork));
 
-    if (!cuda_ok(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
+    if (!cuda_ok(sph_prepare_kernels(), "kernel attributes") ||
+        !cuda_ok(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
         !cuda_ok(cudaMalloc(&s->arena.base, total), "cudaMalloc(store)")) {
         *err = sph_last_error();
         destroy(s);

@@ -12,6 +12,17 @@ static inline unsigned grid_for(const BlockMap &m, unsigned cap) {
     return g ? g : 1;
 }
 
+cudaError_t sph_prepare_kernels() {
+    // the staged density pass may use more than the default 48 KB of
+    // dynamic shared memory for large pair blocks
+    int dev = 0, max_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    size_t want = density_smem_bytes(1024, true);
+    if (max_optin > 0 && want > (size_t)max_optin) want = (size_t)max_optin;
+    return cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+}
+
 cudaError_t sph_check_launch(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) sph_set_error("%s: %s", what, cudaGetErrorString(e));
@@ -56,14 +67,19 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens) {
                                                                           dens ? 1 : 0);
 }
 
-void sph_launch_density(const Launch &L, bool original) {
-    k_density<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles,
-                                                                                      original ? 1 : 0);
+void sph_launch_density(const Launch &L, bool original, bool mask) {
+    const size_t smem = density_smem_bytes(L.pair_block, mask);
+    k_density<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, smem, L.stream>>>(
+        L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0);
 }
 
-void sph_launch_forces_fluids(const Launch &L, bool fuse_step) {
-    k_forces_fluids<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-        L.scenes, L.pair_particles, fuse_step ? 1 : 0);
+void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
+    if (masked)
+        k_forces_fluids_masked<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+            L.scenes, L.pair_particles, fuse_step ? 1 : 0);
+    else
+        k_forces_fluids<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+            L.scenes, L.pair_particles, fuse_step ? 1 : 0);
 }
 
 void sph_launch_step_forward(const Launch &L) {
@@ -135,7 +151,8 @@ void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az) 
 //           compute_forces_solids, step_forward (scripts/sph/systems.py:194-204)
 //   SVK solid: the same with compute_deformations (systems.py:225-235)
 // Positions do not move between the bins and the integrator, so the sorted
-// copies are gathered once; for fluids the integrator is fused into the
+// copies are gathered once, the force pass walks the candidate masks the
+// density pass recorded, and for fluids the integrator is fused into the
 // force pass.
 void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *ctx) {
     auto phase = [&](const char *name) {
@@ -151,10 +168,10 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     phase("gather");
     sph_launch_gather(L, mat == MAT_FLUID, false);
     phase("density");
-    sph_launch_density(L, false);
+    sph_launch_density(L, false, mat == MAT_FLUID);
     if (mat == MAT_FLUID) {
         phase("forces_fluids+step");
-        sph_launch_forces_fluids(L, true);
+        sph_launch_forces_fluids(L, true, true);
         phase(nullptr);
         return;
     }

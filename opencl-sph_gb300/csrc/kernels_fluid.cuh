@@ -15,46 +15,107 @@
 // (solids.cl:99-170): rho_i = m * sum_j W_poly6(|x_j - x_i|), j = i
 // included, plus mirror images across the symmetry planes.  With
 // `original` the result goes to density0 and no neighbour count is kept.
-__global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original) {
+//
+// With `want_mask` (fused fluid substeps, where positions cannot change
+// before the force pass) each fluid particle also records which of its
+// stencil candidates lie within h, in stencil order, as a bitmask
+// (SceneDesc::nbmask).
+//
+// Each warp stages its neighbour rows in shared memory: for every (z, y)
+// row of the stencil the union of its lanes' ranges is copied once with
+// coalesced float4 loads, and each lane then walks its own range from
+// shared memory (lanes of one cell read the same address: a broadcast).
+// Values, order and arithmetic are those of a direct walk; a union wider
+// than the buffer (a warp that spans two grid rows) is read from global
+// memory instead.  Dynamic shared memory: SPH_MASK_WORDS words per thread
+// when masking, then SPH_STAGE float4 per warp.
+#define SPH_STAGE 256
+
+__host__ __device__ constexpr size_t density_smem_bytes(unsigned block, bool mask) {
+    return (mask ? sizeof(unsigned) * SPH_MASK_WORDS * block : 0) + sizeof(float4) * SPH_STAGE * (block / 32);
+}
+
+__global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    unsigned *sm_mask = reinterpret_cast<unsigned *>(sm_raw);
+    float4 *wstage = reinterpret_cast<float4 *>(sm_raw + (want_mask ? sizeof(unsigned) * SPH_MASK_WORDS * blockDim.x
+                                                                      : 0)) +
+                     (threadIdx.x >> 5) * SPH_STAGE;
+    const unsigned lane = threadIdx.x & 31u;
     SPH_FOR_WORK(map)
     const unsigned n = active_count(S);
-    if (item < n) {
-        const unsigned k = item;
-        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
-        const float h = *S.h;
-        const DistBounds B = dist_bounds(h);
-        const float h2 = h * h;
-        const float3 ipos = xyz(S.spos[k]);
-        Planes P;
-        load_planes(S, ipos, h, P);
-        Kahan rho;
-        unsigned count = 0;
-        const float4 *__restrict__ spos = S.spos;
-        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-            const float3 jpos = xyz(spos[kk]);
-            const float r2 = norm2(sub3(jpos, ipos));
-            if (r2 <= B.le) {
-                float d = fmaxf(h2 - r2, 0.f);
-                rho.add(d * d * d);
-                count += r2 <= B.lt;
-            }
-            if (P.imask) {
-                unsigned jm = plane_jmask(P, jpos, h);
-                // subsets of jm in increasing order: the reference's
-                // plane_bits order restricted to the subsets it keeps
-                for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
-                    float3 ref = jpos;
-                    for (unsigned s = 0; s < P.count; ++s)
-                        if (bits & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
-                    float m2 = norm2(sub3(ref, ipos));
-                    if (m2 <= B.lt) {
-                        float d = fmaxf(h2 - m2, 0.f);
-                        rho.add(d * d * d);
-                        ++count;
-                    }
+    const bool mask = want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original;
+    if (mask)
+        for (unsigned w = 0; w < SPH_MASK_WORDS; ++w) sm_mask[w * blockDim.x + threadIdx.x] = 0u;
+    const bool active = item < n;
+    const unsigned k = item;
+    const unsigned i = active ? min(S.cellparticles[k], S.pnum - 1) : 0u;
+    const float h = *S.h;
+    const DistBounds B = dist_bounds(h);
+    const float h2 = h * h;
+    const float3 ipos = active ? xyz(S.spos[k]) : make_float3(0.f, 0.f, 0.f);
+    Planes P;
+    load_planes(S, ipos, h, P);
+    if (!active) P.imask = 0;
+    Kahan rho;
+    unsigned count = 0, cand = 0;
+    auto visit = [&](float3 jpos) {
+        const float r2 = norm2(sub3(jpos, ipos));
+        if (r2 <= B.le) {
+            float d = fmaxf(h2 - r2, 0.f);
+            rho.add(d * d * d);
+            count += r2 <= B.lt;
+            if (mask && cand < SPH_MASK_BITS) sm_mask[(cand >> 5) * blockDim.x + threadIdx.x] |= 1u << (cand & 31u);
+        }
+        ++cand;
+        if (P.imask) {
+            unsigned jm = plane_jmask(P, jpos, h);
+            // subsets of jm in increasing order: the reference's
+            // plane_bits order restricted to the subsets it keeps
+            for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
+                float3 ref = jpos;
+                for (unsigned s = 0; s < P.count; ++s)
+                    if (bits & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
+                float m2 = norm2(sub3(ref, ipos));
+                if (m2 <= B.lt) {
+                    float d = fmaxf(h2 - m2, 0.f);
+                    rho.add(d * d * d);
+                    ++count;
                 }
             }
-        });
+        }
+    };
+    // the stencil of for_each_neighbour, row by row
+    const unsigned R0 = S.gridres[0], R1 = S.gridres[1], R2 = S.gridres[2];
+    const unsigned layer = R0 * R1;
+    const unsigned cell = active ? S.gridcell[i] : 0u;
+    const unsigned cz = cell / layer, rem = cell - cz * layer, cy = rem / R0, cx = rem - cy * R0;
+    const unsigned x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
+    const float4 *__restrict__ spos = S.spos;
+    for (int dz = -1; dz <= 1; ++dz) {
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int z = (int)cz + dz, y = (int)cy + dy;
+            unsigned b = 0, e = 0;
+            if (active && z >= 0 && z < (int)R2 && y >= 0 && y < (int)R1) {
+                const unsigned row = (unsigned)z * layer + (unsigned)y * R0;
+                b = __ldg(S.celloffset + row + x0);
+                e = __ldg(S.celloffset + row + x1) + __ldg(S.gridcount + row + x1);
+                if (e > S.pnum) e = S.pnum;
+                if (b > e) b = e;
+            }
+            const unsigned ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
+            const unsigned ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
+            if (ub < ue && ue - ub <= SPH_STAGE) {
+                __syncwarp();
+                for (unsigned t = lane; t < ue - ub; t += 32) wstage[t] = spos[ub + t];
+                __syncwarp();
+                for (unsigned kk = b; kk < e; ++kk) visit(xyz(wstage[kk - ub]));
+            } else {
+                for (unsigned kk = b; kk < e; ++kk) visit(xyz(spos[kk]));
+            }
+        }
+    }
+    if (active) {
         // poly6 normalisation 315 / (64 pi h^9), applied once
         const float h3 = h2 * h;
         const float coef = 315.0f / (64.0f * SPH_PI_F * h3 * h3 * h3);
@@ -65,6 +126,12 @@ __global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, in
             S.density[i] = value;
             S.num_neighbours[i] = count;
             S.sdens[k] = value;
+        }
+        if (mask) {
+            S.ncand[k] = cand;
+            const unsigned words = (min(cand, (unsigned)SPH_MASK_BITS) + 31u) >> 5;
+            for (unsigned w = 0; w < words; ++w)
+                S.nbmask[(size_t)w * S.pnum + k] = sm_mask[w * blockDim.x + threadIdx.x];
         }
     }
     SPH_END_WORK
@@ -89,52 +156,92 @@ __device__ __forceinline__ float cube_bound(float p, float f) {
 // the sorted copies, which no other thread reads afterwards.
 __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p);
 
+// One particle's fluid force, visiting its within-h neighbours either by
+// scanning the stencil (`masked` false) or through the candidate mask the
+// density pass recorded (`masked` true, SPH_MASK_BITS candidates at most;
+// a particle with more is scanned).  Both visit the same neighbours in the
+// same order with the same arithmetic, so the results are identical.
+template <bool MASKED>
+__device__ __forceinline__ void fluid_force(const SceneDesc &S, unsigned k, int fuse_step) {
+    const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+    const float h = *S.h;
+    const DistBounds B = dist_bounds(h);
+    const float rho0 = *S.restdens, stiff = *S.stiffness, visc = *S.viscosity;
+    const float h3 = h * h * h;
+    const float kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
+    const float3 ipos = xyz(S.spos[k]);
+    const float3 ivel = xyz(S.svel[k]);
+    const float rhoi = S.sdens[k];
+    const float pi = (rhoi - rho0) * stiff;
+    Kahan3 f;
+    const float4 *__restrict__ spos = S.spos;
+    const float4 *__restrict__ svel = S.svel;
+    const float *__restrict__ sdens = S.sdens;
+    auto pair = [&](unsigned kk) {
+        if (kk == k) return;
+        const float3 d = sub3(xyz(spos[kk]), ipos);
+        const float r2 = norm2(d);
+        // distinct particles at exactly zero distance: no defined
+        // direction (the reference divides by the distance, fluids.cl:48)
+        if (!(r2 <= B.le) || r2 == 0.f) return;
+        const float rinv = rsqrtf(r2);
+        const float dist = r2 * rinv;
+        const float din = h - dist;
+        const float rhoj = sdens[kk];
+        const float pj = (rhoj - rho0) * stiff;
+        const float inv_didj = 1.0f / (rhoi * rhoj);
+        const float vterm = visc * din * kv;
+        const float pterm = -(pi + pj) * 0.5f * rinv * din * din * kv;
+        const float3 rv = xyz(svel[kk]) - ivel;
+        f.add(make_float3((d.x * pterm + rv.x * vterm) * inv_didj, (d.y * pterm + rv.y * vterm) * inv_didj,
+                          (d.z * pterm + rv.z * vterm) * inv_didj));
+    };
+    const unsigned cell = S.gridcell[i];
+    bool scanned = true;
+    if (MASKED) {
+        const unsigned cand = S.ncand[k];
+        if (cand <= SPH_MASK_BITS) {
+            scanned = false;
+            RowWalk rows(S, cell);
+            unsigned rb = 0, rl = 0, base = 0, total = 0;
+            bool have = rows.next(&rb, &rl);
+            const unsigned words = (cand + 31u) >> 5;
+            for (unsigned w = 0; w < words && have; ++w) {
+                unsigned m = S.nbmask[(size_t)w * S.pnum + k];
+                while (m) {
+                    const unsigned b = (w << 5) + (unsigned)(__ffs(m) - 1);
+                    m &= m - 1u;
+                    while (have && b >= base + rl) {
+                        base += rl;
+                        have = rows.next(&rb, &rl);
+                    }
+                    if (!have) break;
+                    pair(rb + (b - base));
+                }
+            }
+            (void)total;
+        }
+    }
+    if (scanned) for_each_neighbour(S, cell, pair);
+    const float m = *S.mass;
+    float3 fi = f.get() * m;
+    fi.x = cube_bound(ipos.x, fi.x);
+    fi.y = cube_bound(ipos.y, fi.y);
+    fi.z = cube_bound(ipos.z, fi.z);
+    st3(S.force, i, fi);
+    if (fuse_step) integrate(S, i, fi, ivel, ipos);
+}
+
 __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
-    const unsigned n = active_count(S);
-    if (item < n) {
-        const unsigned k = item;
-        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
-        const float h = *S.h;
-        const DistBounds B = dist_bounds(h);
-        const float rho0 = *S.restdens, stiff = *S.stiffness, visc = *S.viscosity;
-        const float h3 = h * h * h;
-        const float kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
-        const float3 ipos = xyz(S.spos[k]);
-        const float3 ivel = xyz(S.svel[k]);
-        const float rhoi = S.sdens[k];
-        const float pi = (rhoi - rho0) * stiff;
-        Kahan3 f;
-        const float4 *__restrict__ spos = S.spos;
-        const float4 *__restrict__ svel = S.svel;
-        const float *__restrict__ sdens = S.sdens;
-        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-            if (kk == k) return;
-            const float3 d = sub3(xyz(spos[kk]), ipos);
-            const float r2 = norm2(d);
-            // distinct particles at exactly zero distance: no defined
-            // direction (the reference divides by the distance, fluids.cl:48)
-            if (!(r2 <= B.le) || r2 == 0.f) return;
-            const float rinv = rsqrtf(r2);
-            const float dist = r2 * rinv;
-            const float din = h - dist;
-            const float rhoj = sdens[kk];
-            const float pj = (rhoj - rho0) * stiff;
-            const float inv_didj = 1.0f / (rhoi * rhoj);
-            const float vterm = visc * din * kv;
-            const float pterm = -(pi + pj) * 0.5f * rinv * din * din * kv;
-            const float3 rv = xyz(svel[kk]) - ivel;
-            f.add(make_float3((d.x * pterm + rv.x * vterm) * inv_didj, (d.y * pterm + rv.y * vterm) * inv_didj,
-                              (d.z * pterm + rv.z * vterm) * inv_didj));
-        });
-        const float m = *S.mass;
-        float3 fi = f.get() * m;
-        fi.x = cube_bound(ipos.x, fi.x);
-        fi.y = cube_bound(ipos.y, fi.y);
-        fi.z = cube_bound(ipos.z, fi.z);
-        st3(S.force, i, fi);
-        if (fuse_step) integrate(S, i, fi, ivel, ipos);
-    }
+    if (item < active_count(S)) fluid_force<false>(S, item, fuse_step);
+    SPH_END_WORK
+}
+
+// The fused-substep force pass: walks the density pass's candidate masks.
+__global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S)) fluid_force<true>(S, item, fuse_step);
     SPH_END_WORK
 }
 

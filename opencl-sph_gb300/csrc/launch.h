@@ -34,8 +34,8 @@ void sph_launch_bins(const Launch &L);
 // Cell-sorted copies (positions; velocities and densities on request).
 void sph_launch_gather(const Launch &L, bool vel, bool dens);
 
-void sph_launch_density(const Launch &L, bool original);
-void sph_launch_forces_fluids(const Launch &L, bool fuse_step);
+void sph_launch_density(const Launch &L, bool original, bool mask = false);
+void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked = false);
 void sph_launch_step_forward(const Launch &L);
 void sph_launch_plane_constraints(const Launch &L);
 void sph_launch_init_original_position(const Launch &L);
@@ -54,6 +54,9 @@ void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
 // before the phase is enqueued and with nullptr after the last one.
 typedef void (*PhaseMark)(void *ctx, const char *phase);
 void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark = nullptr, void *ctx = nullptr);
+
+// One-time kernel attributes (call outside any stream capture).
+cudaError_t sph_prepare_kernels();
 
 // cudaGetLastError() after the enqueues above; records and returns it.
 cudaError_t sph_check_launch(const char *what);

@@ -82,7 +82,17 @@ struct SceneDesc {
     unsigned num_scan_blocks;
     unsigned *big_cells;      // [0] = count, [1..] = cells above SPH_SMALL_CELL
     unsigned *status;         // SphStatus bits
+    // candidate masks (fluids, fused substep): bit b of particle k's mask is
+    // set when its b-th stencil candidate lies within h; word w of sorted
+    // particle k at nbmask[w * pnum + k]; ncand[k] = its candidate count
+    unsigned *nbmask;
+    unsigned *ncand;
 };
+
+// Candidate-mask capacity (candidates per particle); more fall back to a
+// scan of the stencil.
+#define SPH_MASK_WORDS 16
+#define SPH_MASK_BITS (32 * SPH_MASK_WORDS)
 
 // Block map entry: block b of a launch works on `scene`, items
 // [first, first + block size).

@@ -287,7 +287,9 @@ size_t sph_scratch_bytes(const SceneDesc &d) {
            + Arena::align(4 * P)             // sdens
            + Arena::align(4ull * d.num_scan_blocks)
            + Arena::align(4ull * (d.num_cells + 1))
-           + Arena::align(4);                // status
+           + Arena::align(4)                 // status
+           + Arena::align(4ull * SPH_MASK_WORDS * P)  // nbmask
+           + Arena::align(4 * P);            // ncand
 }
 
 void sph_place_scratch(SceneDesc *d, char *base) {
@@ -305,6 +307,10 @@ void sph_place_scratch(SceneDesc *d, char *base) {
     d->big_cells = reinterpret_cast<unsigned *>(base + o);
     o += Arena::align(4ull * (d->num_cells + 1));
     d->status = reinterpret_cast<unsigned *>(base + o);
+    o += Arena::align(4);
+    d->nbmask = reinterpret_cast<unsigned *>(base + o);
+    o += Arena::align(4ull * SPH_MASK_WORDS * P);
+    d->ncand = reinterpret_cast<unsigned *>(base + o);
 }
 
 void sph_build_maps(const std::vector<SceneDesc> &descs, const std::vector<unsigned> &ids, unsigned block,

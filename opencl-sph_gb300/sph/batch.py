@@ -79,6 +79,22 @@ class Batch(object):
             raise bnd.SphError(bnd.last_error())
         return s.views
 
+    def read_field(self, sid, name):
+        """Copies one field of scene `sid` back; returns its host view."""
+        s = self.scenes[sid]
+        if bnd.sph_batch_read_field(self.handle, sid, name, ctypes.byref(s.psdata)) != 0:
+            raise bnd.SphError(bnd.last_error())
+        return s.views[name]
+
+    def profile(self, reps=3):
+        """Mean device ms per phase of a substep (phases run one by one)."""
+        ms = (ctypes.c_float * 16)()
+        names = (ctypes.c_char_p * 16)()
+        k = bnd.sph_batch_profile(self.handle, reps, ms, names, 16)
+        if k < 0:
+            raise bnd.SphError(bnd.last_error())
+        return {names[i].decode(): float(ms[i]) for i in range(k)}
+
     def tune(self, block, pair_block, grid_cap):
         if bnd.sph_batch_tune(self.handle, block, pair_block, grid_cap) != 0:
             raise bnd.SphError(bnd.last_error())

@@ -188,3 +188,29 @@ def test_status_nonfinite():
     ps.update_fused(1)
     assert ps.status() & 1
     ps.close()
+
+
+def test_fused_masks_with_crowded_stencils_equal_named_scan():
+    """The fused substep walks the density pass's candidate masks (at most
+    512 candidates per particle) and scans the stencil beyond that; both
+    must give the named path's result bit for bit."""
+    sc = scenes.wcsph_block(12, 12, 12, jitter=1e-4, seed=13, walls=True)
+    pos = sc.init["position"].copy()
+    rng = np.random.default_rng(3)
+    pos[:600] = 0.2 + rng.uniform(-0.008, 0.008, size=(600, 3))  # > 512 candidates each
+    a = sc.system()
+    b = sc.system()
+    a.set_fields(position=pos)
+    b.set_fields(position=pos)
+    for _ in range(3):
+        a.compute_particle_bins()
+        for k in ["compute_density", "compute_forces_fluids", "step_forward"]:
+            a.call_for_all_particles(k)
+    b.update_fused(3)
+    a.sync_device_to_host()
+    b.sync_device_to_host()
+    n = sc.n
+    for f in ("position", "velocity", "force", "density"):
+        assert np.array_equal(a.get_fields(f)[0][:n], b.get_fields(f)[0][:n]), f
+    a.close()
+    b.close()
