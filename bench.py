@@ -400,15 +400,20 @@ def bench_served(args):
                                     name="q%d" % i)
     reqs = poisson_requests(rate=50.0, duration=args.served_seconds, make_scene=make, steps_range=(100, 2000),
                             seed=args.seed)
-    srv = Server(budget_bytes=150e9, max_chunk=50, keep_results=False)
+    srv = Server(budget_bytes=150e9, max_chunk=25, max_particles=8 << 20, keep_results=False)
     srv.prepare(reqs)
     st = srv.run(reqs, realtime=True)
+    demand = sum(r.work for r in reqs) / args.served_seconds
     model = plain_step_model([2000, 16000, 131072, 262144])
     seq = sequential_fifo(reqs, lambda r: r.steps * model(r.scene.n))
     release(reqs)
     return {"requests": st["requests"], "arrival_rate_per_s": 50.0, "window_s": args.served_seconds,
             "throughput": st["throughput"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
             "makespan_s": st["makespan_s"], "peak_resident": st["peak_resident"],
+            "peak_particles": st["peak_particles"], "chunks": st["chunks"], "gpu_busy_s": st["gpu_busy_s"],
+            "offered_load": demand, "saturated": bool(demand > st["throughput"]),
+            "policy": "FIFO admission by 150 GB HBM budget and 8M resident particles; device-side substep "
+                      "quotas; chunks of up to 25 substeps",
             "sequential_plain_model": {"throughput": seq["throughput"], "p50_s": seq["p50_s"],
                                        "p99_s": seq["p99_s"],
                                        "how": "FIFO queue of one-at-a-time drop-in solves, per-substep times "

@@ -234,6 +234,15 @@ int sph_batch_add(sph_batch *batch, psdata *scene, const char *file_list);
 int sph_batch_remove(sph_batch *batch, int id);
 /* Advances every scene of the batch by num_steps substeps. */
 int sph_batch_step(sph_batch *batch, unsigned int num_steps);
+/* Substep quotas, for serving: a scene given a quota of `steps` takes part
+ * in the next `steps` substeps of the batch and then stays idle -- every
+ * kernel skips it, its store keeps its values -- until it gets a new
+ * quota.  Scenes are added with SPH_BATCH_STEPS_UNLIMITED (never idle).
+ * The write is stream-ordered after the work already enqueued. */
+#define SPH_BATCH_STEPS_UNLIMITED 0xffffffffu
+int sph_batch_set_steps(sph_batch *batch, int id, unsigned int steps);
+/* The scene's remaining quota (waits for the batch's stream). */
+unsigned int sph_batch_steps_left(sph_batch *batch, int id);
 /* Copies a scene's device store into `out` (same layout as when added). */
 int sph_batch_read(sph_batch *batch, int id, psdata *out);
 /* Copies one named field of a scene into the same field of `out`. */

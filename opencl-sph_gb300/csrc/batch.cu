@@ -65,10 +65,10 @@ unsigned cap_of(const sph_batch *b) { return b->grid_cap ? b->grid_cap : (1u << 
 struct TableBuild {
     std::vector<char> host;
     size_t add(const void *p, size_t n) {
-        size_t o = host.size();
-        size_t pad = Arena::align(n);
-        host.resize(o + pad, 0);
-        if (n) memcpy(host.data() + o, p, n);
+        const size_t o = host.size();
+        host.resize(o + Arena::align(n), 0);
+        const char *src = static_cast<const char *>(p);
+        std::copy(src, src + n, host.begin() + o);
         return o;
     }
 };
@@ -211,6 +211,7 @@ bool rebuild(sph_batch *b) {
             cudaStreamWaitEvent(b->stream, b->join[m - 1], 0);
         }
     }
+    sph_launch_count_down(A);
     cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -322,6 +323,8 @@ extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list)
     bool good = ok(cudaMemcpyAsync(sc->mem, scene->data, sc->blob_size, cudaMemcpyHostToDevice, b->stream),
                    "sph_batch_add upload") &&
                 ok(cudaMemsetAsync(sc->desc.status, 0, 4, b->stream), "sph_batch_add") &&
+                ok((sph_launch_set_steps(sc->desc.steps_left, SPH_STEPS_UNLIMITED, b->stream), cudaGetLastError()),
+                   "sph_batch_add") &&
                 ok(cudaStreamSynchronize(b->stream), "sph_batch_add upload");
     if (good && material != MAT_FLUID) good = solid_setup(b, sc);
     if (!good) {
@@ -354,6 +357,23 @@ extern "C" int sph_batch_remove(sph_batch *b, int id) {
     b->slots[id] = nullptr;
     b->dirty = true;
     return 0;
+}
+
+extern "C" int sph_batch_set_steps(sph_batch *b, int id, unsigned int steps) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_set_steps");
+    if (!sc) return -1;
+    sph_launch_set_steps(sc->desc.steps_left, steps, b->stream);
+    return sph_check_launch("sph_batch_set_steps") == cudaSuccess ? 0 : -1;
+}
+
+extern "C" unsigned int sph_batch_steps_left(sph_batch *b, int id) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_steps_left");
+    unsigned v = 0;
+    if (!sc || !ok(cudaMemcpyAsync(&v, sc->desc.steps_left, 4, cudaMemcpyDeviceToHost, b->stream),
+                   "sph_batch_steps_left") ||
+        !ok(cudaStreamSynchronize(b->stream), "sph_batch_steps_left"))
+        return 0;
+    return v;
 }
 
 extern "C" int sph_batch_step(sph_batch *b, unsigned num_steps) {
@@ -441,6 +461,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
                 sph_launch_step_forward(G);
             }
         }
+        sph_launch_count_down(A);
         log.mark(nullptr);
         bool good = sph_check_launch("sph_batch_profile") == cudaSuccess &&
                     ok(cudaStreamSynchronize(b->stream), "sph_batch_profile");

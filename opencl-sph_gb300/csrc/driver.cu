@@ -150,6 +150,7 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     std::string e2;
     sph_resolve_scene(*data, s->d_blob, programs, &s->desc, &e2);
     sph_place_scratch(&s->desc, b + o_scratch);
+    s->desc.steps_left = nullptr;  // a single store has no substep quota
     s->d_desc = reinterpret_cast<SceneDesc *>(b + o_desc);
     auto up = [&](size_t off, const void *src, size_t bytes) {
         return bytes == 0 || cuda_ok(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, s->stream),

@@ -190,3 +190,24 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     sph_launch_step_forward(L);
     phase(nullptr);
 }
+
+// End of a batched substep: each scene with a finite quota left uses one.
+__global__ void k_count_down(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
+    for (unsigned s = blockIdx.x * blockDim.x + threadIdx.x; s < num_scenes; s += gridDim.x * blockDim.x) {
+        unsigned *q = scenes[s].steps_left;
+        if (!q) continue;
+        const unsigned v = *q;
+        if (v != 0u && v != SPH_STEPS_UNLIMITED) *q = v - 1u;
+    }
+}
+
+__global__ void k_set_steps(unsigned *steps_left, unsigned steps) { *steps_left = steps; }
+
+void sph_launch_count_down(const Launch &L) {
+    unsigned g = (L.num_scenes + 255) / 256;
+    k_count_down<<<g ? g : 1, 256, 0, L.stream>>>(L.scenes, L.num_scenes);
+}
+
+void sph_launch_set_steps(unsigned *steps_left, unsigned steps, cudaStream_t stream) {
+    k_set_steps<<<1, 1, 0, stream>>>(steps_left, steps);
+}

@@ -10,12 +10,18 @@
 
 #define SPH_FULL_MASK 0xffffffffu
 
+// A batched scene whose substep quota is used up: every kernel leaves it
+// (fields, grid tables and scratch) untouched.
+__device__ __forceinline__ bool scene_idle(const SceneDesc &S) { return S.steps_left && *S.steps_left == 0u; }
+
 // Iterate the virtual blocks of a segment-aware launch.  Inside the body,
 // `S` is the block's scene and `item` this thread's item index in it.
+// Blocks of idle scenes are skipped (uniformly for the whole block).
 #define SPH_FOR_WORK(map)                                                      \
     for (unsigned vb_ = blockIdx.x; vb_ < (map).num; vb_ += gridDim.x) {       \
         const BlockWork bw_ = (map).work[vb_];                                 \
         const SceneDesc &S = scenes[bw_.scene];                                \
+        if (scene_idle(S)) continue;                                           \
         const unsigned item = bw_.first + threadIdx.x;
 #define SPH_END_WORK }
 

@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_tiles(const SceneDesc
     for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
         const BlockWork bw = map.work[vb];
         const SceneDesc &S = scenes[bw.scene];
+        if (scene_idle(S)) continue;
         const unsigned per = SPH_SCAN_TILE / SPH_SCAN_THREADS;
         const unsigned c0 = bw.first + threadIdx.x * per;
         unsigned v[SPH_SCAN_TILE / SPH_SCAN_THREADS];
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_tiles(const SceneDesc
 __global__ void __launch_bounds__(1024) k_scan_sums(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
     for (unsigned s = blockIdx.x; s < num_scenes; s += gridDim.x) {
         const SceneDesc &S = scenes[s];
+        if (scene_idle(S)) continue;
         unsigned carry = 0;
         for (unsigned base = 0; base < S.num_scan_blocks; base += blockDim.x) {
             unsigned i = base + threadIdx.x;
@@ -161,6 +163,7 @@ __global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_add(const SceneDesc *
     for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
         const BlockWork bw = map.work[vb];
         const SceneDesc &S = scenes[bw.scene];
+        if (scene_idle(S)) continue;
         const unsigned add = S.scan_sums[bw.first / SPH_SCAN_TILE];
         if (add == 0) continue;
         for (unsigned c = bw.first + threadIdx.x; c < bw.first + SPH_SCAN_TILE && c < S.num_cells; c += blockDim.x)
@@ -220,6 +223,7 @@ __global__ void k_sort_cells(const SceneDesc *__restrict__ scenes, BlockMap map)
 __global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
     for (unsigned s = 0; s < num_scenes; ++s) {
         const SceneDesc &S = scenes[s];
+        if (scene_idle(S)) continue;
         const unsigned nbig = S.big_cells[0];
         for (unsigned b = blockIdx.x; b < nbig; b += gridDim.x) {
             const unsigned cell = S.big_cells[1 + b];

@@ -47,6 +47,10 @@ void sph_launch_set_body_position(const Launch &L, unsigned body, const float po
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
 void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);
 void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
+// Batched form: the end-of-substep quota count-down over all scenes, and a
+// stream-ordered write of one scene's quota.
+void sph_launch_count_down(const Launch &L);
+void sph_launch_set_steps(unsigned *steps_left, unsigned steps, cudaStream_t stream);
 
 // One substep of a material's recipe for every scene of the launch.  All
 // scenes of L must share the material (batches launch one Launch per

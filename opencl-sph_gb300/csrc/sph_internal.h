@@ -87,7 +87,12 @@ struct SceneDesc {
     // particle k at nbmask[w * pnum + k]; ncand[k] = its candidate count
     unsigned *nbmask;
     unsigned *ncand;
+    // batched form only (null otherwise): substeps this scene still takes;
+    // at 0 every kernel skips the scene, SPH_STEPS_UNLIMITED never expires
+    unsigned *steps_left;
 };
+
+#define SPH_STEPS_UNLIMITED 0xffffffffu
 
 // Candidate-mask capacity (candidates per particle); more fall back to a
 // scan of the stencil.

@@ -289,7 +289,8 @@ size_t sph_scratch_bytes(const SceneDesc &d) {
            + Arena::align(4ull * (d.num_cells + 1))
            + Arena::align(4)                 // status
            + Arena::align(4ull * SPH_MASK_WORDS * P)  // nbmask
-           + Arena::align(4 * P);            // ncand
+           + Arena::align(4 * P)             // ncand
+           + Arena::align(4);                // steps_left
 }
 
 void sph_place_scratch(SceneDesc *d, char *base) {
@@ -311,6 +312,8 @@ void sph_place_scratch(SceneDesc *d, char *base) {
     d->nbmask = reinterpret_cast<unsigned *>(base + o);
     o += Arena::align(4ull * SPH_MASK_WORDS * P);
     d->ncand = reinterpret_cast<unsigned *>(base + o);
+    o += Arena::align(4 * P);
+    d->steps_left = reinterpret_cast<unsigned *>(base + o);
 }
 
 void sph_build_maps(const std::vector<SceneDesc> &descs, const std::vector<unsigned> &ids, unsigned block,

@@ -68,6 +68,17 @@ class Batch(object):
         if bnd.sph_batch_step(self.handle, steps) != 0:
             raise bnd.SphError(bnd.last_error())
 
+    UNLIMITED = 0xFFFFFFFF
+
+    def set_steps(self, sid, steps):
+        """Substep quota: the scene takes part in the next `steps` substeps
+        and then stays idle (unchanged) until given a new quota."""
+        if bnd.sph_batch_set_steps(self.handle, sid, int(steps)) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def steps_left(self, sid):
+        return int(bnd.sph_batch_steps_left(self.handle, sid))
+
     def synchronize(self):
         if bnd.sph_batch_synchronize(self.handle) != 0:
             raise bnd.SphError(bnd.last_error())

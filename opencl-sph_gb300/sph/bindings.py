@@ -203,6 +203,8 @@ _SIGS = {
     "sph_batch_add": ([c_void_p, POINTER(psdata), String], c_int),
     "sph_batch_remove": ([c_void_p, c_int], c_int),
     "sph_batch_step": ([c_void_p, c_uint], c_int),
+    "sph_batch_set_steps": ([c_void_p, c_int, c_uint], c_int),
+    "sph_batch_steps_left": ([c_void_p, c_int], c_uint),
     "sph_batch_read": ([c_void_p, c_int, POINTER(psdata)], c_int),
     "sph_batch_synchronize": ([c_void_p], c_int),
     "sph_batch_read_field": ([c_void_p, c_int, String, POINTER(psdata)], c_int),

@@ -1,15 +1,17 @@
 """Served form: a request loop with continuous batching.
 
 Requests (a scene and a substep count) arrive over time.  The server keeps
-one :class:`~sph.batch.Batch` on the device; whenever it is between
-chunks it admits every arrived request whose store fits in the HBM budget
-(first come, first served), advances all resident scenes together by a
-chunk of substeps -- no longer than the shortest remaining request, so no
-scene overshoots its count -- and retires finished scenes, reading their
-results back and freeing their memory for the next admissions.  Scenes
-that arrive while others run join at the next chunk boundary, and their
-work shares the same launches; a scene's result is the same as when it
-runs alone (the batch kernels treat scenes independently).
+one :class:`~sph.batch.Batch` on the device.  Between chunks it admits
+arrived requests first come, first served, while the batch stays within
+the HBM budget and the resident-particle cap (enough particles to fill
+the GPU; admitting more only makes everyone wait longer).  Each admitted
+scene gets a substep quota equal to its request (`Batch.set_steps`), then
+the whole batch advances by a chunk of up to `max_chunk` substeps: a scene
+whose quota runs out inside the chunk goes idle on the device (every kernel
+skips it) until the chunk ends, when its result is read back and its memory
+freed for the next admissions.  Scenes that arrive while others run join at
+the next chunk boundary and share their launches; a scene's result is the
+same as when it runs alone (the batch kernels treat scenes independently).
 
 Reports p50/p99 time to completion (arrival -> result on the host) beside
 aggregate particle-steps/s.
@@ -55,9 +57,10 @@ def poisson_requests(rate, duration, make_scene, steps_range, seed=0):
 
 
 class Server(object):
-    def __init__(self, budget_bytes=150e9, max_chunk=50, keep_results=True, tune=None):
+    def __init__(self, budget_bytes=150e9, max_chunk=25, max_particles=8 << 20, keep_results=True, tune=None):
         self.budget = float(budget_bytes)
         self.max_chunk = int(max_chunk)
+        self.max_particles = int(max_particles)
         self.keep = keep_results
         self.tune = tune
 
@@ -67,6 +70,11 @@ class Server(object):
             if r.host is None:
                 r.host = Batch.host_store(r.scene)
                 r.bytes = Batch.scene_bytes(r.scene, r.host)
+
+    def _fits(self, batch, resident, r, active):
+        if not active:
+            return True  # a lone request always runs, whatever its size
+        return batch.bytes + r.bytes <= self.budget and resident + r.scene.n <= self.max_particles
 
     def run(self, requests, realtime=True):
         """Serves `requests` (arrival times in seconds from the start).
@@ -78,6 +86,7 @@ class Server(object):
         if self.tune:
             batch.tune(*self.tune)
         active = {}
+        resident = 0
         t0 = time.perf_counter()
         skew = 0.0
 
@@ -85,19 +94,21 @@ class Server(object):
             return time.perf_counter() - t0 + skew
 
         chunks = 0
+        substeps = 0
         peak_resident = 0
+        peak_particles = 0
         peak_bytes = 0
+        busy = 0.0
         while pending or active:
             now = clock()
-            while pending and pending[0].arrival <= now:
-                r = pending[0]
-                if active and batch.bytes + r.bytes > self.budget:
-                    break
-                pending.popleft()
+            while pending and pending[0].arrival <= now and self._fits(batch, resident, pending[0], active):
+                r = pending.popleft()
                 sid = batch.add(r.scene, ps=r.host)
                 r.host = None  # owned by the batch now
+                batch.set_steps(sid, r.remaining)
                 r.admitted = clock()
                 active[sid] = r
+                resident += r.scene.n
             if not active:
                 if pending:
                     wait = pending[0].arrival - clock()
@@ -108,13 +119,17 @@ class Server(object):
                             skew += wait
                 continue
             peak_resident = max(peak_resident, len(active))
+            peak_particles = max(peak_particles, resident)
             peak_bytes = max(peak_bytes, batch.bytes)
-            chunk = min(self.max_chunk, min(r.remaining for r in active.values()))
+            chunk = min(self.max_chunk, max(r.remaining for r in active.values()))
+            c0 = time.perf_counter()
             batch.step(chunk)
             batch.synchronize()
+            busy += time.perf_counter() - c0
             chunks += 1
+            substeps += chunk
             for sid, r in list(active.items()):
-                r.remaining -= chunk
+                r.remaining -= min(chunk, r.remaining)
                 if r.remaining == 0:
                     if self.keep:
                         v = batch.read(sid)
@@ -122,6 +137,7 @@ class Server(object):
                                     "velocity": np.array(v["velocity"][: r.scene.n])}
                     batch.remove(sid)
                     r.done = clock()
+                    resident -= r.scene.n
                     del active[sid]
         makespan = clock()
         batch.close()
@@ -135,7 +151,10 @@ class Server(object):
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else 0.0,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else 0.0,
             "chunks": chunks,
+            "substeps": substeps,
+            "gpu_busy_s": busy,
             "peak_resident": peak_resident,
+            "peak_particles": peak_particles,
             "peak_bytes": peak_bytes,
         }
 

@@ -131,3 +131,31 @@ def test_served_results_equal_alone():
         assert np.array_equal(r.result["position"], pos), r.scene.name
         assert np.array_equal(r.result["velocity"], vel), r.scene.name
     release(reqs)
+
+
+def test_step_quota_idles_scene():
+    """A scene whose quota runs out stays unchanged while the batch goes
+    on; given a new quota it resumes exactly where it stopped."""
+    scs = mix(seed=40)
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    b.set_steps(ids[0], 5)
+    b.set_steps(ids[1], 0)
+    b.step(9)
+    assert b.steps_left(ids[0]) == 0 and b.steps_left(ids[1]) == 0
+    assert b.steps_left(ids[2]) == Batch.UNLIMITED
+    pos, vel = alone(scs[0], 5)
+    v = b.read(ids[0])
+    assert np.array_equal(v["position"][: scs[0].n], pos) and np.array_equal(v["velocity"][: scs[0].n], vel)
+    p1 = b.read(ids[1])["position"][: scs[1].n]
+    assert np.array_equal(p1, np.asarray(scs[1].init["position"], np.float32).reshape(p1.shape))
+    for k in (2, 3):
+        pos, _ = alone(scs[k], 9)
+        assert np.array_equal(b.read(ids[k])["position"][: scs[k].n], pos), scs[k].name
+    b.set_steps(ids[0], 3)
+    b.step(4)
+    assert b.steps_left(ids[0]) == 0
+    pos, vel = alone(scs[0], 8)
+    v = b.read(ids[0])
+    assert np.array_equal(v["position"][: scs[0].n], pos) and np.array_equal(v["velocity"][: scs[0].n], vel)
+    b.close()
