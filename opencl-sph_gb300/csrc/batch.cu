@@ -110,6 +110,7 @@ bool solid_setup(sph_batch *b, BatchScene *sc) {
     L.pair_block = b->pair_block;
     L.grid_cap = cap_of(b);
     L.stream = b->stream;
+    L.no_symmetry_planes = sc->desc.num_symmetry_planes == 0;
     sph_launch_init_original_position(L);
     sph_launch_bins(L);
     sph_launch_gather(L, false, false);
@@ -176,6 +177,8 @@ bool rebuild(sph_batch *b) {
     A.pair_block = b->pair_block;
     A.grid_cap = cap_of(b);
     A.stream = b->stream;
+    A.no_symmetry_planes = std::all_of(descs.begin(), descs.end(),
+                                       [](const SceneDesc &d) { return d.num_symmetry_planes == 0; });
     cudaStream_t streams[3] = {b->stream, b->side[0], b->side[1]};
     for (int m = 0; m < 3; ++m) {
         GroupLaunch &G = b->group[m];

@@ -179,6 +179,7 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     L.pair_block = pair_block;
     L.grid_cap = 1u << 30;
     L.stream = s->stream;
+    L.no_symmetry_planes = s->desc.num_symmetry_planes == 0;
     {
         std::lock_guard<std::mutex> lk(g_stores_mu);
         g_stores.insert(s);

@@ -18,9 +18,11 @@ cudaError_t sph_prepare_kernels() {
     int dev = 0, max_optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    size_t want = density_smem_bytes(1024, true);
+    size_t want = density_smem_bytes(1024);
     if (max_optin > 0 && want > (size_t)max_optin) want = (size_t)max_optin;
-    return cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    cudaError_t e = cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
 }
 
 cudaError_t sph_check_launch(const char *what) {
@@ -68,9 +70,12 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens) {
 }
 
 void sph_launch_density(const Launch &L, bool original, bool mask) {
-    const size_t smem = density_smem_bytes(L.pair_block, mask);
-    k_density<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, smem, L.stream>>>(
-        L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0);
+    const size_t smem = density_smem_bytes(L.pair_block);
+    const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    k_density<false><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0);
+    if (!L.no_symmetry_planes)
+        k_density<true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0,
+                                                             mask ? 1 : 0);
 }
 
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {

@@ -143,43 +143,6 @@ __device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned 
     }
 }
 
-// The rows of for_each_neighbour one at a time, in the same order and with
-// the same clamping, as (first sorted index, length) pairs.
-struct RowWalk {
-    const SceneDesc *S;
-    unsigned layer, cx0, cx1, cy, cz;
-    int dz, dy;
-    __device__ __forceinline__ RowWalk(const SceneDesc &s, unsigned cell) : S(&s), dz(-1), dy(-2) {
-        const unsigned R0 = s.gridres[0];
-        layer = R0 * s.gridres[1];
-        cz = cell / layer;
-        const unsigned rem = cell - cz * layer;
-        cy = rem / R0;
-        const unsigned cx = rem - cy * R0;
-        cx0 = cx > 0 ? cx - 1 : 0;
-        cx1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
-    }
-    // Advances to the next row inside the grid; false when none is left.
-    __device__ __forceinline__ bool next(unsigned *begin, unsigned *len) {
-        for (;;) {
-            if (++dy > 1) {
-                dy = -1;
-                if (++dz > 1) return false;
-            }
-            int z = (int)cz + dz, y = (int)cy + dy;
-            if (z < 0 || z >= (int)S->gridres[2] || y < 0 || y >= (int)S->gridres[1]) continue;
-            unsigned row = (unsigned)z * layer + (unsigned)y * S->gridres[0];
-            unsigned b = __ldg(S->celloffset + row + cx0);
-            unsigned e = __ldg(S->celloffset + row + cx1) + __ldg(S->gridcount + row + cx1);
-            if (e > S->pnum) e = S->pnum;
-            if (b > e) b = e;
-            *begin = b;
-            *len = e - b;
-            return true;
-        }
-    }
-};
-
 // ---- symmetry planes (the SYMMETRY blocks, e.g. common.cl:647-686) ----------
 
 #define SPH_MAX_PLANES 8

@@ -16,103 +16,131 @@
 // included, plus mirror images across the symmetry planes.  With
 // `original` the result goes to density0 and no neighbour count is kept.
 //
-// With `want_mask` (fused fluid substeps, where positions cannot change
-// before the force pass) each fluid particle also records which of its
-// stencil candidates lie within h, in stencil order, as a bitmask
-// (SceneDesc::nbmask).
+// The stencil is walked as 9 rows (dz outer, dy inner, as the reference's
+// z, y, x loops): cells x-1..x+1 of one (z, y) row are one contiguous range
+// of the cell-sorted order.  Each warp stages its rows in shared memory:
+// for every row the union of its lanes' ranges is copied once with
+// coalesced float4 loads and each lane walks its own range there (lanes of
+// one cell read the same address: a broadcast).  Values, order and
+// arithmetic are those of a direct walk; a union wider than the buffer (a
+// warp that spans two grid rows) is read from global memory instead.
 //
-// Each warp stages its neighbour rows in shared memory: for every (z, y)
-// row of the stencil the union of its lanes' ranges is copied once with
-// coalesced float4 loads, and each lane then walks its own range from
-// shared memory (lanes of one cell read the same address: a broadcast).
-// Values, order and arithmetic are those of a direct walk; a union wider
-// than the buffer (a warp that spans two grid rows) is read from global
-// memory instead.  Dynamic shared memory: SPH_MASK_WORDS words per thread
-// when masking, then SPH_STAGE float4 per warp.
+// With `want_mask` (fused fluid substeps, where positions cannot change
+// before the force pass) each fluid particle also records, per row, which
+// candidates lie within h: bit t of row r's 64-bit mask is candidate
+// b_r + t.  The low word goes to nbmask[(2r) * pnum + k], the high word to
+// nbmask[(2r+1) * pnum + k] only when the row holds more than 32
+// candidates; a row of more than 64 marks the particle for a scan
+// (ncand[k] = SPH_NCAND_SCAN).  The stores of one row are one coalesced
+// store per warp.
 #define SPH_STAGE 256
 
-__host__ __device__ constexpr size_t density_smem_bytes(unsigned block, bool mask) {
-    return (mask ? sizeof(unsigned) * SPH_MASK_WORDS * block : 0) + sizeof(float4) * SPH_STAGE * (block / 32);
+__host__ __device__ constexpr size_t density_smem_bytes(unsigned block) {
+    return sizeof(float4) * SPH_STAGE * (block / 32);
 }
 
-__global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask) {
-    extern __shared__ __align__(16) unsigned char sm_raw[];
-    unsigned *sm_mask = reinterpret_cast<unsigned *>(sm_raw);
-    float4 *wstage = reinterpret_cast<float4 *>(sm_raw + (want_mask ? sizeof(unsigned) * SPH_MASK_WORDS * blockDim.x
-                                                                      : 0)) +
-                     (threadIdx.x >> 5) * SPH_STAGE;
-    const unsigned lane = threadIdx.x & 31u;
-    SPH_FOR_WORK(map)
-    const unsigned n = active_count(S);
-    const bool mask = want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original;
-    if (mask)
-        for (unsigned w = 0; w < SPH_MASK_WORDS; ++w) sm_mask[w * blockDim.x + threadIdx.x] = 0u;
+// Row r of particle k's stencil: [b, e) of the cell-sorted order, empty
+// when the row lies outside the grid.
+struct StencilRows {
+    unsigned layer, R0, R1, R2, cx0, cx1, cy, cz;
+    __device__ __forceinline__ StencilRows(const SceneDesc &S, unsigned cell) {
+        R0 = S.gridres[0];
+        R1 = S.gridres[1];
+        R2 = S.gridres[2];
+        layer = R0 * R1;
+        cz = cell / layer;
+        const unsigned rem = cell - cz * layer;
+        cy = rem / R0;
+        const unsigned cx = rem - cy * R0;
+        cx0 = cx > 0 ? cx - 1 : 0;
+        cx1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
+    }
+    __device__ __forceinline__ void row(const SceneDesc &S, int r, unsigned *b, unsigned *e) const {
+        const int z = (int)cz + r / 3 - 1, y = (int)cy + r % 3 - 1;
+        *b = *e = 0;
+        if (z < 0 || z >= (int)R2 || y < 0 || y >= (int)R1) return;
+        const unsigned first = (unsigned)z * layer + (unsigned)y * R0;
+        unsigned bb = __ldg(S.celloffset + first + cx0);
+        unsigned ee = __ldg(S.celloffset + first + cx1) + __ldg(S.gridcount + first + cx1);
+        if (ee > S.pnum) ee = S.pnum;  // only with inconsistent host-written tables
+        if (bb > ee) bb = ee;
+        *b = bb;
+        *e = ee;
+    }
+};
+
+template <bool PLANES, bool MASK>
+__device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsigned item, unsigned lane,
+                                            float4 *__restrict__ wstage, int original) {
     const bool active = item < n;
     const unsigned k = item;
     const unsigned i = active ? min(S.cellparticles[k], S.pnum - 1) : 0u;
     const float h = *S.h;
     const DistBounds B = dist_bounds(h);
-    const float h2 = h * h;
+    const float h2 = __fmul_rn(h, h);
     const float3 ipos = active ? xyz(S.spos[k]) : make_float3(0.f, 0.f, 0.f);
     Planes P;
-    load_planes(S, ipos, h, P);
-    if (!active) P.imask = 0;
+    if (PLANES) {
+        load_planes(S, ipos, h, P);
+        if (!active) P.imask = 0;
+    }
     Kahan rho;
-    unsigned count = 0, cand = 0;
-    auto visit = [&](float3 jpos) {
-        const float r2 = norm2(sub3(jpos, ipos));
-        if (r2 <= B.le) {
-            float d = fmaxf(h2 - r2, 0.f);
-            rho.add(d * d * d);
-            count += r2 <= B.lt;
-            if (mask && cand < SPH_MASK_BITS) sm_mask[(cand >> 5) * blockDim.x + threadIdx.x] |= 1u << (cand & 31u);
+    unsigned count = 0, total = 0;
+    bool overflow = false;
+    const StencilRows rows(S, active ? S.gridcell[i] : 0u);
+    const float4 *__restrict__ spos = S.spos;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        unsigned b = 0, e = 0;
+        if (active) rows.row(S, r, &b, &e);
+        const unsigned ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
+        const unsigned ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
+        const bool staged = ub < ue && ue - ub <= SPH_STAGE;
+        if (staged) {
+            __syncwarp();
+            for (unsigned t = lane; t < ue - ub; t += 32) wstage[t] = spos[ub + t];
+            __syncwarp();
         }
-        ++cand;
-        if (P.imask) {
-            unsigned jm = plane_jmask(P, jpos, h);
-            // subsets of jm in increasing order: the reference's
-            // plane_bits order restricted to the subsets it keeps
-            for (unsigned bits = (0u - jm) & jm; bits; bits = (bits - jm) & jm) {
-                float3 ref = jpos;
-                for (unsigned s = 0; s < P.count; ++s)
-                    if (bits & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
-                float m2 = norm2(sub3(ref, ipos));
-                if (m2 <= B.lt) {
-                    float d = fmaxf(h2 - m2, 0.f);
-                    rho.add(d * d * d);
-                    ++count;
+        unsigned long long bits = 0;
+        auto visit = [&](float3 jpos, unsigned t) {
+            const float r2 = norm2(sub3(jpos, ipos));
+            if (r2 <= B.le) {
+                const float d = fmaxf(h2 - r2, 0.f);
+                rho.add(d * d * d);
+                count += r2 <= B.lt;
+                if (MASK && t < 64) bits |= 1ull << t;
+            }
+            if (PLANES && P.imask) {
+                const unsigned jm = plane_jmask(P, jpos, h);
+                // subsets of jm in increasing order: the reference's
+                // plane_bits order restricted to the subsets it keeps
+                for (unsigned sb = (0u - jm) & jm; sb; sb = (sb - jm) & jm) {
+                    float3 ref = jpos;
+                    for (unsigned s = 0; s < P.count; ++s)
+                        if (sb & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
+                    const float m2 = norm2(sub3(ref, ipos));
+                    if (m2 <= B.lt) {
+                        const float d = fmaxf(h2 - m2, 0.f);
+                        rho.add(d * d * d);
+                        ++count;
+                    }
                 }
             }
+        };
+        if (staged) {
+            const float4 *src = wstage + (b - ub);
+            const unsigned len = e - b;
+#pragma unroll 2
+            for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
+        } else {
+            for (unsigned t = 0; t < e - b; ++t) visit(xyz(spos[b + t]), t);
         }
-    };
-    // the stencil of for_each_neighbour, row by row
-    const unsigned R0 = S.gridres[0], R1 = S.gridres[1], R2 = S.gridres[2];
-    const unsigned layer = R0 * R1;
-    const unsigned cell = active ? S.gridcell[i] : 0u;
-    const unsigned cz = cell / layer, rem = cell - cz * layer, cy = rem / R0, cx = rem - cy * R0;
-    const unsigned x0 = cx > 0 ? cx - 1 : 0, x1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
-    const float4 *__restrict__ spos = S.spos;
-    for (int dz = -1; dz <= 1; ++dz) {
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int z = (int)cz + dz, y = (int)cy + dy;
-            unsigned b = 0, e = 0;
-            if (active && z >= 0 && z < (int)R2 && y >= 0 && y < (int)R1) {
-                const unsigned row = (unsigned)z * layer + (unsigned)y * R0;
-                b = __ldg(S.celloffset + row + x0);
-                e = __ldg(S.celloffset + row + x1) + __ldg(S.gridcount + row + x1);
-                if (e > S.pnum) e = S.pnum;
-                if (b > e) b = e;
-            }
-            const unsigned ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
-            const unsigned ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
-            if (ub < ue && ue - ub <= SPH_STAGE) {
-                __syncwarp();
-                for (unsigned t = lane; t < ue - ub; t += 32) wstage[t] = spos[ub + t];
-                __syncwarp();
-                for (unsigned kk = b; kk < e; ++kk) visit(xyz(wstage[kk - ub]));
-            } else {
-                for (unsigned kk = b; kk < e; ++kk) visit(xyz(spos[kk]));
-            }
+        if (MASK && active) {
+            const unsigned len = e - b;
+            S.nbmask[(size_t)(2 * r) * S.pnum + k] = (unsigned)bits;
+            if (len > 32) S.nbmask[(size_t)(2 * r + 1) * S.pnum + k] = (unsigned)(bits >> 32);
+            overflow |= len > 64;
+            total += len;
         }
     }
     if (active) {
@@ -127,13 +155,26 @@ __global__ void k_density(const SceneDesc *__restrict__ scenes, BlockMap map, in
             S.num_neighbours[i] = count;
             S.sdens[k] = value;
         }
-        if (mask) {
-            S.ncand[k] = cand;
-            const unsigned words = (min(cand, (unsigned)SPH_MASK_BITS) + 31u) >> 5;
-            for (unsigned w = 0; w < words; ++w)
-                S.nbmask[(size_t)w * S.pnum + k] = sm_mask[w * blockDim.x + threadIdx.x];
-        }
+        if (MASK) S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
     }
+}
+
+// Two instantiations, each skipping the other's scenes: the plane variant
+// (launched only when some scene has symmetry planes) keeps the common
+// plane-free loop free of its registers.
+template <bool PLANES>
+__global__ void __launch_bounds__(512, 2)
+    k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask) {
+    extern __shared__ float4 sm_stage[];
+    float4 *wstage = sm_stage + (threadIdx.x >> 5) * SPH_STAGE;
+    const unsigned lane = threadIdx.x & 31u;
+    SPH_FOR_WORK(map)
+    if ((S.num_symmetry_planes != 0) != PLANES) continue;
+    const unsigned n = active_count(S);
+    if (want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original)
+        density_one<PLANES, true>(S, n, item, lane, wstage, original);
+    else
+        density_one<PLANES, false>(S, n, item, lane, wstage, original);
     SPH_END_WORK
 }
 
@@ -157,9 +198,9 @@ __device__ __forceinline__ float cube_bound(float p, float f) {
 __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p);
 
 // One particle's fluid force, visiting its within-h neighbours either by
-// scanning the stencil (`masked` false) or through the candidate mask the
-// density pass recorded (`masked` true, SPH_MASK_BITS candidates at most;
-// a particle with more is scanned).  Both visit the same neighbours in the
+// scanning the stencil (`masked` false) or through the per-row candidate
+// masks the density pass recorded (`masked` true; a particle with a row of
+// more than 64 candidates is scanned).  Both visit the same neighbours in the
 // same order with the same arithmetic, so the results are identical.
 template <bool MASKED>
 __device__ __forceinline__ void fluid_force(const SceneDesc &S, unsigned k, int fuse_step) {
@@ -198,28 +239,32 @@ __device__ __forceinline__ void fluid_force(const SceneDesc &S, unsigned k, int 
     };
     const unsigned cell = S.gridcell[i];
     bool scanned = true;
-    if (MASKED) {
-        const unsigned cand = S.ncand[k];
-        if (cand <= SPH_MASK_BITS) {
-            scanned = false;
-            RowWalk rows(S, cell);
-            unsigned rb = 0, rl = 0, base = 0, total = 0;
-            bool have = rows.next(&rb, &rl);
-            const unsigned words = (cand + 31u) >> 5;
-            for (unsigned w = 0; w < words && have; ++w) {
-                unsigned m = S.nbmask[(size_t)w * S.pnum + k];
+    if (MASKED && S.ncand[k] != SPH_NCAND_SCAN) {
+        scanned = false;
+        const StencilRows rows(S, cell);
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+            unsigned m = S.nbmask[(size_t)(2 * r) * S.pnum + k];
+            unsigned rb, re;
+            rows.row(S, r, &rb, &re);
+            const unsigned len = re - rb;
+            // bits past the row's end cannot be set; the mask makes every
+            // visited index provably inside [rb, re)
+            m &= len >= 32 ? 0xffffffffu : (1u << len) - 1u;
+            while (m) {
+                const unsigned t = (unsigned)(__ffs(m) - 1);
+                m &= m - 1u;
+                pair(rb + t);
+            }
+            if (len > 32) {
+                m = S.nbmask[(size_t)(2 * r + 1) * S.pnum + k];
+                m &= len >= 64 ? 0xffffffffu : (1u << (len - 32)) - 1u;
                 while (m) {
-                    const unsigned b = (w << 5) + (unsigned)(__ffs(m) - 1);
+                    const unsigned t = (unsigned)(__ffs(m) - 1);
                     m &= m - 1u;
-                    while (have && b >= base + rl) {
-                        base += rl;
-                        have = rows.next(&rb, &rl);
-                    }
-                    if (!have) break;
-                    pair(rb + (b - base));
+                    pair(rb + 32u + t);
                 }
             }
-            (void)total;
         }
     }
     if (scanned) for_each_neighbour(S, cell, pair);

@@ -19,6 +19,9 @@ struct Launch {
     BlockMap pair_particles;  // `pair_block` items per entry
     unsigned grid_cap;        // upper bound on blocks per launch (persistent loop)
     cudaStream_t stream;
+    // no scene of the table has symmetry planes: the density pass's plane
+    // variant is not launched (false is always safe)
+    bool no_symmetry_planes;
 };
 
 enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2 };

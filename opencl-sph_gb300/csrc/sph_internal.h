@@ -82,9 +82,12 @@ struct SceneDesc {
     unsigned num_scan_blocks;
     unsigned *big_cells;      // [0] = count, [1..] = cells above SPH_SMALL_CELL
     unsigned *status;         // SphStatus bits
-    // candidate masks (fluids, fused substep): bit b of particle k's mask is
-    // set when its b-th stencil candidate lies within h; word w of sorted
-    // particle k at nbmask[w * pnum + k]; ncand[k] = its candidate count
+    // candidate masks (fluids, fused substep): bit t of stencil row r's
+    // 64-bit mask of sorted particle k is set when the row's t-th candidate
+    // lies within h; low word at nbmask[(2r) * pnum + k], high word at
+    // nbmask[(2r+1) * pnum + k] (written only for rows of more than 32
+    // candidates); ncand[k] = candidate count, or SPH_NCAND_SCAN when a row
+    // exceeds 64 and the force pass must scan
     unsigned *nbmask;
     unsigned *ncand;
     // batched form only (null otherwise): substeps this scene still takes;
@@ -94,10 +97,9 @@ struct SceneDesc {
 
 #define SPH_STEPS_UNLIMITED 0xffffffffu
 
-// Candidate-mask capacity (candidates per particle); more fall back to a
-// scan of the stencil.
-#define SPH_MASK_WORDS 16
-#define SPH_MASK_BITS (32 * SPH_MASK_WORDS)
+// Candidate masks: two words for each of the 9 stencil rows.
+#define SPH_MASK_WORDS 18
+#define SPH_NCAND_SCAN 0xffffffffu
 
 // Block map entry: block b of a launch works on `scene`, items
 // [first, first + block size).
