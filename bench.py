@@ -334,9 +334,10 @@ def bench_batched(args, torch, world):
 
 
 def bench_plain_loop(scs, steps):
-    """The plain per-scene loop: each scene through the drop-in path, one
-    sph_update substep at a time, scene after scene, waiting for each as the
-    reference's blocking calls do."""
+    """The plain per-scene loop: the scenes one after another through the
+    drop-in path.  Two forms: `synced` runs one sph_update substep at a time
+    and waits for it (the reference's blocking calls); `graph` runs each
+    scene's substeps as one sph_update call and waits once per scene."""
     systems = []
     for s in scs:
         ps = s.system()
@@ -350,33 +351,46 @@ def bench_plain_loop(scs, steps):
         for ps in systems:
             ps.update_fused(1)
             ps.synchronize()
-    el = time.perf_counter() - t0
+    synced = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for ps in systems:
+        ps.update_fused(steps)
+        ps.synchronize()
+    graph = time.perf_counter() - t0
     for ps in systems:
         ps.close()
     n = sum(s.n for s in scs)
-    return {"value": n * steps / el, "unit": UNIT, "s": el}
+    return {"synced": n * steps / synced, "graph": n * steps / graph}
 
 
 def plain_step_model(sizes, steps=20):
-    """Measured seconds per drop-in substep for WCSPH scenes of given sizes
-    (for the sequential-server model); returns a log-log interpolator."""
+    """Measured seconds per drop-in substep (sph_update loop, one sync at
+    the end) for scenes of the mix of each material at the given sizes;
+    returns model(material, n), a log-log interpolation."""
     from sph import scenes
-    pts = []
-    for n_target in sizes:
-        d = max(2, int(round((n_target / 0.5) ** (1 / 3))))
-        sc = scenes.wcsph_block(d, max(2, d // 2), d, seed=1)
-        ps = sc.system()
-        ps.update_fused(2)
-        ps.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            ps.update_fused(1)
+    table = {}
+    for material in scenes.MATERIALS:
+        pts = []
+        for n_target in sizes:
+            sc = scenes.mix_member(material, n_target, seed=1)
+            ps = sc.system()
+            if material != "fluid":
+                ps.call_for_all_particles("init_original_position")
+                ps.compute_particle_bins()
+                ps.call_for_all_particles("compute_original_density")
+            ps.update_fused(3)
             ps.synchronize()
-        pts.append((sc.n, (time.perf_counter() - t0) / steps))
-        ps.close()
-    xs = np.log([p[0] for p in pts])
-    ys = np.log([p[1] for p in pts])
-    return lambda n: float(np.exp(np.interp(np.log(n), xs, ys)))
+            t0 = time.perf_counter()
+            ps.update_fused(steps)
+            ps.synchronize()
+            pts.append((sc.n, (time.perf_counter() - t0) / steps))
+            ps.close()
+        table[material] = (np.log([p[0] for p in pts]), np.log([p[1] for p in pts]))
+
+    def model(material, n):
+        xs, ys = table[material]
+        return float(np.exp(np.interp(np.log(n), xs, ys)))
+    return model
 
 
 def bench_served(args):
@@ -388,16 +402,7 @@ def bench_served(args):
     from sph.serving import Server, poisson_requests, release, sequential_fifo
 
     def make(rng, i):
-        n_target = math.exp(rng.uniform(math.log(2000), math.log(262144)))
-        kind = rng.choice(3, p=[0.6, 0.25, 0.15])
-        if kind == 0:
-            d = max(2, int(round((n_target / 0.5) ** (1 / 3))))
-            return scenes.wcsph_block(d, max(2, d // 2), d, seed=i, name="q%d" % i)
-        d = max(2, int(round((n_target / 2.0) ** (1 / 3))))
-        return scenes.solid_lattice(d, d, 2 * d, material="corot" if kind == 1 else "svk",
-                                    youngs_modulus=math.exp(rng.uniform(math.log(1e4), math.log(1e6))),
-                                    poisson=rng.uniform(0.25, 0.45), jitter=1e-4, seed=i, clamp_layers=1,
-                                    name="q%d" % i)
+        return scenes.mixed_scene(rng, i, n_range=(2000, 262144), prefix="q")
     reqs = poisson_requests(rate=50.0, duration=args.served_seconds, make_scene=make, steps_range=(100, 2000),
                             seed=args.seed)
     srv = Server(budget_bytes=150e9, max_chunk=25, max_particles=8 << 20, keep_results=False)
@@ -405,7 +410,7 @@ def bench_served(args):
     st = srv.run(reqs, realtime=True)
     demand = sum(r.work for r in reqs) / args.served_seconds
     model = plain_step_model([2000, 16000, 131072, 262144])
-    seq = sequential_fifo(reqs, lambda r: r.steps * model(r.scene.n))
+    seq = sequential_fifo(reqs, lambda r: r.steps * model(r.scene.material, r.scene.n))
     release(reqs)
     return {"requests": st["requests"], "arrival_rate_per_s": 50.0, "window_s": args.served_seconds,
             "throughput": st["throughput"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
@@ -416,8 +421,9 @@ def bench_served(args):
                       "quotas; chunks of up to 25 substeps",
             "sequential_plain_model": {"throughput": seq["throughput"], "p50_s": seq["p50_s"],
                                        "p99_s": seq["p99_s"],
-                                       "how": "FIFO queue of one-at-a-time drop-in solves, per-substep times "
-                                              "measured on this GPU at 2k-262k particles"}}
+                                       "how": "FIFO queue of one-at-a-time drop-in solves (sph_update loops), "
+                                              "per-substep times measured on this GPU per material at 2k-262k "
+                                              "particles"}}
 
 
 def fp64_error_sample(scs, steps):
@@ -532,11 +538,15 @@ def run_ours(args, rank, world, local_rank):
             extra["autotune"] = t
         l2 = "working set %.2f GB > L2 (129 MB); no flush needed" % (r["n"] * 300e-9)
         if rank == 0 and not args.quick:
-            pl = bench_plain_loop(r["scenes"], max(3, args.steps // 4))
-            extra["plain_per_scene"] = {"value": pl["value"], "unit": UNIT,
-                                        "how": "same 256 scenes through the drop-in path, one sph_update "
-                                               "substep per scene per step, waiting for each"}
-            extra["batched_vs_plain"] = (r["n"] * args.steps / r["total_s"]) / pl["value"]
+            pl = bench_plain_loop(r["scenes"], max(3, args.steps // 2))
+            batched = r["n"] * args.steps / r["total_s"]
+            extra["plain_per_scene"] = {
+                "value": pl["graph"], "unit": UNIT, "synced_value": pl["synced"],
+                "how": "the same 256 scenes through the drop-in path one after another: value = each scene's "
+                       "substeps as one sph_update call (graph launches back to back, one wait per scene); "
+                       "synced_value = one substep per call, waiting for each (the reference's blocking calls)"}
+            extra["batched_vs_plain"] = batched / pl["graph"]
+            extra["batched_vs_plain_synced"] = batched / pl["synced"]
             extra["fp64_error"] = fp64_error_sample(r["scenes"], 100)
             extra["served"] = bench_served(args)
             sc1m, d1m = workload("wcsph-1m", args.seed)

@@ -22,6 +22,7 @@ namespace {
 struct BatchScene {
     unsigned programs = 0;
     int material = -1;
+    std::vector<unsigned> rigid;  // rigid bodies (1-based), from the host store at add
     char *mem = nullptr;     // blob followed by scratch
     size_t bytes = 0;
     size_t blob_size = 0;
@@ -153,6 +154,11 @@ bool rebuild(sph_batch *b) {
     size_t o_pp = t.add(all.pair_particles.data(), all.pair_particles.size() * sizeof(BlockWork));
     size_t o_c = t.add(all.cells.data(), all.cells.size() * sizeof(BlockWork));
     size_t o_s = t.add(all.scan.data(), all.scan.size() * sizeof(BlockWork));
+    std::vector<RigidWork> rigid;
+    for (unsigned k = 0; k < descs.size(); ++k)
+        for (unsigned body : b->slots[ids[k]]->rigid)
+            if (rigid.size() < SPH_MAX_RIGID_WORK) rigid.push_back(RigidWork{k, body});
+    size_t o_rw = t.add(rigid.data(), rigid.size() * sizeof(RigidWork));
     size_t o_gp[3], o_gpp[3];
     for (int m = 0; m < 3; ++m) {
         o_gp[m] = t.add(g[m].particles.data(), g[m].particles.size() * sizeof(BlockWork));
@@ -177,6 +183,8 @@ bool rebuild(sph_batch *b) {
     A.pair_block = b->pair_block;
     A.grid_cap = cap_of(b);
     A.stream = b->stream;
+    A.rigid = rigid.empty() ? nullptr : reinterpret_cast<const RigidWork *>(d + o_rw);
+    A.num_rigid = (unsigned)rigid.size();
     A.no_symmetry_planes = std::all_of(descs.begin(), descs.end(),
                                        [](const SceneDesc &d) { return d.num_symmetry_planes == 0; });
     cudaStream_t streams[3] = {b->stream, b->side[0], b->side[1]};
@@ -214,6 +222,7 @@ bool rebuild(sph_batch *b) {
             cudaStreamWaitEvent(b->stream, b->join[m - 1], 0);
         }
     }
+    sph_launch_rigid(A);
     sph_launch_count_down(A);
     cudaError_t le = cudaGetLastError();
     cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
@@ -326,10 +335,15 @@ extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list)
     bool good = ok(cudaMemcpyAsync(sc->mem, scene->data, sc->blob_size, cudaMemcpyHostToDevice, b->stream),
                    "sph_batch_add upload") &&
                 ok(cudaMemsetAsync(sc->desc.status, 0, 4, b->stream), "sph_batch_add") &&
+                (!sc->desc.rigid_state ||
+                 ok(cudaMemsetAsync(sc->desc.rigid_state, 0, 8ull * sc->desc.body_capacity * SPH_RIGID_STRIDE,
+                                    b->stream),
+                    "sph_batch_add")) &&
                 ok((sph_launch_set_steps(sc->desc.steps_left, SPH_STEPS_UNLIMITED, b->stream), cudaGetLastError()),
                    "sph_batch_add") &&
                 ok(cudaStreamSynchronize(b->stream), "sph_batch_add upload");
     if (good && material != MAT_FLUID) good = solid_setup(b, sc);
+    if (good) sc->rigid = sph_rigid_bodies(*scene, sc->desc);
     if (!good) {
         cudaFreeAsync(sc->mem, b->stream);
         delete sc;
@@ -463,6 +477,10 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
                 sph_launch_forces_solids(G, m == MAT_COROT);
                 sph_launch_step_forward(G);
             }
+        }
+        if (A.num_rigid) {
+            log.mark("rigid bodies");
+            sph_launch_rigid(A);
         }
         sph_launch_count_down(A);
         log.mark(nullptr);

@@ -81,6 +81,9 @@ struct Store {
     Launch L{};
     cudaGraphExec_t step_graph = nullptr;
     unsigned graph_kernels = 0;
+    std::vector<unsigned> rigid;   // rigid bodies (1-based), as last read from the host store
+    RigidWork *d_rigid = nullptr;  // device list, room for every body
+    unsigned rigid_room = 0;
 };
 
 std::mutex g_stores_mu;
@@ -110,6 +113,37 @@ void destroy(Store *s) {
     delete s;
 }
 
+// Re-reads which bodies are rigid from the host store; a change of the
+// list re-records the substep graph.
+bool refresh_rigid(Store *s, const psdata &data) {
+    std::vector<unsigned> now = sph_rigid_bodies(data, s->desc);
+    if (now.size() > s->rigid_room) now.resize(s->rigid_room);
+    if (now == s->rigid) return true;
+    std::vector<RigidWork> w;
+    for (unsigned b : now) w.push_back(RigidWork{0u, b});
+    if (!w.empty() &&
+        !cuda_ok(cudaMemcpyAsync(s->d_rigid, w.data(), w.size() * sizeof(RigidWork), cudaMemcpyHostToDevice,
+                                 s->stream),
+                 "rigid body list") )
+        return false;
+    // the list is read by launches already queued: let them finish first
+    if (!cuda_ok(cudaStreamSynchronize(s->stream), "rigid body list")) return false;
+    s->rigid = now;
+    s->L.num_rigid = (unsigned)now.size();
+    if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
+    s->step_graph = nullptr;
+    s->graph_kernels = 0;
+    return true;
+}
+
+// Fields the rigid bodies are set up from.
+bool touches_rigid_setup(const char *name) {
+    static const char *kNames[] = {"position", "velocity", "body_number", "body_dynamic", "body_count", "n"};
+    for (const char *k : kNames)
+        if (!strcmp(name, k)) return true;
+    return false;
+}
+
 // Builds the device mirror of a host store.
 Store *create_store(psdata *data, const char *file_list, std::string *err) {
     unsigned programs = sph_parse_programs(file_list, err);
@@ -135,7 +169,9 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     size_t o_ppm = o_pm + Arena::align(maps.particles.size() * sizeof(BlockWork));
     size_t o_cm = o_ppm + Arena::align(maps.pair_particles.size() * sizeof(BlockWork));
     size_t o_sm = o_cm + Arena::align(maps.cells.size() * sizeof(BlockWork));
-    size_t total = o_sm + Arena::align(maps.scan.size() * sizeof(BlockWork));
+    size_t o_rw = o_sm + Arena::align(maps.scan.size() * sizeof(BlockWork));
+    s->rigid_room = std::min(probe.body_capacity, SPH_MAX_RIGID_WORK);
+    size_t total = o_rw + Arena::align(s->rigid_room * sizeof(RigidWork));
 
     if (!cuda_ok(sph_prepare_kernels(), "kernel attributes") ||
         !cuda_ok(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate") ||
@@ -152,6 +188,7 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     sph_place_scratch(&s->desc, b + o_scratch);
     s->desc.steps_left = nullptr;  // a single store has no substep quota
     s->d_desc = reinterpret_cast<SceneDesc *>(b + o_desc);
+    s->d_rigid = s->rigid_room ? reinterpret_cast<RigidWork *>(b + o_rw) : nullptr;
     auto up = [&](size_t off, const void *src, size_t bytes) {
         return bytes == 0 || cuda_ok(cudaMemcpyAsync(b + off, src, bytes, cudaMemcpyHostToDevice, s->stream),
                                      "cudaMemcpy(store)");
@@ -162,6 +199,10 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
               up(o_cm, maps.cells.data(), maps.cells.size() * sizeof(BlockWork)) &&
               up(o_sm, maps.scan.data(), maps.scan.size() * sizeof(BlockWork)) &&
               cuda_ok(cudaMemsetAsync(s->desc.status, 0, 4, s->stream), "cudaMemset(status)") &&
+              (!s->desc.rigid_state ||
+               cuda_ok(cudaMemsetAsync(s->desc.rigid_state, 0, 8ull * s->desc.body_capacity * SPH_RIGID_STRIDE,
+                                       s->stream),
+                       "cudaMemset(rigid)")) &&
               cuda_ok(cudaStreamSynchronize(s->stream), "create_psdata_cuda");
     if (!ok) {
         *err = sph_last_error();
@@ -180,6 +221,13 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     L.grid_cap = 1u << 30;
     L.stream = s->stream;
     L.no_symmetry_planes = s->desc.num_symmetry_planes == 0;
+    L.rigid = s->d_rigid;
+    L.num_rigid = 0;
+    if (!refresh_rigid(s, *data)) {
+        *err = sph_last_error();
+        destroy(s);
+        return nullptr;
+    }
     {
         std::lock_guard<std::mutex> lk(g_stores_mu);
         g_stores.insert(s);
@@ -223,7 +271,11 @@ bool dispatch(Store *s, const char *name) {
         sph_launch_density(L, false);
         return true;
     }
-    if (k == "step_forward") { sph_launch_step_forward(L); return true; }
+    if (k == "step_forward") {
+        sph_launch_step_forward(L);
+        sph_launch_rigid(L);  // rigid bodies (extension) take their step with the particles'
+        return true;
+    }
     if (k == "compute_forces_fluids") {
         if (!need(PROG_FLUIDS, "fluids")) return false;
         sph_launch_gather(L, true, true);
@@ -376,7 +428,11 @@ extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int ful
             sph_set_error("store layout differs from the device copy");
             return false;
         }
-        return cuda_ok(cudaMemcpyAsync(s->d_blob, data.data, sz, cudaMemcpyHostToDevice, s->stream), "sync");
+        if (!cuda_ok(cudaMemcpyAsync(s->d_blob, data.data, sz, cudaMemcpyHostToDevice, s->stream), "sync") ||
+            !refresh_rigid(s, data))
+            return false;
+        if (s->desc.rigid_state) sph_launch_rigid_reset(s->L);
+        return true;
     });
 }
 
@@ -384,8 +440,15 @@ extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int ful
 extern "C" void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso, size_t num_fields,
                                                   const char *const *names) {
     with_store(pso, "sync_psdata_fields_host_to_device", true, [&](Store *s) {
-        for (size_t i = 0; i < num_fields; ++i)
+        bool rigid = false;
+        for (size_t i = 0; i < num_fields; ++i) {
             if (names[i] && !copy_field(s, data, names[i], true)) return false;
+            rigid = rigid || (names[i] && touches_rigid_setup(names[i]));
+        }
+        if (rigid && s->desc.rigid_state) {
+            if (!refresh_rigid(s, data)) return false;
+            sph_launch_rigid_reset(s->L);
+        }
         return true;
     });
 }
@@ -435,6 +498,7 @@ extern "C" void populate_position_cuboid_device_cuda(psdata_cuda pso, float x1, 
         const unsigned sz[3] = {xs, ys, zs};
         if (xs == 0 || ys == 0 || zs == 0) return true;
         sph_launch_populate_cuboid(s->L, c1, c2, sz);
+        if (s->desc.rigid_state) sph_launch_rigid_reset(s->L);
         return true;
     });
 }
@@ -442,6 +506,7 @@ extern "C" void populate_position_cuboid_device_cuda(psdata_cuda pso, float x1, 
 extern "C" void rotate_particles_device_cuda(psdata_cuda pso, float ax, float ay, float az) {
     with_store(pso, "rotate_particles", false, [&](Store *s) {
         sph_launch_rotate_particles(s->L, ax, ay, az);
+        if (s->desc.rigid_state) sph_launch_rigid_reset(s->L);
         return true;
     });
 }

@@ -4,6 +4,7 @@
 
 #include "kernels_fluid.cuh"
 #include "kernels_grid.cuh"
+#include "kernels_rigid.cuh"
 #include "kernels_solid.cuh"
 #include "launch.h"
 
@@ -177,6 +178,10 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     if (mat == MAT_FLUID) {
         phase("forces_fluids+step");
         sph_launch_forces_fluids(L, true, true);
+        if (L.num_rigid) {
+            phase("rigid_bodies");
+            sph_launch_rigid(L);
+        }
         phase(nullptr);
         return;
     }
@@ -193,7 +198,24 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     sph_launch_forces_solids(L, mat == MAT_COROT);
     phase("step_forward");
     sph_launch_step_forward(L);
+    if (L.num_rigid) {
+        phase("rigid_bodies");
+        sph_launch_rigid(L);
+    }
     phase(nullptr);
+}
+
+void sph_launch_rigid(const Launch &L) {
+    if (!L.num_rigid || !L.rigid) return;
+    const dim3 grid(SPH_RIGID_BLOCKS, L.num_rigid);
+    k_rigid_reduce<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
+    k_rigid_integrate<<<(L.num_rigid + 63) / 64, 64, 0, L.stream>>>(L.scenes, L.rigid, L.num_rigid);
+    k_rigid_scatter<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
+}
+
+void sph_launch_rigid_reset(const Launch &L) {
+    const unsigned g = L.num_scenes < 1024 ? L.num_scenes : 1024;
+    k_rigid_reset<<<g ? g : 1, 64, 0, L.stream>>>(L.scenes, L.num_scenes);
 }
 
 // End of a batched substep: each scene with a finite quota left uses one.

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "kernels_common.cuh"
+#include "kernels_rigid.cuh"
 
 #define SPH_PI_F 3.1415926535f
 
@@ -291,15 +292,13 @@ __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, Blo
 }
 
 // step_forward (common.cl:691-722): a = f/m + g, v += dt a, x += dt v;
-// particles of a fixed (non-dynamic) body are skipped.  An optional
+// particles of a fixed (non-dynamic) body are skipped, and so are those of
+// a rigid body (extension), which its own step moves.  An optional
 // `wallbounds` field (extension) mirrors particles that leave the box back
 // inside and reverses their normal velocity.
 __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p) {
-    if (S.body_number) {
-        // a body number beyond body_dynamic's size is treated as dynamic
-        unsigned b = S.body_number[i];
-        if (b > 0 && b <= S.body_capacity && !S.body_dynamic[b - 1]) return;
-    }
+    // fixed bodies stay put; rigid bodies are moved by k_rigid_scatter
+    if (body_skips_step(S, i)) return;
     const float m = *S.mass, dt = *S.timestep;
     const float3 g = make_float3(S.gravity[0], S.gravity[1], S.gravity[2]);
     const float3 a = make_float3(f.x / m + g.x, f.y / m + g.y, f.z / m + g.z);

@@ -22,7 +22,13 @@ struct Launch {
     // no scene of the table has symmetry planes: the density pass's plane
     // variant is not launched (false is always safe)
     bool no_symmetry_planes;
+    // rigid bodies of the table (device list; none when num_rigid is 0)
+    const RigidWork *rigid;
+    unsigned num_rigid;
 };
+
+// At most this many rigid bodies per launch (the reduction grid's y extent).
+#define SPH_MAX_RIGID_WORK 65535u
 
 enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2 };
 
@@ -50,6 +56,11 @@ void sph_launch_set_body_position(const Launch &L, unsigned body, const float po
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
 void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);
 void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
+// Rigid bodies: force/torque sums, body substep and particle placement
+// (after the material's step), and the reset that sets bodies up again
+// from their particles' current state.
+void sph_launch_rigid(const Launch &L);
+void sph_launch_rigid_reset(const Launch &L);
 // Batched form: the end-of-substep quota count-down over all scenes, and a
 // stream-ordered write of one scene's quota.
 void sph_launch_count_down(const Launch &L);

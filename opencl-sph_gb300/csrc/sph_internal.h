@@ -93,6 +93,29 @@ struct SceneDesc {
     // batched form only (null otherwise): substeps this scene still takes;
     // at 0 every kernel skips the scene, SPH_STEPS_UNLIMITED never expires
     unsigned *steps_left;
+    // rigid bodies (extension; present when the store has body fields):
+    // per body SPH_RIGID_STRIDE doubles of state, the reduction's per-block
+    // partial sums, and each rigid particle's offset from its body's centre
+    // in the body frame
+    double *rigid_state;
+    double *rigid_partial;
+    float4 *rigid_offset;
+};
+
+// body_dynamic value that makes a body rigid (extension): its particles
+// move with the body's rigid motion, driven by the sum of their forces.
+// 0 (fixed) and any other value (free particles) keep the reference's
+// meaning.
+#define SPH_BODY_RIGID 2u
+#define SPH_RIGID_BLOCKS 32     // reduction blocks per body
+#define SPH_RIGID_THREADS 256
+#define SPH_RIGID_Q 24          // reduced quantities per body
+#define SPH_RIGID_STRIDE 64     // doubles of state per body
+
+// One rigid body of one scene (body is 1-based, as body_number).
+struct RigidWork {
+    unsigned scene;
+    unsigned body;
 };
 
 #define SPH_STEPS_UNLIMITED 0xffffffffu

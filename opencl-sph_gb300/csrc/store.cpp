@@ -279,6 +279,15 @@ bool sph_resolve_scene(const psdata &h, char *d, unsigned programs, SceneDesc *d
     return true;
 }
 
+// Rigid-body state, partial sums and per-particle offsets, for stores
+// with body fields.
+static size_t rigid_bytes(const SceneDesc &d) {
+    if (!d.body_capacity) return 0;
+    const size_t B = d.body_capacity;
+    return Arena::align(8 * B * SPH_RIGID_STRIDE) + Arena::align(8 * B * SPH_RIGID_BLOCKS * SPH_RIGID_Q) +
+           Arena::align(16ull * d.pnum);
+}
+
 size_t sph_scratch_bytes(const SceneDesc &d) {
     size_t P = d.pnum;
     return Arena::align(4 * P)               // slot
@@ -290,7 +299,8 @@ size_t sph_scratch_bytes(const SceneDesc &d) {
            + Arena::align(4)                 // status
            + Arena::align(4ull * SPH_MASK_WORDS * P)  // nbmask
            + Arena::align(4 * P)             // ncand
-           + Arena::align(4);                // steps_left
+           + Arena::align(4)                 // steps_left
+           + rigid_bytes(d);
 }
 
 void sph_place_scratch(SceneDesc *d, char *base) {
@@ -314,6 +324,34 @@ void sph_place_scratch(SceneDesc *d, char *base) {
     d->ncand = reinterpret_cast<unsigned *>(base + o);
     o += Arena::align(4 * P);
     d->steps_left = reinterpret_cast<unsigned *>(base + o);
+    o += Arena::align(4);
+    d->rigid_state = nullptr;
+    d->rigid_partial = nullptr;
+    d->rigid_offset = nullptr;
+    if (d->body_capacity) {
+        const size_t B = d->body_capacity;
+        d->rigid_state = reinterpret_cast<double *>(base + o);
+        o += Arena::align(8 * B * SPH_RIGID_STRIDE);
+        d->rigid_partial = reinterpret_cast<double *>(base + o);
+        o += Arena::align(8 * B * SPH_RIGID_BLOCKS * SPH_RIGID_Q);
+        d->rigid_offset = reinterpret_cast<float4 *>(base + o);
+    }
+}
+
+std::vector<unsigned> sph_rigid_bodies(const psdata &h, const SceneDesc &d) {
+    std::vector<unsigned> out;
+    const int f = get_field_psdata(h, "body_dynamic");
+    if (f < 0 || !d.body_capacity || !d.rigid_state) return out;
+    const unsigned *dyn = reinterpret_cast<const unsigned *>(static_cast<const char *>(h.data) + h.data_offsets[f]);
+    unsigned count = d.body_capacity;
+    const int c = get_field_psdata(h, "body_count");
+    if (c >= 0) {
+        const unsigned bc = *reinterpret_cast<const unsigned *>(static_cast<const char *>(h.data) + h.data_offsets[c]);
+        count = std::min(count, bc);
+    }
+    for (unsigned b = 0; b < count; ++b)
+        if (dyn[b] == SPH_BODY_RIGID) out.push_back(b + 1);
+    return out;
 }
 
 void sph_build_maps(const std::vector<SceneDesc> &descs, const std::vector<unsigned> &ids, unsigned block,

@@ -31,6 +31,10 @@ int sph_material_of(unsigned programs);
 size_t sph_scratch_bytes(const SceneDesc &d);
 void sph_place_scratch(SceneDesc *d, char *base);
 
+// Rigid bodies of a host store (extension): the 1-based numbers of the
+// bodies whose body_dynamic is SPH_BODY_RIGID, among the first body_count.
+std::vector<unsigned> sph_rigid_bodies(const psdata &h, const SceneDesc &d);
+
 // Block maps for a table of scenes (host vectors; BlockWork entries).
 struct HostMaps {
     std::vector<BlockWork> particles, pair_particles, cells, scan;

@@ -9,7 +9,9 @@ workloads of the benchmark (all synthetic; no dataset is involved):
 * :func:`solid_lattice` -- corotational or St. Venant-Kirchhoff solid
   lattice with clamped layers (the 10x10x40 beam);
 * :func:`batch_mix` -- many uneven scenes, 60% fluid / 25% corotational /
-  15% SVK, particle counts log-uniform.
+  15% SVK, particle counts log-uniform;
+* :func:`rigid_body_scene` -- a rigid ball (the rigid-body extension),
+  alone or dropped into a fluid block.
 
 Lattices are x-fastest, so particle order follows the grid's cell order.
 """
@@ -128,6 +130,52 @@ def wcsph_block(nx=20, ny=20, nz=20, spacing=0.01, h=0.02, box=(0.0, 0.4), jitte
     return Scene(name or "wcsph-%d" % n, "fluid", FLUID_KERNELS, entries, {"position": pos, "n": n}, n)
 
 
+def ball(radius, spacing, center):
+    """Lattice points within `radius` of `center` (x-fastest order)."""
+    k = int(math.floor(radius / spacing))
+    g = np.arange(-k, k + 1) * spacing
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    p = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    p = p[np.sum(p * p, axis=1) <= radius * radius * (1 + 1e-9)]
+    return (p + np.asarray(center, dtype=np.float64)).astype(np.float32)
+
+
+def rigid_body_scene(radius=0.05, spacing=0.01, h=0.02, center=(0.2, 0.2, 0.2), velocity=(0.0, 0.0, 0.0),
+                     omega=(0.0, 0.0, 0.0), fluid=None, box=(0.0, 0.4), gravity=(0.0, -9.8, 0.0), dt=1e-4,
+                     restdens=1000.0, stiffness=3.0, viscosity=0.2, jitter=1e-4, seed=0, walls=True, name=None):
+    """A rigid ball (body 1, body_dynamic = 2: the rigid-body extension) of
+    lattice particles, optionally in a WCSPH fluid block `fluid` = (nx, ny,
+    nz) filling the low corner of the box.  The ball starts with linear
+    velocity `velocity` and angular velocity `omega` about its centre.  The
+    ball's particles come after the fluid's; they carry the store's particle
+    mass, so the ball is as dense as the fluid."""
+    rng = np.random.default_rng(seed)
+    parts, body = [], []
+    if fluid is not None:
+        f = lattice(*fluid, spacing, origin=(box[0] + spacing / 2,) * 3, jitter=jitter, rng=rng)
+        parts.append(f)
+        body.append(np.zeros(len(f), np.uint32))
+    b = ball(radius, spacing, center)
+    parts.append(b)
+    body.append(np.ones(len(b), np.uint32))
+    pos = np.concatenate(parts).astype(np.float32)
+    bn = np.concatenate(body)
+    n = len(pos)
+    vel = np.zeros((n, 3), np.float32)
+    r = b.astype(np.float64) - np.asarray(center, dtype=np.float64)
+    vel[bn == 1] = (np.asarray(velocity, dtype=np.float64) + np.cross(np.asarray(omega, dtype=np.float64), r))
+    mass = restdens * spacing ** 3
+    gb = [box[0], box[1]] * 3
+    entries = _common_entries(n, mass, dt, h, gravity, gb)
+    entries += [("restdens", "1", "float", restdens), ("stiffness", "1", "float", stiffness),
+                ("viscosity", "1", "float", viscosity), ("body_position", "3, body_count", "float", None)]
+    if walls:
+        entries.append(("wallbounds", "6", "float", gb))
+    init = {"position": pos, "n": n, "velocity": vel, "body_number": bn,
+            "body_dynamic": np.array([2], np.uint32)}
+    return Scene(name or "rigid-%d" % n, "fluid", FLUID_KERNELS, entries, init, n)
+
+
 def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", youngs_modulus=1e5,
                   poisson=0.3, density=1000.0, viscosity=6e-5, gravity=(0.0, -9.8, 0.0), dt=5e-5,
                   clamp_layers=2, jitter=0.0, seed=0, margin=None, name=None):
@@ -180,30 +228,44 @@ def _dims_for(n_target, aspect=(1.0, 1.0, 1.0)):
     return int(d[0]), int(d[1]), int(d[2])
 
 
-def batch_mix(count=256, seed=0, n_range=(1000, 65536), mix=(0.6, 0.25, 0.15), e_range=(1e4, 1e6),
-              nu_range=(0.25, 0.45), spacing=0.01, h=0.02, dt_fluid=1e-4, dt_solid=5e-5, jitter=1e-4):
-    """`count` independent scenes: particle counts log-uniform in n_range,
+MATERIALS = ("fluid", "corot", "svk")
+
+
+def mix_member(material, n_target, seed=0, youngs_modulus=1e5, poisson=0.3, spacing=0.01, h=0.02, dt_fluid=1e-4,
+               dt_solid=5e-5, jitter=1e-4, name=None):
+    """A scene of the batched/served mix with about n_target particles.  A
+    fluid block is 1 x 1/2 x 1 and sits in a box twice its width (room to
+    collapse); a solid is a 1 x 1 x 2 beam clamped at one end."""
+    if material == "fluid":
+        nx, ny, nz = _dims_for(n_target, (1.0, 0.5, 1.0))
+        ext = max(nx, nz) * spacing
+        box_hi = 2.0 * ext + 4 * h
+        return wcsph_block(nx, ny, nz, spacing=spacing, h=h, box=(0.0, box_hi), jitter=jitter, seed=seed,
+                           dt=dt_fluid, name=name)
+    nx, ny, nz = _dims_for(n_target, (1.0, 1.0, 2.0))
+    return solid_lattice(nx, ny, nz, spacing=spacing, h=h, material=material, youngs_modulus=youngs_modulus,
+                         poisson=poisson, dt=dt_solid, clamp_layers=1, jitter=jitter, seed=seed, name=name)
+
+
+def mixed_scene(rng, index, n_range=(1000, 65536), mix=(0.6, 0.25, 0.15), e_range=(1e4, 1e6),
+                nu_range=(0.25, 0.45), prefix="b", **kw):
+    """One random scene of the mix: particle count log-uniform in n_range,
     material drawn with probabilities `mix` (fluid, corotational, SVK),
     Young's modulus log-uniform in e_range, Poisson ratio uniform in
-    nu_range; seeded lattice jitter."""
+    nu_range; seeded lattice jitter (see mix_member)."""
+    n_target = math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))
+    kind = int(rng.choice(3, p=np.asarray(mix) / np.sum(mix)))
+    sub = int(rng.integers(1 << 30))
+    material = MATERIALS[kind]
+    if kind == 0:
+        return mix_member(material, n_target, seed=sub, name="%s%03d-fluid" % (prefix, index), **kw)
+    E = math.exp(rng.uniform(math.log(e_range[0]), math.log(e_range[1])))
+    nu = rng.uniform(*nu_range)
+    return mix_member(material, n_target, seed=sub, youngs_modulus=E, poisson=nu,
+                      name="%s%03d-%s" % (prefix, index, material), **kw)
+
+
+def batch_mix(count=256, seed=0, **kw):
+    """`count` independent scenes of the mix (see mixed_scene)."""
     rng = np.random.default_rng(seed)
-    scenes = []
-    for s in range(count):
-        n_target = math.exp(rng.uniform(math.log(n_range[0]), math.log(n_range[1])))
-        kind = rng.choice(3, p=np.asarray(mix) / np.sum(mix))
-        sub = int(rng.integers(1 << 30))
-        if kind == 0:
-            nx, ny, nz = _dims_for(n_target, (1.0, 0.5, 1.0))
-            ext = max(nx, nz) * spacing
-            box_hi = 2.0 * ext + 4 * h
-            scenes.append(wcsph_block(nx, ny, nz, spacing=spacing, h=h, box=(0.0, box_hi), jitter=jitter,
-                                      seed=sub, dt=dt_fluid, name="b%03d-fluid" % s))
-        else:
-            nx, ny, nz = _dims_for(n_target, (1.0, 1.0, 2.0))
-            E = math.exp(rng.uniform(math.log(e_range[0]), math.log(e_range[1])))
-            nu = rng.uniform(*nu_range)
-            mat = "corot" if kind == 1 else "svk"
-            scenes.append(solid_lattice(nx, ny, nz, spacing=spacing, h=h, material=mat, youngs_modulus=E,
-                                        poisson=nu, dt=dt_solid, clamp_layers=1, jitter=jitter, seed=sub,
-                                        name="b%03d-%s" % (s, mat)))
-    return scenes
+    return [mixed_scene(rng, s, **kw) for s in range(count)]

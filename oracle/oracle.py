@@ -61,7 +61,10 @@ def _state_type(real):
         ("num_neighbours", U), ("gridcell", U), ("gridcount", U), ("celloffset", U), ("cellparticles", U),
         ("has_wallbounds", c_uint), ("wallbounds", real * 6),
         ("guards", c_int), ("nthreads", c_int),
+        ("body_capacity", c_uint), ("rigid_state", POINTER(c_double)), ("rigid_offset", P),
     ]})
+
+RIGID_STRIDE = 64  # ORACLE_RIGID_STRIDE
 
 
 _STATES = {"f32": _state_type(c_float), "f64": _state_type(c_double)}
@@ -84,7 +87,7 @@ class OracleScene(object):
                "compute_original_density", "compute_density", "compute_forces_fluids",
                "compute_rotations_and_strains", "compute_stresses_corot", "compute_forces_solids_corot",
                "compute_deformations", "compute_stresses_svk", "compute_forces_solids_svk", "step_forward",
-               "apply_plane_constraints"]
+               "apply_plane_constraints", "rigid_step"]
 
     def __init__(self, fields, prec="f32", nthreads=1, guards=3):
         """`fields`: name -> array as given by ParticleSystem.get_fields
@@ -127,7 +130,8 @@ class OracleScene(object):
 
         self.a["symmetry_planes"], nsp = planes("symmetry_planes")
         self.a["plane_constraints"], npc = planes("plane_constraints")
-        bd = np.asarray(fields.get("body_dynamic", np.zeros(1)), dtype=np.uint32).reshape(-1)
+        # a copy: the oracle must not alias the store it was built from
+        bd = np.array(fields.get("body_dynamic", np.zeros(1)), dtype=np.uint32).reshape(-1)
         self.a["body_dynamic"] = np.ascontiguousarray(bd if bd.size else np.zeros(1, np.uint32))
         for name in ("body_position", "body_euler_rotation"):
             v = np.asarray(fields.get(name, np.zeros((1, 3))), dtype=np.float64).reshape(-1, 3)
@@ -151,6 +155,11 @@ class OracleScene(object):
             st.wallbounds[:] = [float(x) for x in np.ravel(fields["wallbounds"])[:6]]
         st.guards = guards
         st.nthreads = nthreads
+        # rigid bodies (extension): state per body, offsets per particle
+        st.body_capacity = int(self.a["body_dynamic"].size)
+        self.rigid_state = np.zeros((st.body_capacity, RIGID_STRIDE), np.float64)
+        self.a["rigid_offset"] = np.zeros((P, 3), dtype=self.T)
+        st.rigid_state = self.rigid_state.ctypes.data_as(POINTER(c_double))
         for name, arr in self.a.items():
             ctype = c_uint if arr.dtype == np.uint32 else real
             setattr(st, name, arr.ctypes.data_as(POINTER(ctype)))
@@ -177,6 +186,11 @@ class OracleScene(object):
         ptr = v.ctypes.data_as(POINTER(c_float if self.prec == "f32" else c_double))
         getattr(lib(), "oracle_set_body_rotation" + self._sfx)(ctypes.byref(self.state), body, ptr)
 
+    def reset_rigid(self):
+        """Rigid bodies are set up again from the particles on their next
+        substep (what a host upload of positions does on the device)."""
+        self.rigid_state[:, 0] = 0.0
+
     # the reference's driver recipes ------------------------------------------
     def setup_solid(self):
         """StrainSolid.setup (systems.py:185-192)."""
@@ -200,6 +214,7 @@ class OracleScene(object):
         else:
             raise ValueError(material)
         self.call("step_forward")
+        self.call("rigid_step")  # rigid bodies (extension); nothing without any
 
     def run(self, material, steps):
         for _ in range(steps):

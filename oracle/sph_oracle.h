@@ -66,7 +66,33 @@ extern "C" {
     /* optional reflective box (extension, not in the reference): */          \
     unsigned int has_wallbounds; REAL wallbounds[6];                           \
     int guards; /* bit 0: Givens zero pivot, bit 1: zero-distance pairs */     \
-    int nthreads;
+    int nthreads;                                                              \
+    /* rigid bodies (extension, not in the reference; oracle_rigid_step):  */ \
+    /* body_dynamic[b-1] == 2 marks body b rigid; rigid_state holds        */ \
+    /* ORACLE_RIGID_STRIDE doubles per body (zeroed = to set up), and     */ \
+    /* rigid_offset[3 * n] the particles' body-frame offsets               */ \
+    unsigned int body_capacity;                                                \
+    double *rigid_state;                                                       \
+    REAL *rigid_offset;
+
+#define ORACLE_BODY_RIGID 2u
+#define ORACLE_RIGID_STRIDE 64
+/* slots of a body's rigid_state */
+enum {
+    ORS_FLAG = 0, /* 0: to set up, 1: set up this substep, 2: running */
+    ORS_N = 1,    /* particle count */
+    ORS_LO = 2,   /* lowest / highest particle index */
+    ORS_HI = 3,
+    ORS_C = 4,    /* centre (3) */
+    ORS_V = 7,    /* linear velocity (3) */
+    ORS_Q = 10,   /* orientation quaternion (w, x, y, z) */
+    ORS_L = 14,   /* angular momentum (3) */
+    ORS_IINV0 = 17, /* body-frame inverse inertia, 3x3 row-major */
+    ORS_W = 26,   /* angular velocity (3) */
+    ORS_A = 29,   /* linear acceleration of the last substep (3) */
+    ORS_R = 32,   /* rotation matrix (3x3 row-major) */
+    ORS_C0 = 41   /* centre at set-up (3) */
+};
 
 typedef struct { SPH_ORACLE_STATE_FIELDS(float)  } sph_oracle_state_f32;
 typedef struct { SPH_ORACLE_STATE_FIELDS(double) } sph_oracle_state_f64;
@@ -86,6 +112,7 @@ typedef struct { SPH_ORACLE_STATE_FIELDS(double) } sph_oracle_state_f64;
     void oracle_compute_stresses_svk##SFX(sph_oracle_state##SFX *s);           \
     void oracle_compute_forces_solids_svk##SFX(sph_oracle_state##SFX *s);      \
     void oracle_step_forward##SFX(sph_oracle_state##SFX *s);                   \
+    void oracle_rigid_step##SFX(sph_oracle_state##SFX *s);                     \
     void oracle_apply_plane_constraints##SFX(sph_oracle_state##SFX *s);        \
     void oracle_set_body_position##SFX(sph_oracle_state##SFX *s,               \
                                        unsigned int body, const REAL *pos);   \

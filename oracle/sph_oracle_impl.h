@@ -685,6 +685,9 @@ void OF(oracle_step_forward)(OST *s) {
         unsigned i = (unsigned)ii;
         unsigned b = s->body_number[i];
         if (b > 0 && !s->body_dynamic[b - 1]) continue;
+        /* rigid bodies (extension) are moved by oracle_rigid_step */
+        if (b > 0 && s->rigid_state && b <= s->body_capacity && s->body_dynamic[b - 1] == ORACLE_BODY_RIGID)
+            continue;
         V3 f = OF(v3_load)(s->force, i);
         V3 a = OF(v3_add)(OF(v3_div)(f, m), g);
         OF(v3_store)(a, s->acceleration, i);
@@ -702,6 +705,155 @@ void OF(oracle_step_forward)(OST *s) {
         }
         OF(v3_store)(pn, s->position, i);
         OF(v3_store)(vn, s->velocity, i);
+    }
+}
+
+/* Rigid bodies: an extension with no reference counterpart (the
+ * reference's bodies are only fixed or kinematic, rigidbody.cl).  A body b
+ * with body_dynamic[b-1] == ORACLE_BODY_RIGID moves rigidly.  After the
+ * material's step: its particles' forces are summed (FP64, in index order)
+ * into the total force F and the torque about the centre; the body takes
+ * the particles' semi-implicit Euler step (a = F/M + g, v += dt a,
+ * c += dt v; L += dt tau, q += dt/2 (0, w) q normalised, w = R I0^-1 R^T L)
+ * and its particles are placed at x = c + R r0, v = v_c + w x (R r0).  On
+ * the body's first substep (or after a reset: flag 0) the centre, mean
+ * velocity, inertia, angular momentum and offsets r0 = x - c0 are taken
+ * from the particles.  The same algorithm as the CUDA kernels
+ * (kernels_rigid.cuh), which sum in a different (blocked) order. */
+static void OF(rigid_sym_inverse)(const double I[9], double out[9]) {
+    double c00 = I[4] * I[8] - I[5] * I[7], c01 = I[5] * I[6] - I[3] * I[8], c02 = I[3] * I[7] - I[4] * I[6];
+    double det = I[0] * c00 + I[1] * c01 + I[2] * c02, tr = I[0] + I[4] + I[8];
+    for (int k = 0; k < 9; ++k) out[k] = 0.0;
+    if (!(tr > 0.0) || !(fabs(det) > 1e-12 * tr * tr * tr)) return;
+    double inv = 1.0 / det;
+    out[0] = c00 * inv;
+    out[1] = (I[2] * I[7] - I[1] * I[8]) * inv;
+    out[2] = (I[1] * I[5] - I[2] * I[4]) * inv;
+    out[3] = c01 * inv;
+    out[4] = (I[0] * I[8] - I[2] * I[6]) * inv;
+    out[5] = (I[2] * I[3] - I[0] * I[5]) * inv;
+    out[6] = c02 * inv;
+    out[7] = (I[1] * I[6] - I[0] * I[7]) * inv;
+    out[8] = (I[0] * I[4] - I[1] * I[3]) * inv;
+}
+
+static void OF(rigid_quat_matrix)(const double q[4], double R[9]) {
+    double w = q[0], x = q[1], y = q[2], z = q[3];
+    R[0] = 1 - 2 * (y * y + z * z); R[1] = 2 * (x * y - w * z);     R[2] = 2 * (x * z + w * y);
+    R[3] = 2 * (x * y + w * z);     R[4] = 1 - 2 * (x * x + z * z); R[5] = 2 * (y * z - w * x);
+    R[6] = 2 * (x * z - w * y);     R[7] = 2 * (y * z + w * x);     R[8] = 1 - 2 * (x * x + y * y);
+}
+
+static void OF(rigid_omega)(const double R[9], const double Iinv0[9], const double L[3], double w[3]) {
+    double a[3], b[3];
+    for (int r = 0; r < 3; ++r) a[r] = R[r] * L[0] + R[3 + r] * L[1] + R[6 + r] * L[2];
+    for (int r = 0; r < 3; ++r) b[r] = Iinv0[3 * r] * a[0] + Iinv0[3 * r + 1] * a[1] + Iinv0[3 * r + 2] * a[2];
+    for (int r = 0; r < 3; ++r) w[r] = R[3 * r] * b[0] + R[3 * r + 1] * b[1] + R[3 * r + 2] * b[2];
+}
+
+void OF(oracle_rigid_step)(OST *s) {
+    if (!s->rigid_state) return;
+    const double m = (double)s->mass, dt = (double)s->timestep;
+    unsigned nb = s->body_count < s->body_capacity ? s->body_count : s->body_capacity;
+    for (unsigned b = 1; b <= nb; ++b) {
+        if (s->body_dynamic[b - 1] != ORACLE_BODY_RIGID) continue;
+        double *st = s->rigid_state + (size_t)(b - 1) * ORACLE_RIGID_STRIDE;
+        unsigned lo = 0, hi = s->n;
+        if (st[ORS_FLAG] != 0.0) {
+            unsigned h1 = (unsigned)st[ORS_HI] + 1u;
+            lo = (unsigned)st[ORS_LO];
+            hi = h1 < s->n ? h1 : s->n;
+        }
+        double N = 0, X[3] = {0, 0, 0}, Vs[3] = {0, 0, 0}, XX[6] = {0, 0, 0, 0, 0, 0}, XV[3] = {0, 0, 0};
+        double F[3] = {0, 0, 0}, XF[3] = {0, 0, 0}, mn = 4294967296.0, mx = -1.0;
+        for (unsigned i = lo; i < hi; ++i) {
+            if (s->body_number[i] != b) continue;
+            double x = s->position[3 * i], y = s->position[3 * i + 1], z = s->position[3 * i + 2];
+            double vx = s->velocity[3 * i], vy = s->velocity[3 * i + 1], vz = s->velocity[3 * i + 2];
+            double fx = s->force[3 * i], fy = s->force[3 * i + 1], fz = s->force[3 * i + 2];
+            N += 1.0;
+            X[0] += x; X[1] += y; X[2] += z;
+            Vs[0] += vx; Vs[1] += vy; Vs[2] += vz;
+            XX[0] += x * x; XX[1] += y * y; XX[2] += z * z; XX[3] += x * y; XX[4] += x * z; XX[5] += y * z;
+            XV[0] += y * vz - z * vy; XV[1] += z * vx - x * vz; XV[2] += x * vy - y * vx;
+            F[0] += fx; F[1] += fy; F[2] += fz;
+            XF[0] += y * fz - z * fy; XF[1] += z * fx - x * fz; XF[2] += x * fy - y * fx;
+            if (i < mn) mn = i;
+            if (i > mx) mx = i;
+        }
+        if (N == 0.0) { st[ORS_FLAG] = 0.0; continue; }
+        if (st[ORS_FLAG] == 0.0) {
+            double c[3], v[3];
+            for (int k = 0; k < 3; ++k) { c[k] = X[k] / N; v[k] = Vs[k] / N; }
+            double cxx = XX[0] - N * c[0] * c[0], cyy = XX[1] - N * c[1] * c[1], czz = XX[2] - N * c[2] * c[2];
+            double cxy = XX[3] - N * c[0] * c[1], cxz = XX[4] - N * c[0] * c[2], cyz = XX[5] - N * c[1] * c[2];
+            double I0[9] = {m * (cyy + czz), -m * cxy, -m * cxz, -m * cxy, m * (cxx + czz),
+                            -m * cyz, -m * cxz, -m * cyz, m * (cxx + cyy)};
+            OF(rigid_sym_inverse)(I0, st + ORS_IINV0);
+            st[ORS_L] = m * (XV[0] - N * (c[1] * v[2] - c[2] * v[1]));
+            st[ORS_L + 1] = m * (XV[1] - N * (c[2] * v[0] - c[0] * v[2]));
+            st[ORS_L + 2] = m * (XV[2] - N * (c[0] * v[1] - c[1] * v[0]));
+            for (int k = 0; k < 3; ++k) { st[ORS_C + k] = c[k]; st[ORS_C0 + k] = c[k]; st[ORS_V + k] = v[k]; }
+            st[ORS_Q] = 1.0; st[ORS_Q + 1] = st[ORS_Q + 2] = st[ORS_Q + 3] = 0.0;
+            st[ORS_N] = N; st[ORS_LO] = mn; st[ORS_HI] = mx;
+            st[ORS_FLAG] = 1.0;
+        } else if (st[ORS_FLAG] == 1.0) {
+            st[ORS_FLAG] = 2.0;
+        }
+        double M = st[ORS_N] * m, c[3] = {st[ORS_C], st[ORS_C + 1], st[ORS_C + 2]};
+        double tau[3] = {XF[0] - (c[1] * F[2] - c[2] * F[1]), XF[1] - (c[2] * F[0] - c[0] * F[2]),
+                         XF[2] - (c[0] * F[1] - c[1] * F[0])};
+        double v[3], L[3], q[4], R[9], w[3];
+        for (int k = 0; k < 3; ++k) {
+            double a = F[k] / M + (double)s->gravity[k];
+            st[ORS_A + k] = a;
+            v[k] = st[ORS_V + k] + dt * a;
+            c[k] += dt * v[k];
+            L[k] = st[ORS_L + k] + dt * tau[k];
+        }
+        for (int k = 0; k < 4; ++k) q[k] = st[ORS_Q + k];
+        OF(rigid_quat_matrix)(q, R);
+        OF(rigid_omega)(R, st + ORS_IINV0, L, w);
+        double h = 0.5 * dt;
+        double dq[4] = {-(w[0] * q[1] + w[1] * q[2] + w[2] * q[3]), w[0] * q[0] + w[1] * q[3] - w[2] * q[2],
+                        w[1] * q[0] + w[2] * q[1] - w[0] * q[3], w[2] * q[0] + w[0] * q[2] - w[1] * q[1]};
+        double nq = 0.0;
+        for (int k = 0; k < 4; ++k) { q[k] += h * dq[k]; nq += q[k] * q[k]; }
+        nq = 1.0 / sqrt(nq);
+        for (int k = 0; k < 4; ++k) q[k] *= nq;
+        OF(rigid_quat_matrix)(q, R);
+        OF(rigid_omega)(R, st + ORS_IINV0, L, w);
+        for (int k = 0; k < 3; ++k) { st[ORS_C + k] = c[k]; st[ORS_V + k] = v[k]; st[ORS_L + k] = L[k]; st[ORS_W + k] = w[k]; }
+        for (int k = 0; k < 4; ++k) st[ORS_Q + k] = q[k];
+        for (int k = 0; k < 9; ++k) st[ORS_R + k] = R[k];
+        if (s->body_position)
+            for (int k = 0; k < 3; ++k) s->body_position[3 * (b - 1) + k] = (REAL)c[k];
+        /* place the particles on the body */
+        unsigned slo = (unsigned)st[ORS_LO], sh1 = (unsigned)st[ORS_HI] + 1u;
+        unsigned shi = sh1 < s->n ? sh1 : s->n;
+        REAL a3[3] = {(REAL)st[ORS_A], (REAL)st[ORS_A + 1], (REAL)st[ORS_A + 2]};
+        for (unsigned i = slo; i < shi; ++i) {
+            if (s->body_number[i] != b) continue;
+            double r0[3];
+            if (st[ORS_FLAG] == 1.0) {
+                for (int k = 0; k < 3; ++k) {
+                    REAL o = (REAL)((double)s->position[3 * i + k] - st[ORS_C0 + k]);
+                    s->rigid_offset[3 * i + k] = o;
+                    r0[k] = o;
+                }
+            } else {
+                for (int k = 0; k < 3; ++k) r0[k] = s->rigid_offset[3 * i + k];
+            }
+            double rr[3];
+            for (int k = 0; k < 3; ++k) rr[k] = R[3 * k] * r0[0] + R[3 * k + 1] * r0[1] + R[3 * k + 2] * r0[2];
+            s->position[3 * i] = (REAL)(c[0] + rr[0]);
+            s->position[3 * i + 1] = (REAL)(c[1] + rr[1]);
+            s->position[3 * i + 2] = (REAL)(c[2] + rr[2]);
+            s->velocity[3 * i] = (REAL)(v[0] + (w[1] * rr[2] - w[2] * rr[1]));
+            s->velocity[3 * i + 1] = (REAL)(v[1] + (w[2] * rr[0] - w[0] * rr[2]));
+            s->velocity[3 * i + 2] = (REAL)(v[2] + (w[0] * rr[1] - w[1] * rr[0]));
+            for (int k = 0; k < 3; ++k) s->acceleration[3 * i + k] = a3[k];
+        }
     }
 }
 
