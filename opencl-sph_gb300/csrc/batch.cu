@@ -201,7 +201,7 @@ bool rebuild(sph_batch *b) {
     cudaGraph_t graph = nullptr;
     if (!ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture")) return false;
     sph_launch_bins(A);
-    sph_launch_gather(A, true, false);
+    sph_launch_gather(A, true, false, true);
     sph_launch_density(A, false, true);  // masks for the fluid scenes only
     cudaEventRecord(b->fork, b->stream);
     for (int m = 0; m < 3; ++m) {
@@ -213,8 +213,8 @@ bool rebuild(sph_batch *b) {
         } else {
             if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L);
             else sph_launch_deformations(G.L);
-            sph_launch_stresses(G.L, m == MAT_COROT);
-            sph_launch_forces_solids(G.L, m == MAT_COROT);
+            sph_launch_stresses(G.L, m == MAT_COROT, true);
+            sph_launch_forces_solids(G.L, m == MAT_COROT, true);
             sph_launch_step_forward(G.L);
         }
         if (m > 0) {
@@ -460,7 +460,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
         log.mark("bins");
         sph_launch_bins(A);
         log.mark("gather");
-        sph_launch_gather(A, true, false);
+        sph_launch_gather(A, true, false, true);
         log.mark("density");
         sph_launch_density(A, false, true);
         for (int m = 0; m < 3; ++m) {
@@ -473,8 +473,8 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
             } else {
                 if (m == MAT_COROT) sph_launch_rotations_and_strains(G);
                 else sph_launch_deformations(G);
-                sph_launch_stresses(G, m == MAT_COROT);
-                sph_launch_forces_solids(G, m == MAT_COROT);
+                sph_launch_stresses(G, m == MAT_COROT, true);
+                sph_launch_forces_solids(G, m == MAT_COROT, true);
                 sph_launch_step_forward(G);
             }
         }

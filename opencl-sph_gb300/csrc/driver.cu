@@ -295,13 +295,13 @@ bool dispatch(Store *s, const char *name) {
     }
     if (k == "compute_rotations_and_strains") {
         if (!need(PROG_COROT, "solid_corotation")) return false;
-        sph_launch_gather(L, false, false);
+        sph_launch_gather(L, false, false, true);
         sph_launch_rotations_and_strains(L);
         return true;
     }
     if (k == "compute_deformations") {
         if (!need(PROG_SVK, "solid_svk")) return false;
-        sph_launch_gather(L, false, false);
+        sph_launch_gather(L, false, false, true);
         sph_launch_deformations(L);
         return true;
     }

@@ -23,7 +23,8 @@ cudaError_t sph_prepare_kernels() {
     if (max_optin > 0 && want > (size_t)max_optin) want = (size_t)max_optin;
     cudaError_t e = cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    e = cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    return e;
 }
 
 cudaError_t sph_check_launch(const char *what) {
@@ -65,9 +66,9 @@ void sph_launch_bins(const Launch &L) {
     sph_launch_insert(L);
 }
 
-void sph_launch_gather(const Launch &L, bool vel, bool dens) {
+void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid) {
     k_gather<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, vel ? 1 : 0,
-                                                                          dens ? 1 : 0);
+                                                                          dens ? 1 : 0, solid ? 1 : 0);
 }
 
 void sph_launch_density(const Launch &L, bool original, bool mask) {
@@ -101,29 +102,42 @@ void sph_launch_init_original_position(const Launch &L) {
 }
 
 void sph_launch_rotations_and_strains(const Launch &L) {
-    k_rotations_and_strains<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-        L.scenes, L.pair_particles);
+    const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    if (!L.no_symmetry_planes)
+        k_rotations_and_strains_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 
-void sph_launch_stresses(const Launch &L, bool corot) {
-    if (corot)
-        k_stresses_corot<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
-    else
-        k_stresses_svk<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+void sph_launch_stresses(const Launch &L, bool corot, bool sorted) {
+    const unsigned g = grid_for(L.particles, L.grid_cap);
+    if (sorted) {
+        if (corot) k_stresses_sorted<true><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
+        else k_stresses_sorted<false><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
+    } else {
+        if (corot) k_stresses_corot<<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
+        else k_stresses_svk<<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
+    }
 }
 
 void sph_launch_deformations(const Launch &L) {
-    k_deformations<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(L.scenes,
-                                                                                           L.pair_particles);
+    const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    if (!L.no_symmetry_planes) k_deformations_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 
-void sph_launch_forces_solids(const Launch &L, bool corot) {
-    if (corot)
-        k_forces_solids<true><<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-            L.scenes, L.pair_particles);
-    else
-        k_forces_solids<false><<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-            L.scenes, L.pair_particles);
+void sph_launch_forces_solids(const Launch &L, bool corot, bool masked) {
+    const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    if (corot) {
+        if (masked) k_forces_solids<true, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        else k_forces_solids<true, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        if (!L.no_symmetry_planes)
+            k_forces_solids_planes<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    } else {
+        if (masked) k_forces_solids<false, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        else k_forces_solids<false, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        if (!L.no_symmetry_planes)
+            k_forces_solids_planes<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    }
 }
 
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]) {
@@ -172,7 +186,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     phase("insert");
     sph_launch_insert(L);
     phase("gather");
-    sph_launch_gather(L, mat == MAT_FLUID, false);
+    sph_launch_gather(L, mat == MAT_FLUID, false, mat != MAT_FLUID);
     phase("density");
     sph_launch_density(L, false, mat == MAT_FLUID);
     if (mat == MAT_FLUID) {
@@ -193,9 +207,9 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
         sph_launch_deformations(L);
     }
     phase("stresses");
-    sph_launch_stresses(L, mat == MAT_COROT);
+    sph_launch_stresses(L, mat == MAT_COROT, true);
     phase("forces_solids");
-    sph_launch_forces_solids(L, mat == MAT_COROT);
+    sph_launch_forces_solids(L, mat == MAT_COROT, true);
     phase("step_forward");
     sph_launch_step_forward(L);
     if (L.num_rigid) {

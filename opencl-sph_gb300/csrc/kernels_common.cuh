@@ -143,6 +143,93 @@ __device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned 
     }
 }
 
+// Row r of particle k's stencil (dz outer, dy inner, as the reference's
+// z, y, x loops): cells x-1..x+1 of one (z, y) row are consecutive in the
+// cell-sorted order, so a row is one range [b, e); empty when the row lies
+// outside the grid.  The rows' presence and x extent are packed into one
+// word when the stencil is set up.
+struct StencilRows {
+    unsigned cell, layer, R0;
+    // bit r: row r lies in the grid; bit 9 + r: its cell x-1 exists;
+    // bit 18 + r: its cell x+1 exists
+    unsigned bits;
+    __device__ __forceinline__ StencilRows(const SceneDesc &S, unsigned cell_) {
+        cell = cell_;
+        R0 = S.gridres[0];
+        const unsigned R1 = S.gridres[1], R2 = S.gridres[2];
+        layer = R0 * R1;
+        const unsigned cz = cell / layer;
+        const unsigned rem = cell - cz * layer;
+        const unsigned cy = rem / R0;
+        const unsigned cx = rem - cy * R0;
+        const unsigned xm = cx > 0, xp = cx + 1 < R0;
+        bits = 0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r) {
+            const int z = (int)cz + r / 3 - 1, y = (int)cy + r % 3 - 1;
+            if (z < 0 || z >= (int)R2 || y < 0 || y >= (int)R1) continue;
+            bits |= (1u << r) | (xm << (9 + r)) | (xp << (18 + r));
+        }
+    }
+    __device__ __forceinline__ void row(const SceneDesc &S, int r, unsigned *b, unsigned *e) const {
+        *b = *e = 0;
+        if (!((bits >> r) & 1u)) return;
+        const int dz = r / 3 - 1, dy = r % 3 - 1;
+        const unsigned c = (unsigned)((int)cell + dz * (int)layer + dy * (int)R0);
+        const unsigned x0 = c - ((bits >> (9 + r)) & 1u), x1 = c + ((bits >> (18 + r)) & 1u);
+        unsigned bb = __ldg(S.celloffset + x0);
+        unsigned ee = __ldg(S.celloffset + x1) + __ldg(S.gridcount + x1);
+        if (ee > S.pnum) ee = S.pnum;  // only with inconsistent host-written tables
+        if (bb > ee) bb = ee;
+        *b = bb;
+        *e = ee;
+    }
+};
+
+// ---- candidate masks -----------------------------------------------------------
+// The first pair pass of a fused substep records, per stencil row r of
+// sorted particle k, which candidates the later passes need: bit t of the
+// row's 64-bit mask is candidate b_r + t; the low word is at
+// nbmask[(2r) * pnum + k], the high word at nbmask[(2r+1) * pnum + k] (only
+// for rows of more than 32 candidates); ncand[k] = SPH_NCAND_SCAN when a
+// row exceeds 64 and the later passes must scan.
+
+// Records row r's mask: low word always, high word for rows over 32.
+__device__ __forceinline__ void store_row_mask(const SceneDesc &S, unsigned k, int r, unsigned len,
+                                               unsigned long long bits) {
+    S.nbmask[(size_t)(2 * r) * S.pnum + k] = (unsigned)bits;
+    if (len > 32) S.nbmask[(size_t)(2 * r + 1) * S.pnum + k] = (unsigned)(bits >> 32);
+}
+
+// Row r's mask as recorded, with bits past the row's end cleared (every
+// visited index stays inside [b, e)).
+__device__ __forceinline__ unsigned long long load_row_mask(const SceneDesc &S, unsigned k, int r, unsigned len) {
+    unsigned lo = S.nbmask[(size_t)(2 * r) * S.pnum + k];
+    lo &= len >= 32 ? 0xffffffffu : (1u << len) - 1u;
+    unsigned hi = 0;
+    if (len > 32) {
+        hi = S.nbmask[(size_t)(2 * r + 1) * S.pnum + k];
+        hi &= len >= 64 ? 0xffffffffu : (1u << (len - 32)) - 1u;
+    }
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+// Calls f(kk) for the candidates of particle k's recorded masks, in order.
+template <class F>
+__device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        unsigned b, e;
+        rows.row(S, r, &b, &e);
+        unsigned long long m = load_row_mask(S, k, r, e - b);
+        while (m) {
+            const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
+            m &= m - 1ull;
+            f(b + t);
+        }
+    }
+}
+
 // ---- symmetry planes (the SYMMETRY blocks, e.g. common.cl:647-686) ----------
 
 #define SPH_MAX_PLANES 8

@@ -40,35 +40,48 @@ __host__ __device__ constexpr size_t density_smem_bytes(unsigned block) {
     return sizeof(float4) * SPH_STAGE * (block / 32);
 }
 
-// Row r of particle k's stencil: [b, e) of the cell-sorted order, empty
-// when the row lies outside the grid.
-struct StencilRows {
-    unsigned layer, R0, R1, R2, cx0, cx1, cy, cz;
-    __device__ __forceinline__ StencilRows(const SceneDesc &S, unsigned cell) {
-        R0 = S.gridres[0];
-        R1 = S.gridres[1];
-        R2 = S.gridres[2];
-        layer = R0 * R1;
-        cz = cell / layer;
-        const unsigned rem = cell - cz * layer;
-        cy = rem / R0;
-        const unsigned cx = rem - cy * R0;
-        cx0 = cx > 0 ? cx - 1 : 0;
-        cx1 = cx + 1 < R0 ? cx + 1 : R0 - 1;
+// Plane-free rows are walked in two phases: a branch-free sweep computes
+// every candidate's squared distance and sets the row's hit bits (r2 <= le,
+// the reference's dist <= h), then the hits are summed in ascending order --
+// the order, values and arithmetic of a direct walk.  Candidates past the
+// 64th of a row (crowded cells only) are summed directly after them.
+template <class P4>
+__device__ __forceinline__ unsigned long long row_hits(const P4 *src, unsigned len, float3 ipos, float le) {
+    unsigned lo = 0, hi = 0, bit = 1;
+    const unsigned n1 = len < 32 ? len : 32, n2 = len < 64 ? len : 64;
+#pragma unroll 4
+    for (unsigned t = 0; t < n1; ++t, bit <<= 1) {
+        const float r2 = norm2(sub3(xyz(src[t]), ipos));
+        lo |= r2 <= le ? bit : 0u;
     }
-    __device__ __forceinline__ void row(const SceneDesc &S, int r, unsigned *b, unsigned *e) const {
-        const int z = (int)cz + r / 3 - 1, y = (int)cy + r % 3 - 1;
-        *b = *e = 0;
-        if (z < 0 || z >= (int)R2 || y < 0 || y >= (int)R1) return;
-        const unsigned first = (unsigned)z * layer + (unsigned)y * R0;
-        unsigned bb = __ldg(S.celloffset + first + cx0);
-        unsigned ee = __ldg(S.celloffset + first + cx1) + __ldg(S.gridcount + first + cx1);
-        if (ee > S.pnum) ee = S.pnum;  // only with inconsistent host-written tables
-        if (bb > ee) bb = ee;
-        *b = bb;
-        *e = ee;
+    bit = 1;
+    for (unsigned t = 32; t < n2; ++t, bit <<= 1) {
+        const float r2 = norm2(sub3(xyz(src[t]), ipos));
+        hi |= r2 <= le ? bit : 0u;
     }
-};
+    return ((unsigned long long)hi << 32) | lo;
+}
+
+template <class P4>
+__device__ __forceinline__ void row_sum(const P4 *src, unsigned len, unsigned long long m, float3 ipos,
+                                        const DistBounds &B, float h2, Kahan &rho, unsigned &count) {
+    while (m) {
+        const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
+        m &= m - 1ull;
+        const float r2 = norm2(sub3(xyz(src[t]), ipos));
+        const float d = fmaxf(h2 - r2, 0.f);
+        rho.add(d * d * d);
+        count += r2 <= B.lt;
+    }
+    for (unsigned t = 64; t < len; ++t) {
+        const float r2 = norm2(sub3(xyz(src[t]), ipos));
+        if (r2 <= B.le) {
+            const float d = fmaxf(h2 - r2, 0.f);
+            rho.add(d * d * d);
+            count += r2 <= B.lt;
+        }
+    }
+}
 
 template <bool PLANES, bool MASK>
 __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsigned item, unsigned lane,
@@ -102,44 +115,53 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             for (unsigned t = lane; t < ue - ub; t += 32) wstage[t] = spos[ub + t];
             __syncwarp();
         }
+        const unsigned len = e - b;
         unsigned long long bits = 0;
-        auto visit = [&](float3 jpos, unsigned t) {
-            const float r2 = norm2(sub3(jpos, ipos));
-            if (r2 <= B.le) {
-                const float d = fmaxf(h2 - r2, 0.f);
-                rho.add(d * d * d);
-                count += r2 <= B.lt;
-                if (MASK && t < 64) bits |= 1ull << t;
+        if (!PLANES) {
+            if (staged) {
+                bits = row_hits(wstage + (b - ub), len, ipos, B.le);
+                row_sum(wstage + (b - ub), len, bits, ipos, B, h2, rho, count);
+            } else {
+                bits = row_hits(spos + b, len, ipos, B.le);
+                row_sum(spos + b, len, bits, ipos, B, h2, rho, count);
             }
-            if (PLANES && P.imask) {
-                const unsigned jm = plane_jmask(P, jpos, h);
-                // subsets of jm in increasing order: the reference's
-                // plane_bits order restricted to the subsets it keeps
-                for (unsigned sb = (0u - jm) & jm; sb; sb = (sb - jm) & jm) {
-                    float3 ref = jpos;
-                    for (unsigned s = 0; s < P.count; ++s)
-                        if (sb & (1u << s)) ref = reflect3(ref, P.p[s], P.n[s]);
-                    const float m2 = norm2(sub3(ref, ipos));
-                    if (m2 <= B.lt) {
-                        const float d = fmaxf(h2 - m2, 0.f);
-                        rho.add(d * d * d);
-                        ++count;
+        } else {
+            // with symmetry planes every candidate's images are tested too,
+            // in the reference's order: direct term, then the images
+            auto visit = [&](float3 jpos, unsigned t) {
+                const float r2 = norm2(sub3(jpos, ipos));
+                if (r2 <= B.le) {
+                    const float d = fmaxf(h2 - r2, 0.f);
+                    rho.add(d * d * d);
+                    count += r2 <= B.lt;
+                    if (MASK && t < 64) bits |= 1ull << t;
+                }
+                if (P.imask) {
+                    const unsigned jm = plane_jmask(P, jpos, h);
+                    // subsets of jm in increasing order: the reference's
+                    // plane_bits order restricted to the subsets it keeps
+                    for (unsigned sb = (0u - jm) & jm; sb; sb = (sb - jm) & jm) {
+                        float3 ref = jpos;
+                        for (unsigned s2 = 0; s2 < P.count; ++s2)
+                            if (sb & (1u << s2)) ref = reflect3(ref, P.p[s2], P.n[s2]);
+                        const float m2 = norm2(sub3(ref, ipos));
+                        if (m2 <= B.lt) {
+                            const float d = fmaxf(h2 - m2, 0.f);
+                            rho.add(d * d * d);
+                            ++count;
+                        }
                     }
                 }
+            };
+            if (staged) {
+                const float4 *src = wstage + (b - ub);
+                for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
+            } else {
+                for (unsigned t = 0; t < len; ++t) visit(xyz(spos[b + t]), t);
             }
-        };
-        if (staged) {
-            const float4 *src = wstage + (b - ub);
-            const unsigned len = e - b;
-#pragma unroll 2
-            for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
-        } else {
-            for (unsigned t = 0; t < e - b; ++t) visit(xyz(spos[b + t]), t);
         }
         if (MASK && active) {
-            const unsigned len = e - b;
-            S.nbmask[(size_t)(2 * r) * S.pnum + k] = (unsigned)bits;
-            if (len > 32) S.nbmask[(size_t)(2 * r + 1) * S.pnum + k] = (unsigned)(bits >> 32);
+            store_row_mask(S, k, r, len, bits);
             overflow |= len > 64;
             total += len;
         }
@@ -156,7 +178,11 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             S.num_neighbours[i] = count;
             S.sdens[k] = value;
         }
-        if (MASK) S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        if (MASK) {
+            S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+            // the force pass reads a neighbour's velocity and density together
+            S.svel[k].w = value;
+        }
     }
 }
 
@@ -198,96 +224,109 @@ __device__ __forceinline__ float cube_bound(float p, float f) {
 // the sorted copies, which no other thread reads afterwards.
 __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3 f, float3 v, float3 p);
 
-// One particle's fluid force, visiting its within-h neighbours either by
-// scanning the stencil (`masked` false) or through the per-row candidate
-// masks the density pass recorded (`masked` true; a particle with a row of
-// more than 64 candidates is scanned).  Both visit the same neighbours in the
-// same order with the same arithmetic, so the results are identical.
-template <bool MASKED>
-__device__ __forceinline__ void fluid_force(const SceneDesc &S, unsigned k, int fuse_step) {
-    const unsigned i = min(S.cellparticles[k], S.pnum - 1);
-    const float h = *S.h;
-    const DistBounds B = dist_bounds(h);
-    const float rho0 = *S.restdens, stiff = *S.stiffness, visc = *S.viscosity;
-    const float h3 = h * h * h;
-    const float kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
-    const float3 ipos = xyz(S.spos[k]);
-    const float3 ivel = xyz(S.svel[k]);
-    const float rhoi = S.sdens[k];
-    const float pi = (rhoi - rho0) * stiff;
-    Kahan3 f;
+// Particle i's side of the fluid pair term.
+struct FluidI {
+    float3 ipos, ivel;
+    float rhoi, pi, h, rho0, stiff, visc, kv;
+    DistBounds B;
+};
+
+__device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float3 ivel, float rhoi) {
+    FluidI I;
+    I.ipos = ipos;
+    I.ivel = ivel;
+    I.rhoi = rhoi;
+    I.h = *S.h;
+    I.B = dist_bounds(I.h);
+    I.rho0 = *S.restdens;
+    I.stiff = *S.stiffness;
+    I.visc = *S.viscosity;
+    const float h3 = I.h * I.h * I.h;
+    I.kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
+    I.pi = (rhoi - I.rho0) * I.stiff;
+    return I;
+}
+
+// One neighbour's pressure + viscosity term (fluids.cl:37-56), added to f.
+// Every rounding is pinned, so all three walks (scan, mask, staged mask)
+// produce the same sum.  Distinct particles at exactly zero distance (and
+// i itself) contribute nothing.
+__device__ __forceinline__ void fluid_pair(const FluidI &I, float3 jpos, float3 jvel, float rhoj, Kahan3 &f) {
+    const float3 d = sub3(jpos, I.ipos);
+    const float r2 = norm2(d);
+    if (!(r2 <= I.B.le) || r2 == 0.f) return;
+    const float rinv = rsqrtf(r2);
+    const float dist = __fmul_rn(r2, rinv);
+    const float din = __fsub_rn(I.h, dist);
+    const float pj = __fmul_rn(__fsub_rn(rhoj, I.rho0), I.stiff);
+    const float inv_didj = __frcp_rn(__fmul_rn(I.rhoi, rhoj));
+    const float vterm = __fmul_rn(__fmul_rn(I.visc, din), I.kv);
+    const float pterm = __fmul_rn(
+        __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(-__fadd_rn(I.pi, pj), 0.5f), rinv), din), din), I.kv);
+    const float3 rv = sub3(jvel, I.ivel);
+    f.add(make_float3(__fmul_rn(__fmaf_rn(d.x, pterm, __fmul_rn(rv.x, vterm)), inv_didj),
+                      __fmul_rn(__fmaf_rn(d.y, pterm, __fmul_rn(rv.y, vterm)), inv_didj),
+                      __fmul_rn(__fmaf_rn(d.z, pterm, __fmul_rn(rv.z, vterm)), inv_didj)));
+}
+
+// The end of a fluid particle's force pass: mass, cube band, store, step.
+__device__ __forceinline__ void fluid_finish(const SceneDesc &S, unsigned i, const FluidI &I, const Kahan3 &f,
+                                             int fuse_step) {
+    const float m = *S.mass;
+    float3 fi = f.get() * m;
+    fi.x = cube_bound(I.ipos.x, fi.x);
+    fi.y = cube_bound(I.ipos.y, fi.y);
+    fi.z = cube_bound(I.ipos.z, fi.z);
+    st3(S.force, i, fi);
+    if (fuse_step) integrate(S, i, fi, I.ivel, I.ipos);
+}
+
+// The stencil scan: every candidate of the 27 cells, in the reference's order.
+__device__ __forceinline__ void fluid_scan(const SceneDesc &S, unsigned cell, const FluidI &I, Kahan3 &f) {
     const float4 *__restrict__ spos = S.spos;
     const float4 *__restrict__ svel = S.svel;
     const float *__restrict__ sdens = S.sdens;
-    auto pair = [&](unsigned kk) {
-        if (kk == k) return;
-        const float3 d = sub3(xyz(spos[kk]), ipos);
-        const float r2 = norm2(d);
-        // distinct particles at exactly zero distance: no defined
-        // direction (the reference divides by the distance, fluids.cl:48)
-        if (!(r2 <= B.le) || r2 == 0.f) return;
-        const float rinv = rsqrtf(r2);
-        const float dist = r2 * rinv;
-        const float din = h - dist;
-        const float rhoj = sdens[kk];
-        const float pj = (rhoj - rho0) * stiff;
-        const float inv_didj = 1.0f / (rhoi * rhoj);
-        const float vterm = visc * din * kv;
-        const float pterm = -(pi + pj) * 0.5f * rinv * din * din * kv;
-        const float3 rv = xyz(svel[kk]) - ivel;
-        f.add(make_float3((d.x * pterm + rv.x * vterm) * inv_didj, (d.y * pterm + rv.y * vterm) * inv_didj,
-                          (d.z * pterm + rv.z * vterm) * inv_didj));
-    };
-    const unsigned cell = S.gridcell[i];
-    bool scanned = true;
-    if (MASKED && S.ncand[k] != SPH_NCAND_SCAN) {
-        scanned = false;
-        const StencilRows rows(S, cell);
-#pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
-            unsigned m = S.nbmask[(size_t)(2 * r) * S.pnum + k];
-            unsigned rb, re;
-            rows.row(S, r, &rb, &re);
-            const unsigned len = re - rb;
-            // bits past the row's end cannot be set; the mask makes every
-            // visited index provably inside [rb, re)
-            m &= len >= 32 ? 0xffffffffu : (1u << len) - 1u;
-            while (m) {
-                const unsigned t = (unsigned)(__ffs(m) - 1);
-                m &= m - 1u;
-                pair(rb + t);
-            }
-            if (len > 32) {
-                m = S.nbmask[(size_t)(2 * r + 1) * S.pnum + k];
-                m &= len >= 64 ? 0xffffffffu : (1u << (len - 32)) - 1u;
-                while (m) {
-                    const unsigned t = (unsigned)(__ffs(m) - 1);
-                    m &= m - 1u;
-                    pair(rb + 32u + t);
-                }
-            }
-        }
-    }
-    if (scanned) for_each_neighbour(S, cell, pair);
-    const float m = *S.mass;
-    float3 fi = f.get() * m;
-    fi.x = cube_bound(ipos.x, fi.x);
-    fi.y = cube_bound(ipos.y, fi.y);
-    fi.z = cube_bound(ipos.z, fi.z);
-    st3(S.force, i, fi);
-    if (fuse_step) integrate(S, i, fi, ivel, ipos);
+    for_each_neighbour(S, cell, [&](unsigned kk) { fluid_pair(I, xyz(spos[kk]), xyz(svel[kk]), sdens[kk], f); });
 }
 
 __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
-    if (item < active_count(S)) fluid_force<false>(S, item, fuse_step);
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(S.svel[k]), S.sdens[k]);
+        Kahan3 f;
+        fluid_scan(S, S.gridcell[i], I, f);
+        fluid_finish(S, i, I, f, fuse_step);
+    }
     SPH_END_WORK
 }
 
-// The fused-substep force pass: walks the density pass's candidate masks.
+// The fused-substep force pass: walks the candidate masks the density pass
+// recorded, row by row, reading each neighbour's position and its velocity
+// with the density in w (two float4 loads).  Lanes whose masks overflowed
+// scan the stencil.
 __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
-    if (item < active_count(S)) fluid_force<true>(S, item, fuse_step);
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const float4 v4 = S.svel[k];
+        const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(v4), v4.w);
+        const unsigned cell = S.gridcell[i];
+        Kahan3 f;
+        if (S.ncand[k] != SPH_NCAND_SCAN) {
+            const float4 *__restrict__ spos = S.spos;
+            const float4 *__restrict__ svel = S.svel;
+            for_each_masked(S, k, StencilRows(S, cell), [&](unsigned kk) {
+                const float4 v = svel[kk];
+                fluid_pair(I, xyz(spos[kk]), xyz(v), v.w, f);
+            });
+        } else {
+            fluid_scan(S, cell, I, f);
+        }
+        fluid_finish(S, i, I, f, fuse_step);
+    }
     SPH_END_WORK
 }
 

@@ -258,19 +258,27 @@ __global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__rest
 }
 
 // Cell-sorted copies: spos[k] = position[cellparticles[k]] (and velocity,
-// density when asked).  Gathers once so the pair loops stream float4s.
-__global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int with_vel, int with_dens) {
+// density when asked; for solids also the rest position with the body
+// number, and density0 in the velocity copy's w).  Gathers once so the pair loops stream float4s.
+__global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int with_vel, int with_dens,
+                         int with_solid) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
         unsigned i = S.cellparticles[item];
         if (i >= S.pnum) i = 0;  // host-written garbage
         float3 p = ld3(S.position, i);
         S.spos[item] = make_float4(p.x, p.y, p.z, 0.f);
-        if (with_vel) {
+        const bool solid = with_solid && S.spos0;
+        if (with_vel || solid) {
             float3 v = ld3(S.velocity, i);
-            S.svel[item] = make_float4(v.x, v.y, v.z, 0.f);
+            S.svel[item] = make_float4(v.x, v.y, v.z, solid ? S.density0[i] : 0.f);
         }
         if (with_dens) S.sdens[item] = S.density[i];
+        if (solid) {
+            // rest position, and the body number's bits in w
+            const float3 p0 = ld3(S.originalpos, i);
+            S.spos0[item] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(S.body_number[i]));
+        }
     }
     SPH_END_WORK
 }

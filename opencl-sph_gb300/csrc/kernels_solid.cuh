@@ -175,9 +175,12 @@ __device__ __forceinline__ float3 reflect_bits(const Planes &P, unsigned bits, f
 // compute_rotations_and_strains (solid_corotation.cl:28-195): pass 1 sums
 // Apq = sum W(|p|) p q^T (+ images), R = polar(Apq) in FP64, pass 2 sums
 // D = sum (R^T p - q) m / rho0_i (x) gradW(-q) (+ images), strain =
-// sym(D).  Body particles keep their rotation and strain.
-__global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// sym(D).  Body particles keep their rotation and strain.  This variant
+// serves scenes with symmetry planes (every candidate's images are
+// tested); k_rotations_and_strains serves the others.
+__global__ void k_rotations_and_strains_planes(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes == 0) continue;  // k_rotations_and_strains covers those
     if (item < active_count(S)) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
@@ -280,9 +283,11 @@ __global__ void k_stresses_corot(const SceneDesc *__restrict__ scenes, BlockMap 
 }
 
 // compute_deformations (solid_svk.cl:82-175): F = Apq Aqq^-1.  The poly6
-// normalisation cancels in the product and is left out.
-__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// normalisation cancels in the product and is left out.  Scenes with
+// symmetry planes; k_deformations serves the others.
+__global__ void k_deformations_planes(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes == 0) continue;  // k_deformations covers those
     if (item < active_count(S)) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
@@ -372,9 +377,11 @@ __global__ void k_stresses_svk(const SceneDesc *__restrict__ scenes, BlockMap ma
 // in the rest configuration, rotated by R_i / R_j for the corotational
 // model, plus Laplacian viscosity; symmetry images; the force, its elastic
 // and viscous parts and the test-axis cut-off force are all written.
+// Scenes with symmetry planes; k_forces_solids serves the others.
 template <bool COROT>
-__global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes == 0) continue;  // k_forces_solids covers those
     if (item < active_count(S)) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
@@ -456,6 +463,316 @@ __global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap m
         st3(S.force_elastic, i, fe);
         st3(S.force_viscous, i, fv);
         st3(S.cutoff_force, i, fec_s.get() * 0.5f + fvc_s.get() * visc);
+    }
+    SPH_END_WORK
+}
+
+// ---- plane-free solids: sorted copies and candidate masks -------------------
+//
+// Scenes without symmetry planes.  The first pair pass of the substep
+// (k_rotations_and_strains, k_deformations) walks every stencil candidate
+// from the cell-sorted copies (spos, spos0) and records, per row as the
+// fluid density pass does, the candidates that are direct neighbours of
+// the force pass: j != i with the rest distance |x0_j - x0_i| <= h or the
+// current distance |x_j - x_i| <= h.  The corotational second pass and, in
+// a fused substep, the force pass walk only those.  They visit the same
+// neighbours in the same order with the same arithmetic as a walk over all
+// candidates, so the results are identical; the named force pass (whose
+// masks may be stale) scans.
+
+// compute_rotations_and_strains (solid_corotation.cl:28-195) for
+// plane-free scenes: pass 1 sums Apq over candidates with |p| <= h and
+// records the masks, R = polar(Apq) in FP64, pass 2 sums D over the masked
+// candidates with |q| <= h.  Body particles keep their rotation and strain
+// (their masks are still recorded).  Also writes the sorted rotation copy.
+__global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float4 p4 = S.spos[k], q4 = S.spos0[k];
+        const float3 ipos = xyz(p4), ipos0 = xyz(q4);
+        const StencilRows rows(S, S.gridcell[i]);
+        const float4 *__restrict__ spos = S.spos;
+        const float4 *__restrict__ spos0 = S.spos0;
+        float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        unsigned total = 0;
+        bool overflow = false;
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+            unsigned b, e;
+            rows.row(S, r, &b, &e);
+            unsigned long long bits = 0;
+            for (unsigned t = 0; t < e - b; ++t) {
+                const unsigned kk = b + t;
+                if (kk == k) continue;
+                const float3 p = sub3(xyz(spos[kk]), ipos);
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
+                const float r2 = norm2(p);
+                if (r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    add_outer(p * (d * d * d), q, apq);
+                }
+                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
+            }
+            store_row_mask(S, k, r, e - b, bits);
+            overflow |= e - b > 64;
+            total += e - b;
+        }
+        S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        float R[9];
+        if (__float_as_uint(q4.w) > 0) {
+            // a body particle: rotation and strain stay as they are
+            for (int c = 0; c < 9; ++c) R[c] = S.rotation[9 * (size_t)i + c];
+        } else {
+            for (int c = 0; c < 9; ++c) apq[c] *= C.coef;
+            polar_rotation_fp64(apq, R);
+            for (int c = 0; c < 9; ++c) {
+                S.apq_temp[9 * (size_t)i + c] = apq[c];
+                S.intermediate[9 * (size_t)i + c] = apq[c];
+                S.rotation[9 * (size_t)i + c] = R[c];
+            }
+            const float scale = C.mass / S.density0[i];
+            float D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            auto pass2 = [&](unsigned kk) {
+                if (kk == k) return;
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
+                const float3 g = spiky_grad(-q, C.h, C.kv, C.le);
+                if (g.x != 0.f || g.y != 0.f || g.z != 0.f) {
+                    const float3 u = mat_t_vec(R, sub3(xyz(spos[kk]), ipos)) - q;
+                    add_outer(u * scale, g, D);
+                }
+            };
+            if (overflow) for_each_neighbour(S, S.gridcell[i], pass2);
+            else for_each_masked(S, k, rows, pass2);
+            float *st = S.strain + 6 * (size_t)i;
+            st[0] = D[0];
+            st[1] = D[4];
+            st[2] = D[8];
+            st[3] = 0.5f * (D[1] + D[3]);
+            st[4] = 0.5f * (D[2] + D[6]);
+            st[5] = 0.5f * (D[5] + D[7]);
+        }
+        for (int c = 0; c < 3; ++c) S.srot[3 * (size_t)k + c] = make_float4(R[3 * c], R[3 * c + 1], R[3 * c + 2], 0.f);
+    }
+    SPH_END_WORK
+}
+
+// compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
+// the sorted copies, recording the candidate masks.
+__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float3 ipos = xyz(S.spos[k]), ipos0 = xyz(S.spos0[k]);
+        const StencilRows rows(S, S.gridcell[i]);
+        const float4 *__restrict__ spos = S.spos;
+        const float4 *__restrict__ spos0 = S.spos0;
+        float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        float aqq[6] = {0, 0, 0, 0, 0, 0};
+        unsigned total = 0;
+        bool overflow = false;
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+            unsigned b, e;
+            rows.row(S, r, &b, &e);
+            unsigned long long bits = 0;
+            for (unsigned t = 0; t < e - b; ++t) {
+                const unsigned kk = b + t;
+                if (kk == k) continue;
+                const float3 p = sub3(xyz(spos[kk]), ipos);
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
+                const float r2 = norm2(p);
+                if (r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    const float w = d * d * d;
+                    add_outer(p * w, q, apq);
+                    const float3 wq = q * w;
+                    aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
+                    aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
+                    aqq[2] += wq.z * q.z;
+                }
+                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
+            }
+            store_row_mask(S, k, r, e - b, bits);
+            overflow |= e - b > 64;
+            total += e - b;
+        }
+        S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        float inv[6];
+        sym_inverse(aqq, inv);
+        float F[9];
+        mul_as(apq, inv, F);
+        for (int c = 0; c < 9; ++c) S.deformation[9 * (size_t)i + c] = F[c];
+    }
+    SPH_END_WORK
+}
+
+// Stress laws (solid_corotation.cl:197-208; solid_svk.cl:45-80).
+__device__ __forceinline__ void corot_stress(const SceneDesc &S, const float e[6], float o[6]) {
+    const float E = *S.youngs_modulus, nu = *S.poisson;
+    const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
+    const float mu = E / 2.0f / (1.0f + nu);
+    const float tr = e[0] + e[1] + e[2];
+    o[0] = lam * tr + 2.0f * mu * e[0];
+    o[1] = lam * tr + 2.0f * mu * e[1];
+    o[2] = lam * tr + 2.0f * mu * e[2];
+    o[3] = 2.0f * mu * e[3];
+    o[4] = 2.0f * mu * e[4];
+    o[5] = 2.0f * mu * e[5];
+}
+
+__device__ __forceinline__ void svk_stress(const SceneDesc &S, const float f[9], float o[6]) {
+    const float E = *S.youngs_modulus, nu = *S.poisson;
+    const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
+    const float mu = E / 2.0f / (1.0f + nu);
+    auto ftf = [&](int r, int c) { return f[r] * f[c] + f[3 + r] * f[3 + c] + f[6 + r] * f[6 + c]; };
+    float g[6] = {0.5f * ftf(0, 0) - 0.5f, 0.5f * ftf(1, 1) - 0.5f, 0.5f * ftf(2, 2) - 0.5f,
+                  0.5f * ftf(0, 1), 0.5f * ftf(0, 2), 0.5f * ftf(1, 2)};
+    const float first = lam * (g[0] + g[1] + g[2]);
+    float sv[6] = {first + 2.0f * mu * g[0], first + 2.0f * mu * g[1], first + 2.0f * mu * g[2],
+                   2.0f * mu * g[3], 2.0f * mu * g[4], 2.0f * mu * g[5]};
+    float fs[9];
+    mul_as(f, sv, fs);
+    const float det = f[0] * (f[4] * f[8] - f[5] * f[7]) - f[1] * (f[3] * f[8] - f[5] * f[6]) +
+                      f[2] * (f[3] * f[7] - f[4] * f[6]);
+    const float rdet = 1.0f / det;
+    auto cau = [&](int r, int c) {
+        return (fs[3 * r] * f[3 * c] + fs[3 * r + 1] * f[3 * c + 1] + fs[3 * r + 2] * f[3 * c + 2]) * rdet;
+    };
+    o[0] = cau(0, 0);
+    o[1] = cau(1, 1);
+    o[2] = cau(2, 2);
+    o[3] = cau(0, 1);
+    o[4] = cau(0, 2);
+    o[5] = cau(1, 2);
+}
+
+// compute_stresses in a fused substep: per sorted particle k, the field
+// stress[i] and the sorted copy sstress[k].
+template <bool COROT>
+__global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (item < active_count(S) && S.sstress) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        float o[6];
+        if (COROT) {
+            float e[6];
+            for (int c = 0; c < 6; ++c) e[c] = S.strain[6 * (size_t)i + c];
+            corot_stress(S, e, o);
+        } else {
+            float f[9];
+            for (int c = 0; c < 9; ++c) f[c] = S.deformation[9 * (size_t)i + c];
+            svk_stress(S, f, o);
+        }
+        for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)i + c] = o[c];
+        S.sstress[2 * (size_t)k] = make_float4(o[0], o[1], o[2], o[3]);
+        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], 0.f, 0.f);
+    }
+    SPH_END_WORK
+}
+
+// One side of a solid pair: position, rest position, velocity, densities,
+// stress and rotation, and whether it belongs to a body.
+struct SolidSide {
+    float3 pos, pos0, vel;
+    float rho0, rho;
+    float s[6], R[9];
+    bool body;
+};
+
+template <bool COROT>
+__device__ __forceinline__ void side_from_fields(const SceneDesc &S, unsigned j, float3 pos, SolidSide &J) {
+    J.pos = pos;
+    J.pos0 = ld3(S.originalpos, j);
+    J.vel = ld3(S.velocity, j);
+    J.rho0 = S.density0[j];
+    J.rho = S.density[j];
+    for (int c = 0; c < 6; ++c) J.s[c] = S.stress[6 * (size_t)j + c];
+    if (COROT)
+        for (int c = 0; c < 9; ++c) J.R[c] = S.rotation[9 * (size_t)j + c];
+    J.body = S.body_number[j] > 0;
+}
+
+template <bool COROT>
+__device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk, SolidSide &J) {
+    const float4 p = S.spos[kk], p0 = S.spos0[kk], v = S.svel[kk];
+    J.pos = xyz(p);
+    J.pos0 = xyz(p0);
+    J.vel = xyz(v);
+    J.rho0 = v.w;
+    J.rho = S.sdens[kk];
+    const float4 s0 = S.sstress[2 * (size_t)kk], s1 = S.sstress[2 * (size_t)kk + 1];
+    J.s[0] = s0.x; J.s[1] = s0.y; J.s[2] = s0.z; J.s[3] = s0.w; J.s[4] = s1.x; J.s[5] = s1.y;
+    if (COROT)
+        for (int c = 0; c < 3; ++c) {
+            const float4 r = S.srot[3 * (size_t)kk + c];
+            J.R[3 * c] = r.x;
+            J.R[3 * c + 1] = r.y;
+            J.R[3 * c + 2] = r.z;
+        }
+    J.body = __float_as_uint(p0.w) > 0;
+}
+
+// The direct pair term of compute_forces_solids (solid_corotation.cl:
+// 215-403, solid_svk.cl:182-367) without symmetry images.
+template <bool COROT>
+__device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidSide &I, const SolidSide &J,
+                                           Kahan3 &fe_s, Kahan3 &fv_s) {
+    const float3 x = sub3(I.pos0, J.pos0);
+    const float r2 = norm2(sub3(J.pos, I.pos));
+    if (!(norm2(x) <= C.le || r2 <= C.le)) return;
+    const float vivj = C.mass * C.mass / I.rho0 / J.rho0;
+    const float mrj = C.mass / J.rho;
+    const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
+    const float3 f_ji = sym_vec(I.s, gx) * (-vivj);
+    const float3 f_ij = J.body ? -f_ji : sym_vec(J.s, -gx) * (-vivj);
+    const float3 fe = COROT ? mat_vec(J.R, f_ij) - mat_vec(I.R, f_ji) : f_ij - f_ji;
+    const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
+    const float3 fv = (J.vel - I.vel) * (mrj * lap);
+    fe_s.add(fe);
+    fv_s.add(fv);
+}
+
+// compute_forces_solids for plane-free scenes.  MASKED (a fused substep):
+// walks the masks of the substep's first pair pass, reading the sorted
+// copies; otherwise (a named call) scans every candidate, reading the
+// fields.  Without images the cut-off force equals the force.
+template <bool COROT, bool MASKED>
+__global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (S.num_symmetry_planes || (MASKED && !S.sstress)) continue;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        SolidSide I;
+        if (MASKED) side_from_sorted<COROT>(S, k, I);
+        else side_from_fields<COROT>(S, i, xyz(S.spos[k]), I);
+        Kahan3 fe_s, fv_s;
+        auto visit = [&](unsigned kk) {
+            if (kk == k) return;
+            SolidSide J;
+            if (MASKED) side_from_sorted<COROT>(S, kk, J);
+            else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), J);
+            solid_pair<COROT>(C, I, J, fe_s, fv_s);
+        };
+        if (MASKED && S.ncand[k] != SPH_NCAND_SCAN)
+            for_each_masked(S, k, StencilRows(S, S.gridcell[i]), visit);
+        else
+            for_each_neighbour(S, S.gridcell[i], visit);
+        const float visc = *S.viscosity;
+        const float3 fe = fe_s.get() * 0.5f, fv = fv_s.get() * visc;
+        st3(S.force, i, fe + fv);
+        st3(S.force_elastic, i, fe);
+        st3(S.force_viscous, i, fv);
+        st3(S.cutoff_force, i, fe_s.get() * 0.5f + fv_s.get() * visc);
     }
     SPH_END_WORK
 }

@@ -41,7 +41,7 @@ void sph_launch_insert(const Launch &L);  // scatter + per-cell ordering
 // All of compute_particle_bins: zero, bin+count, scan, insert.
 void sph_launch_bins(const Launch &L);
 // Cell-sorted copies (positions; velocities and densities on request).
-void sph_launch_gather(const Launch &L, bool vel, bool dens);
+void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid = false);
 
 void sph_launch_density(const Launch &L, bool original, bool mask = false);
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked = false);
@@ -49,9 +49,11 @@ void sph_launch_step_forward(const Launch &L);
 void sph_launch_plane_constraints(const Launch &L);
 void sph_launch_init_original_position(const Launch &L);
 void sph_launch_rotations_and_strains(const Launch &L);
-void sph_launch_stresses(const Launch &L, bool corot);
+// sorted: a fused substep's stress pass, which also fills the sorted copy
+void sph_launch_stresses(const Launch &L, bool corot, bool sorted = false);
 void sph_launch_deformations(const Launch &L);
-void sph_launch_forces_solids(const Launch &L, bool corot);
+// masked: a fused substep's force pass over the first pair pass's masks
+void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false);
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
 void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);

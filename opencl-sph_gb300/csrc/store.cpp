@@ -158,6 +158,12 @@ unsigned sph_parse_programs(const char *file_list, std::string *err) {
         *err = "solid_corotation and solid_svk both define compute_stresses/compute_forces_solids";
         return 0;
     }
+    if ((bits & (PROG_COROT | PROG_SVK)) && !(bits & PROG_SOLIDS)) {
+        // the solid models build on solids.cl (density0, originalpos), as
+        // every solid conf of the reference lists it
+        *err = "solid_corotation and solid_svk need 'solids' in the kernel file list";
+        return 0;
+    }
     return bits;
 }
 
@@ -288,6 +294,12 @@ static size_t rigid_bytes(const SceneDesc &d) {
            Arena::align(16ull * d.pnum);
 }
 
+// Sorted solid copies (rest position, stress, rotation).
+static size_t solid_bytes(const SceneDesc &d) {
+    if (!(d.programs & PROG_SOLIDS)) return 0;
+    return Arena::align(16ull * d.pnum) + Arena::align(32ull * d.pnum) + Arena::align(48ull * d.pnum);
+}
+
 size_t sph_scratch_bytes(const SceneDesc &d) {
     size_t P = d.pnum;
     return Arena::align(4 * P)               // slot
@@ -300,6 +312,7 @@ size_t sph_scratch_bytes(const SceneDesc &d) {
            + Arena::align(4ull * SPH_MASK_WORDS * P)  // nbmask
            + Arena::align(4 * P)             // ncand
            + Arena::align(4)                 // steps_left
+           + solid_bytes(d)
            + rigid_bytes(d);
 }
 
@@ -325,6 +338,15 @@ void sph_place_scratch(SceneDesc *d, char *base) {
     o += Arena::align(4 * P);
     d->steps_left = reinterpret_cast<unsigned *>(base + o);
     o += Arena::align(4);
+    d->spos0 = d->sstress = d->srot = nullptr;
+    if (d->programs & PROG_SOLIDS) {
+        d->spos0 = reinterpret_cast<float4 *>(base + o);
+        o += Arena::align(16ull * P);
+        d->sstress = reinterpret_cast<float4 *>(base + o);
+        o += Arena::align(32ull * P);
+        d->srot = reinterpret_cast<float4 *>(base + o);
+        o += Arena::align(48ull * P);
+    }
     d->rigid_state = nullptr;
     d->rigid_partial = nullptr;
     d->rigid_offset = nullptr;
