@@ -4,28 +4,32 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
 
 Workloads (seeded synthetic scenes; sph/scenes.py):
-  wcsph-1m   1,048,576-particle WCSPH slab (128 x 64 x 128 lattice, spacing
-             0.005 m, h = 0.01 m, +-5e-5 m jitter) in a [0,1]^3 box, dt = 2e-5 s: the
-             plain single-scene drop-in path, one CUDA-graph substep per step
-             (default)
-  dam-8k     8,000-particle WCSPH dam break (20^3 at 0.01 m, h = 0.02 m) in
-             [0,0.4]^3, dt = 1e-4 s
-  beam-4k    4,000-particle corotational beam (10x10x40), E = 1e5 Pa,
-             nu = 0.3, two clamped layers, dt = 5e-5 s
+  batched-256  256 independent scenes (60% WCSPH, 25% corotational, 15% SVK,
+               1,000-65,536 particles each, log-uniform) advanced together,
+               one CUDA graph per substep (default: the headline metric is
+               the batched/served form against the plain per-scene loop)
+  large-scene  1,048,576 WCSPH particles with a rigid ball dropped into
+               them, plus a 32^3 SVK cube, as one batch
+  wcsph-1m     1,048,576-particle WCSPH slab (128 x 64 x 128 at 0.005 m,
+               h = 0.01 m) in [0,1]^3: the plain single-scene drop-in path
+  dam-8k       8,000-particle WCSPH dam break (20^3 at 0.01 m, h = 0.02 m)
+  beam-4k      4,000-particle corotational beam (10x10x40), E = 1e5 Pa
 
 One JSON line on rank 0.  `value` is device throughput over the K timed
-substeps (CUDA events on the store's stream, the L2 flushed by a 256 MB
-write between substeps, outside the timed events); `e2e` repeats the
-measurement through the C ABI with host buffers (a per-step upload of the
-scene parameters and download of all positions into the pinned host
-store); `roofline` times each phase of the substep live
-(sph_profile_substep) and sets the dominant kernel's algorithmic bytes
-against the measured HBM peak; `cpu_baseline` times the CPU oracle on a
-bounded sample.  With --impl reference the reference's own kernels
-(oracle/_ref, the reference's kernels/*.cl compiled for the host CPU with
-OpenMP) -- or, where they were not built, the C restatement -- run the same
-workload on all host cores.  N > 1 GPUs run independent replicas (no
-collective; the path does not shard), aggregated over ranks.
+substeps (CUDA events on the work's stream; plain scenes flush the L2 with a
+256 MB write between substeps, outside the events; the batched working set
+exceeds the L2).  `e2e` repeats the measurement through the public API with
+host buffers (per step: the substep, then every scene's positions read
+into its host store).  `roofline` sets the dominant phase's algorithmic
+bytes against the measured HBM peak (phase times from live CUDA events).
+`cpu_baseline` times the CPU oracle on a bounded sample.  The default run
+also reports the plain per-scene loop, the served stream (p50/p99), the
+error against the FP64 oracle and the plain 1M scene.  With --impl
+reference the reference's own kernels (oracle/_ref, the reference's
+kernels/*.cl compiled for the host CPU with OpenMP) -- or, where they were
+not built, the C restatement -- run the same workload on all host cores.
+N > 1 GPUs run independent replicas (no collective; scenes do not shard),
+aggregated over ranks.
 """
 import argparse
 import ctypes
@@ -232,9 +236,29 @@ def bench_plain(args, scene, torch, world):
     phases = {names[i].decode(): float(ms[i]) for i in range(k)}
     e2e = run_e2e(ps, scene, args.steps, torch)
     status = ps.status()
+    pairs = pair_counts(ps)
     ps.close()
     return {"n": n, "cells": cells, "total_s": total_s, "clocks": clk, "phases": phases, "e2e": e2e,
-            "status": status, "kernels_per_step": kernels_per_step}
+            "status": status, "kernels_per_step": kernels_per_step, "pairs": pairs}
+
+
+def pair_counts(ps):
+    """Pair evaluations of one substep of the store's current state: stencil
+    candidates (every particle against the 27 cells around its own, from
+    the cell counts) and neighbours within h (num_neighbours, self
+    included)."""
+    ps.sync_device_to_host()
+    res = [int(x) for x in np.ravel(ps.get_fields("gridres")[0])]
+    cnt = np.asarray(ps.get_fields("gridcount")[0], dtype=np.int64).reshape(res[2], res[1], res[0])
+    box = np.pad(cnt, 1)
+    acc = np.zeros_like(cnt)
+    for dz in range(3):
+        for dy in range(3):
+            for dx in range(3):
+                acc += box[dz:dz + res[2], dy:dy + res[1], dx:dx + res[0]]
+    n = int(np.ravel(ps.get_fields("n")[0])[0])
+    return {"candidates": int((cnt * acc).sum()),
+            "neighbours": int(np.asarray(ps.get_fields("num_neighbours")[0][:n], dtype=np.int64).sum())}
 
 
 def run_e2e(ps, scene, steps, torch):
@@ -259,9 +283,14 @@ def run_e2e(ps, scene, steps, torch):
             "d2h_bytes_per_step": 12 * scene.n, "host_memory": "pinned" if registered else "pageable"}
 
 
-def batched_scenes(seed):
+def batched_scenes(seed, workload="batched-256"):
     from sph import scenes
+    if workload == "large-scene":
+        return scenes.large_scene(seed)
     return scenes.batch_mix(256, seed=seed)
+
+
+BATCHED_WORKLOADS = ("batched-256", "large-scene")
 
 
 def bench_batched(args, torch, world):
@@ -269,9 +298,9 @@ def bench_batched(args, torch, world):
     together: one CUDA graph per substep over all scenes."""
     from sph.batch import Batch
     from sph import autotune
-    scs = batched_scenes(args.seed)
+    scs = batched_scenes(args.seed, args.workload)
     tuned = None
-    if not args.quick:
+    if not args.quick and args.workload == "batched-256":
         sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
         cands = [(b_, p_, c_) for b_ in (128, 256) for p_ in (64, 128, 256) for c_ in (0, 4 * sms, 8 * sms)]
         best, best_s, table = autotune.tune(scs, steps=3, cands=cands)
@@ -510,8 +539,8 @@ def cpu_sample(scene, material, steps, nthreads, reference):
 
 
 def cpu_workload(name, seed, budget_scenes=None):
-    if name == "batched-256":
-        scs = batched_scenes(seed)
+    if name in BATCHED_WORKLOADS:
+        scs = batched_scenes(seed, name)
         return scs if budget_scenes is None else scs[:budget_scenes]
     return [workload(name, seed)[0]]
 
@@ -525,11 +554,17 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak_gbs()
     peak_kind = "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"
     extra = {}
-    if args.workload == "batched-256":
+    if args.workload in BATCHED_WORKLOADS:
         r = bench_batched(args, torch, world)
-        desc = ("256 independent scenes, 60% WCSPH / 25% corotational / 15% SVK, particle counts log-uniform "
-                "in [1,000, 65,536], E log-uniform [1e4, 1e6] Pa, Poisson uniform [0.25, 0.45], 0.01 m "
-                "spacing, h=0.02 m, seeded jitter; one CUDA graph per substep over all scenes")
+        if args.workload == "large-scene":
+            desc = ("large scene: 1,048,576 WCSPH particles (128x64x128 at 0.005 m, h=0.01 m, [0,1]^3, dt=2e-5 s, "
+                    "stiffness 0.375, viscosity 0.025) with a rigid ball of radius 0.05 m (4,169 particles, "
+                    "body_dynamic 2) dropped into them, plus a 32^3 SVK cube (E=5e4 Pa, nu=0.35) as a second "
+                    "scene; one CUDA graph per substep")
+        else:
+            desc = ("256 independent scenes, 60% WCSPH / 25% corotational / 15% SVK, particle counts log-uniform "
+                    "in [1,000, 65,536], E log-uniform [1e4, 1e6] Pa, Poisson uniform [0.25, 0.45], 0.01 m "
+                    "spacing, h=0.02 m, seeded jitter; one CUDA graph per substep over all scenes")
         t = r.get("tuned")
         path = ("batched form (sph_batch_step); launch shape chosen by sph.autotune: block %d, pair block %d, "
                 "grid cap %d" % (t["block"], t["pair_block"], t["grid_cap"]) if t else
@@ -537,7 +572,7 @@ def run_ours(args, rank, world, local_rank):
         if t:
             extra["autotune"] = t
         l2 = "working set %.2f GB > L2 (129 MB); no flush needed" % (r["n"] * 300e-9)
-        if rank == 0 and not args.quick:
+        if rank == 0 and not args.quick and args.workload == "batched-256":
             pl = bench_plain_loop(r["scenes"], max(3, args.steps // 2))
             batched = r["n"] * args.steps / r["total_s"]
             extra["plain_per_scene"] = {
@@ -560,6 +595,19 @@ def run_ours(args, rank, world, local_rank):
         r = bench_plain(args, scene, torch, world)
         path = "plain single scene, one CUDA-graph substep per step (sph_update)"
         l2 = "flushed between timed steps (256 MB write, outside the timed events)"
+    if "pairs" in r and r["phases"]:
+        ph = r["phases"]
+        step_s = r["total_s"] / args.steps
+        c, nb = r["pairs"]["candidates"], r["pairs"]["neighbours"]
+        dens = ph.get("density")
+        forces = ph.get("forces_fluids+step")
+        extra["compute"] = {
+            "candidates_per_step": c, "neighbours_per_step": nb,
+            "pair_evals_per_s": (c + nb) / step_s,
+            "density_candidate_evals_per_s": c / (dens * 1e-3) if dens else None,
+            "force_pair_evals_per_s": nb / (forces * 1e-3) if forces else None,
+            "how": "density tests every stencil candidate (27 cells); the fused force pass evaluates only the "
+                   "neighbours within h from the density pass's masks"}
     value, total_s = aggregate_replicas(r["n"], args.steps, r["total_s"], world, device="cuda")
     if rank != 0:
         return None
@@ -629,7 +677,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", default="batched-256",
-                    choices=["batched-256", "wcsph-1m", "dam-8k", "beam-4k"])
+                    choices=["batched-256", "large-scene", "wcsph-1m", "dam-8k", "beam-4k"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=3, help="substeps in the CPU-baseline sample")

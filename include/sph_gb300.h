@@ -213,6 +213,25 @@ unsigned int sph_graph_kernel_count(psdata_cuda pso);
  * number of phases (at most max_phases), or -1 on failure. */
 int sph_profile_substep(psdata_cuda pso, unsigned int reps, float *phase_ms, const char **phase_names,
                         unsigned int max_phases);
+/* ---- NEW: device-resident recording --------------------------------------
+ * Replaces the reference drivers' per-substep host copy of the whole store
+ * (scripts/straintest.py:183-198 syncs every field to the host and appends
+ * it to .npy memmaps; scripts/sph/systems.py:89-99).  sph_record_start
+ * makes every later sph_update substep copy the named fields, on every
+ * `every`-th substep, into a ring of `frames` frames in device memory;
+ * the copy is part of the substep graph, so recording adds no host work or
+ * synchronisation.  A frame is the fields' bytes concatenated in the given
+ * order.  Frames are numbered from 0 in recording order; the ring holds
+ * the last `frames` of them.  Returns 0, or -1 with sph_last_error set. */
+int sph_record_start(psdata_cuda pso, size_t num_fields, const char *const *names, unsigned int every,
+                     unsigned int frames);
+int sph_record_stop(psdata_cuda pso);
+/* Frames recorded so far (waits for the store's stream). */
+unsigned long long sph_record_count(psdata_cuda pso);
+size_t sph_record_frame_bytes(psdata_cuda pso);
+/* Copies frames [first, first + count) into `host` (count x frame bytes). */
+int sph_record_read(psdata_cuda pso, void *host, unsigned long long first, unsigned int count);
+
 /* ---- NEW: batched and served forms ---------------------------------------
  * A batch holds many independent scenes resident on the device and
  * advances all of them together: every phase of the substep is one

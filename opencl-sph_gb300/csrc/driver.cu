@@ -84,6 +84,11 @@ struct Store {
     std::vector<unsigned> rigid;   // rigid bodies (1-based), as last read from the host store
     RigidWork *d_rigid = nullptr;  // device list, room for every body
     unsigned rigid_room = 0;
+    // device-resident recording (sph_record_*): one allocation holding the
+    // counters, the field ranges and the ring
+    char *rec_mem = nullptr;
+    RecordPlan rec{};
+    std::vector<std::string> rec_fields;
 };
 
 std::mutex g_stores_mu;
@@ -107,6 +112,7 @@ Store *store_of(const psdata_cuda &pso, const char *what) {
 
 void destroy(Store *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->rec_mem) cudaFree(s->rec_mem);
     if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
     if (s->arena.base) cudaFree(s->arena.base);
     if (s->stream) cudaStreamDestroy(s->stream);
@@ -561,6 +567,7 @@ extern "C" int sph_update(psdata_cuda pso, unsigned num_steps) {
         cudaGraph_t g = nullptr;
         if (!cuda_ok(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal), "capture")) return -1;
         sph_launch_substep(s->L, (SphMaterial)s->material);
+        if (s->rec_mem) sph_launch_record(s->rec, s->stream);
         cudaError_t le = cudaGetLastError();
         cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
         if (le != cudaSuccess || ce != cudaSuccess) {
@@ -640,6 +647,124 @@ extern "C" int sph_profile_substep(psdata_cuda pso, unsigned reps, float *phase_
         if (phase_names) phase_names[k] = names[k];
     }
     return (int)np;
+}
+
+// ---- device-resident recording ------------------------------------------------
+
+static void drop_graph(Store *s) {
+    if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
+    s->step_graph = nullptr;
+    s->graph_kernels = 0;
+}
+
+extern "C" int sph_record_stop(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_record_stop");
+    if (!s) return -1;
+    if (!cuda_ok(cudaStreamSynchronize(s->stream), "sph_record_stop")) return -1;
+    if (s->rec_mem) cudaFree(s->rec_mem);
+    s->rec_mem = nullptr;
+    s->rec = RecordPlan{};
+    s->rec_fields.clear();
+    drop_graph(s);
+    return 0;
+}
+
+extern "C" int sph_record_start(psdata_cuda pso, size_t num_fields, const char *const *names, unsigned every,
+                                unsigned frames) {
+    Store *s = store_of(pso, "sph_record_start");
+    if (!s) return -1;
+    if (!num_fields || !names || !every || !frames) {
+        sph_set_error("sph_record_start: needs at least one field, every >= 1 and frames >= 1");
+        return -1;
+    }
+    std::vector<uint2> ranges;
+    std::vector<std::string> fields;
+    size_t words = 0;
+    for (size_t k = 0; k < num_fields; ++k) {
+        const int f = names[k] ? get_field_psdata(s->host, names[k]) : -1;
+        if (f < 0) {
+            sph_set_error("sph_record_start: no field '%s' in the store", names[k] ? names[k] : "");
+            return -1;
+        }
+        const size_t off = s->host.data_offsets[f], sz = s->host.data_sizes[f];
+        if (off % 4 || sz % 4) {
+            sph_set_error("sph_record_start: field '%s' is not word-aligned", names[k]);
+            return -1;
+        }
+        ranges.push_back(make_uint2((unsigned)(off / 4), (unsigned)(sz / 4)));
+        fields.push_back(names[k]);
+        words += sz / 4;
+    }
+    const size_t ring_bytes = (size_t)frames * words * 4;
+    if (words > 0xffffffffu || ring_bytes / frames / 4 != words) {
+        sph_set_error("sph_record_start: frame too large");
+        return -1;
+    }
+    if (sph_record_stop(pso) != 0) return -1;
+    const size_t o_ranges = 256, o_ring = Arena::align(o_ranges + ranges.size() * sizeof(uint2));
+    char *mem = nullptr;
+    if (!cuda_ok(cudaMalloc(&mem, o_ring + ring_bytes), "sph_record_start")) return -1;
+    if (!cuda_ok(cudaMemsetAsync(mem, 0, 256, s->stream), "sph_record_start") ||
+        !cuda_ok(cudaMemcpyAsync(mem + o_ranges, ranges.data(), ranges.size() * sizeof(uint2),
+                                 cudaMemcpyHostToDevice, s->stream),
+                 "sph_record_start") ||
+        !cuda_ok(cudaStreamSynchronize(s->stream), "sph_record_start")) {
+        cudaFree(mem);
+        return -1;
+    }
+    s->rec_mem = mem;
+    s->rec.counters = reinterpret_cast<unsigned long long *>(mem);
+    s->rec.ranges = reinterpret_cast<const uint2 *>(mem + o_ranges);
+    s->rec.num_ranges = (unsigned)ranges.size();
+    s->rec.frame_words = (unsigned)words;
+    s->rec.blob = reinterpret_cast<const unsigned *>(s->d_blob);
+    s->rec.ring = reinterpret_cast<unsigned *>(mem + o_ring);
+    s->rec.frames = frames;
+    s->rec.every = every;
+    s->rec_fields = fields;
+    drop_graph(s);
+    return 0;
+}
+
+extern "C" unsigned long long sph_record_count(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_record_count");
+    unsigned long long c[2] = {0, 0};
+    if (!s || !s->rec_mem) return 0;
+    if (!cuda_ok(cudaMemcpyAsync(c, s->rec.counters, sizeof(c), cudaMemcpyDeviceToHost, s->stream),
+                 "sph_record_count") ||
+        !cuda_ok(cudaStreamSynchronize(s->stream), "sph_record_count"))
+        return 0;
+    return c[1];
+}
+
+extern "C" size_t sph_record_frame_bytes(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_record_frame_bytes");
+    return s && s->rec_mem ? (size_t)s->rec.frame_words * 4 : 0;
+}
+
+extern "C" int sph_record_read(psdata_cuda pso, void *host, unsigned long long first, unsigned count) {
+    Store *s = store_of(pso, "sph_record_read");
+    if (!s) return -1;
+    if (!s->rec_mem) {
+        sph_set_error("sph_record_read: not recording");
+        return -1;
+    }
+    const unsigned long long recorded = sph_record_count(pso);
+    const unsigned long long kept = recorded < s->rec.frames ? recorded : s->rec.frames;
+    if (first < recorded - kept || first + count > recorded) {
+        sph_set_error("sph_record_read: frames [%llu, %llu) not held (the ring holds [%llu, %llu))", first,
+                      first + count, recorded - kept, recorded);
+        return -1;
+    }
+    const size_t fb = (size_t)s->rec.frame_words * 4;
+    for (unsigned k = 0; k < count; ++k) {
+        const size_t slot = (size_t)((first + k) % s->rec.frames);
+        if (!cuda_ok(cudaMemcpyAsync(static_cast<char *>(host) + k * fb, s->rec.ring + slot * s->rec.frame_words, fb,
+                                     cudaMemcpyDeviceToHost, s->stream),
+                     "sph_record_read"))
+            return -1;
+    }
+    return cuda_ok(cudaStreamSynchronize(s->stream), "sph_record_read") ? 0 : -1;
 }
 
 extern "C" void *sph_stream(psdata_cuda pso) {

@@ -252,3 +252,31 @@ void sph_launch_count_down(const Launch &L) {
 void sph_launch_set_steps(unsigned *steps_left, unsigned steps, cudaStream_t stream) {
     k_set_steps<<<1, 1, 0, stream>>>(steps_left, steps);
 }
+
+// Recording: the copy reads the counters, the tick (one thread, after the
+// copy in stream order) advances them.
+__global__ void k_record_copy(RecordPlan p) {
+    const unsigned long long step = p.counters[0];
+    if ((step + 1) % p.every) return;
+    unsigned *dst = p.ring + (size_t)(p.counters[1] % p.frames) * p.frame_words;
+    size_t base = 0;
+    for (unsigned r = 0; r < p.num_ranges; ++r) {
+        const uint2 rg = p.ranges[r];
+        for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < rg.y; w += (size_t)gridDim.x * blockDim.x)
+            dst[base + w] = p.blob[rg.x + w];
+        base += rg.y;
+    }
+}
+
+__global__ void k_record_tick(RecordPlan p) {
+    const unsigned long long step = p.counters[0] + 1;
+    p.counters[0] = step;
+    if (step % p.every == 0) p.counters[1] += 1;
+}
+
+void sph_launch_record(const RecordPlan &p, cudaStream_t stream) {
+    unsigned g = (p.frame_words + 255) / 256;
+    if (g > 1024) g = 1024;
+    k_record_copy<<<g ? g : 1, 256, 0, stream>>>(p);
+    k_record_tick<<<1, 1, 0, stream>>>(p);
+}

@@ -40,49 +40,6 @@ __host__ __device__ constexpr size_t density_smem_bytes(unsigned block) {
     return sizeof(float4) * SPH_STAGE * (block / 32);
 }
 
-// Plane-free rows are walked in two phases: a branch-free sweep computes
-// every candidate's squared distance and sets the row's hit bits (r2 <= le,
-// the reference's dist <= h), then the hits are summed in ascending order --
-// the order, values and arithmetic of a direct walk.  Candidates past the
-// 64th of a row (crowded cells only) are summed directly after them.
-template <class P4>
-__device__ __forceinline__ unsigned long long row_hits(const P4 *src, unsigned len, float3 ipos, float le) {
-    unsigned lo = 0, hi = 0, bit = 1;
-    const unsigned n1 = len < 32 ? len : 32, n2 = len < 64 ? len : 64;
-#pragma unroll 4
-    for (unsigned t = 0; t < n1; ++t, bit <<= 1) {
-        const float r2 = norm2(sub3(xyz(src[t]), ipos));
-        lo |= r2 <= le ? bit : 0u;
-    }
-    bit = 1;
-    for (unsigned t = 32; t < n2; ++t, bit <<= 1) {
-        const float r2 = norm2(sub3(xyz(src[t]), ipos));
-        hi |= r2 <= le ? bit : 0u;
-    }
-    return ((unsigned long long)hi << 32) | lo;
-}
-
-template <class P4>
-__device__ __forceinline__ void row_sum(const P4 *src, unsigned len, unsigned long long m, float3 ipos,
-                                        const DistBounds &B, float h2, Kahan &rho, unsigned &count) {
-    while (m) {
-        const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
-        m &= m - 1ull;
-        const float r2 = norm2(sub3(xyz(src[t]), ipos));
-        const float d = fmaxf(h2 - r2, 0.f);
-        rho.add(d * d * d);
-        count += r2 <= B.lt;
-    }
-    for (unsigned t = 64; t < len; ++t) {
-        const float r2 = norm2(sub3(xyz(src[t]), ipos));
-        if (r2 <= B.le) {
-            const float d = fmaxf(h2 - r2, 0.f);
-            rho.add(d * d * d);
-            count += r2 <= B.lt;
-        }
-    }
-}
-
 template <bool PLANES, bool MASK>
 __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsigned item, unsigned lane,
                                             float4 *__restrict__ wstage, int original) {
@@ -117,48 +74,37 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         }
         const unsigned len = e - b;
         unsigned long long bits = 0;
-        if (!PLANES) {
-            if (staged) {
-                bits = row_hits(wstage + (b - ub), len, ipos, B.le);
-                row_sum(wstage + (b - ub), len, bits, ipos, B, h2, rho, count);
-            } else {
-                bits = row_hits(spos + b, len, ipos, B.le);
-                row_sum(spos + b, len, bits, ipos, B, h2, rho, count);
+        auto visit = [&](float3 jpos, unsigned t) {
+            const float r2 = norm2(sub3(jpos, ipos));
+            if (r2 <= B.le) {
+                const float d = fmaxf(h2 - r2, 0.f);
+                rho.add(d * d * d);
+                count += r2 <= B.lt;
+                if (MASK && t < 64) bits |= 1ull << t;
             }
-        } else {
-            // with symmetry planes every candidate's images are tested too,
-            // in the reference's order: direct term, then the images
-            auto visit = [&](float3 jpos, unsigned t) {
-                const float r2 = norm2(sub3(jpos, ipos));
-                if (r2 <= B.le) {
-                    const float d = fmaxf(h2 - r2, 0.f);
-                    rho.add(d * d * d);
-                    count += r2 <= B.lt;
-                    if (MASK && t < 64) bits |= 1ull << t;
-                }
-                if (P.imask) {
-                    const unsigned jm = plane_jmask(P, jpos, h);
-                    // subsets of jm in increasing order: the reference's
-                    // plane_bits order restricted to the subsets it keeps
-                    for (unsigned sb = (0u - jm) & jm; sb; sb = (sb - jm) & jm) {
-                        float3 ref = jpos;
-                        for (unsigned s2 = 0; s2 < P.count; ++s2)
-                            if (sb & (1u << s2)) ref = reflect3(ref, P.p[s2], P.n[s2]);
-                        const float m2 = norm2(sub3(ref, ipos));
-                        if (m2 <= B.lt) {
-                            const float d = fmaxf(h2 - m2, 0.f);
-                            rho.add(d * d * d);
-                            ++count;
-                        }
+            if (PLANES && P.imask) {
+                const unsigned jm = plane_jmask(P, jpos, h);
+                // subsets of jm in increasing order: the reference's
+                // plane_bits order restricted to the subsets it keeps
+                for (unsigned sb = (0u - jm) & jm; sb; sb = (sb - jm) & jm) {
+                    float3 ref = jpos;
+                    for (unsigned s2 = 0; s2 < P.count; ++s2)
+                        if (sb & (1u << s2)) ref = reflect3(ref, P.p[s2], P.n[s2]);
+                    const float m2 = norm2(sub3(ref, ipos));
+                    if (m2 <= B.lt) {
+                        const float d = fmaxf(h2 - m2, 0.f);
+                        rho.add(d * d * d);
+                        ++count;
                     }
                 }
-            };
-            if (staged) {
-                const float4 *src = wstage + (b - ub);
-                for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
-            } else {
-                for (unsigned t = 0; t < len; ++t) visit(xyz(spos[b + t]), t);
             }
+        };
+        if (staged) {
+            const float4 *src = wstage + (b - ub);
+#pragma unroll 2
+            for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
+        } else {
+            for (unsigned t = 0; t < len; ++t) visit(xyz(spos[b + t]), t);
         }
         if (MASK && active) {
             store_row_mask(S, k, r, len, bits);

@@ -58,6 +58,20 @@ void sph_launch_set_body_position(const Launch &L, unsigned body, const float po
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
 void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);
 void sph_launch_rotate_particles(const Launch &L, float ax, float ay, float az);
+// Device-resident recording: on every `every`-th substep the fields' word
+// ranges of the store's blob are copied into the ring's next frame.  The
+// counters live on the device, so the two launches sit in the substep graph.
+struct RecordPlan {
+    const uint2 *ranges;           // (word offset in the blob, word count) per field
+    unsigned num_ranges;
+    unsigned frame_words;
+    const unsigned *blob;
+    unsigned *ring;                // frames x frame_words
+    unsigned frames, every;
+    unsigned long long *counters;  // [0] substeps seen, [1] frames recorded
+};
+void sph_launch_record(const RecordPlan &p, cudaStream_t stream);
+
 // Rigid bodies: force/torque sums, body substep and particle placement
 // (after the material's step), and the reset that sets bodies up again
 // from their particles' current state.

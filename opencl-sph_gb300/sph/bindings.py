@@ -13,7 +13,7 @@ in record-and-return mode instead of the reference's abort-on-error).
 """
 import ctypes
 import os
-from ctypes import (POINTER, Structure, Union, c_char, c_char_p, c_double, c_float, c_int, c_int32,
+from ctypes import (POINTER, c_ulonglong, Structure, Union, c_char, c_char_p, c_double, c_float, c_int, c_int32,
                     c_size_t, c_uint, c_uint32, c_void_p)
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -190,6 +190,11 @@ _SIGS = {
     # additions
     "sph_synchronize": ([psdata_cuda], c_int),
     "sph_update": ([psdata_cuda, c_uint], c_int),
+    "sph_record_start": ([psdata_cuda, c_size_t, _names, c_uint, c_uint], c_int),
+    "sph_record_stop": ([psdata_cuda], c_int),
+    "sph_record_count": ([psdata_cuda], c_ulonglong),
+    "sph_record_frame_bytes": ([psdata_cuda], c_size_t),
+    "sph_record_read": ([psdata_cuda, c_void_p, c_ulonglong, c_uint], c_int),
     "sph_status": ([psdata_cuda], c_uint),
     "sph_clear_status": ([psdata_cuda], None),
     "sph_version": ([], c_char_p),

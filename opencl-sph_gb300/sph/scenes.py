@@ -176,6 +176,24 @@ def rigid_body_scene(radius=0.05, spacing=0.01, h=0.02, center=(0.2, 0.2, 0.2), 
     return Scene(name or "rigid-%d" % n, "fluid", FLUID_KERNELS, entries, init, n)
 
 
+def large_scene(seed=0):
+    """The large single-scene configuration as two scenes: 1,048,576 WCSPH
+    particles (128 x 64 x 128 at 0.005 m, h = 0.01 m, +-5e-5 m jitter, in
+    [0,1]^3, dt = 2e-5 s) with a rigid ball of radius 0.05 m dropped into
+    them (4,169 lattice particles, the rigid-body extension), and a 32^3 SVK
+    cube (E = 5e4 Pa, nu = 0.35) at the same spacing.  Mixed materials
+    within one store are not a reference feature, so the cube is its own
+    scene.  The fluid's stiffness and viscosity are the dam break's scaled
+    by the 1/8 particle mass (the reference's force omits the neighbour
+    mass)."""
+    fluid = rigid_body_scene(radius=0.05, spacing=0.005, h=0.01, center=(0.32, 0.45, 0.32), fluid=(128, 64, 128),
+                             box=(0.0, 1.0), dt=2e-5, stiffness=0.375, viscosity=0.025, jitter=5e-5, seed=seed,
+                             name="large-fluid+ball")
+    cube = solid_lattice(32, 32, 32, spacing=0.005, h=0.01, material="svk", youngs_modulus=5e4, poisson=0.35,
+                         dt=2e-5, clamp_layers=0, jitter=5e-5, seed=seed + 1, name="large-svk-cube")
+    return [fluid, cube]
+
+
 def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", youngs_modulus=1e5,
                   poisson=0.3, density=1000.0, viscosity=6e-5, gravity=(0.0, -9.8, 0.0), dt=5e-5,
                   clamp_layers=2, jitter=0.0, seed=0, margin=None, name=None):
