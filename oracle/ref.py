@@ -62,6 +62,24 @@ def psdata_lib():
     return _plib
 
 
+_prod = None
+
+
+def product_builder_lib():
+    """The product's library under a ctypes handle of its own, typed for the
+    psdata struct above: configuring it leaves the product's bindings (which
+    load the same library through another handle) untouched."""
+    global _prod
+    if _prod is None:
+        from sph import bindings as bnd
+        _prod = ctypes.CDLL(bnd.LIB_PATH)
+        _prod.build_psdata_from_string.argtypes = [POINTER(psdata), c_char_p]
+        _prod.build_psdata_from_string.restype = None
+        _prod.free_psdata.argtypes = [POINTER(psdata)]
+        _prod.free_psdata.restype = None
+    return _prod
+
+
 def layout(ps):
     """(names, entry_sizes, data_sizes, data_offsets, dims) of a psdata."""
     nf = ps.num_fields
@@ -92,10 +110,7 @@ class RefStore(object):
         if self._own:
             psdata_lib().build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
         else:
-            from sph import bindings as bnd
-            lib = bnd.library
-            lib.build_psdata_from_string.argtypes = [POINTER(psdata), c_char_p]
-            lib.build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
+            product_builder_lib().build_psdata_from_string(ctypes.byref(self.ps), spec.encode())
         self.layout = layout(self.ps)
         self.size = self.layout["data_offsets"][-1] + self.layout["data_sizes"][-1]
 
@@ -126,9 +141,7 @@ class RefStore(object):
             if self._own:
                 psdata_lib().free_psdata(ctypes.byref(self.ps))
             else:
-                from sph import bindings as bnd
-                bnd.library.free_psdata.argtypes = [POINTER(psdata)]
-                bnd.library.free_psdata(ctypes.byref(self.ps))
+                product_builder_lib().free_psdata(ctypes.byref(self.ps))
             self.ps.num_fields = 0
 
 
