@@ -9,10 +9,12 @@
 // of the symmetric matrix.  The rotation for a pivot (a = off-diagonal,
 // b, c = its diagonal pair) is the one with tan(2 theta) = 2a / (b - c) and
 // |theta| <= pi/4, computed with Rutishauser's algebraic form
-// t = sign(tau) / (|tau| + sqrt(1 + tau^2)), tau = (b - c) / (2a),
-// cos = 1/sqrt(1 + t^2), sin = t cos, instead of atan/cos/sin.  A zero
-// pivot gives the identity (the reference evaluates atan(0/0) = NaN when
-// b == c there).
+// t = tan(theta) = sign(tau) / (|tau| + sqrt(1 + tau^2)), tau = (b - c)/(2a),
+// written as 2a sign(b - c) / (|b - c| + sqrt((b - c)^2 + 4a^2)), with
+// cos = rsqrt(1 + t^2), sin = t cos, instead of atan/cos/sin: one square
+// root, one division and one reciprocal square root per rotation, which
+// matters in FP64 on GB300.  A zero pivot gives the identity (the reference
+// evaluates atan(0/0) = NaN when b == c there).
 #pragma once
 
 #include "kernels_common.cuh"
@@ -21,59 +23,82 @@
 #define SPH_PI_F 3.1415926535f
 #endif
 
+// A pivot below this fraction of its diagonal pair is already zero to the
+// precision of T: its rotation (angle ~ the fraction) is skipped.  FP32
+// rotates whenever the pivot is nonzero, as the reference does.
 template <typename T>
-__device__ __forceinline__ void givens_rotate(const T in[6], const T pin[9], unsigned off, T o[6], T pout[9]) {
-    // index sets of common.cl:95-99 for off-diagonal 3 (xy), 4 (xz), 5 (yz)
-    unsigned xx, yy, ee, ex, ey;
-    if (off == 3) { xx = 0; yy = 1; ee = 2; ex = 4; ey = 5; }
-    else if (off == 4) { xx = 0; yy = 2; ee = 1; ex = 3; ey = 5; }
-    else { xx = 1; yy = 2; ee = 0; ex = 3; ey = 4; }
-    const T a = in[off], b = in[xx], c = in[yy];
+struct GivensSkip {
+    static constexpr T rel = T(0);
+};
+template <>
+struct GivensSkip<double> {
+    static constexpr double rel = 1e-15;
+};
+
+// One Givens rotation of the symmetric 6-vector s ([xx,yy,zz,xy,xz,yz])
+// zeroing the off-diagonal OFF, applied in place to s and to the columns
+// of the accumulated rotation p (row-major 3x3).  The index sets are those
+// of common.cl:95-99; the pivot is a compile-time constant so that s and p
+// stay in registers.
+template <typename T, int OFF>
+__device__ __forceinline__ void givens_rotate(T s[6], T p[9]) {
+    constexpr int XX = OFF == 5 ? 1 : 0, YY = OFF == 3 ? 1 : 2, EX = OFF == 3 ? 4 : 3, EY = OFF == 5 ? 4 : 5;
+    const T a = s[OFF], b = s[XX], c = s[YY];
     T cs = 1, sn = 0;
-    if (a != T(0)) {
-        T tau = (b - c) / (T(2) * a);
-        T t = copysign(T(1), tau) / (fabs(tau) + sqrt(T(1) + tau * tau));
-        cs = T(1) / sqrt(T(1) + t * t);
+    if (fabs(a) > GivensSkip<T>::rel * (fabs(b) + fabs(c)) && a != T(0)) {
+        // tau = (b - c) / (2a), t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
+        // multiplied through by 2|a|: one sqrt and one division
+        const T d = b - c;
+        const T r = sqrt(d * d + T(4) * a * a);
+        const T t = (d < T(0) ? -T(2) : T(2)) * a / (fabs(d) + r);
+        cs = rsqrt(T(1) + t * t);
         sn = t * cs;
     }
     const T c2 = cs * cs, s2 = sn * sn, csn = cs * sn;
-    o[xx] = b * c2 + c * s2 + T(2) * a * csn;
-    o[off] = -b * csn + c * csn + a * (c2 - s2);
-    o[yy] = b * s2 + c * c2 - T(2) * a * csn;
-    o[ee] = in[ee];
-    o[ex] = in[ex] * cs + in[ey] * sn;
-    o[ey] = -in[ex] * sn + in[ey] * cs;
-    for (unsigned r = 0; r < 3; ++r) {
-        pout[3 * r + xx] = pin[3 * r + xx] * cs + pin[3 * r + yy] * sn;
-        pout[3 * r + yy] = -pin[3 * r + xx] * sn + pin[3 * r + yy] * cs;
-        pout[3 * r + ee] = pin[3 * r + ee];
+    s[XX] = b * c2 + c * s2 + T(2) * a * csn;
+    s[OFF] = -b * csn + c * csn + a * (c2 - s2);
+    s[YY] = b * s2 + c * c2 - T(2) * a * csn;
+    const T ex = s[EX], ey = s[EY];
+    s[EX] = ex * cs + ey * sn;
+    s[EY] = -ex * sn + ey * cs;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const T px = p[3 * r + XX], py = p[3 * r + YY];
+        p[3 * r + XX] = px * cs + py * sn;
+        p[3 * r + YY] = -px * sn + py * cs;
     }
 }
 
 template <typename T>
-__device__ __forceinline__ unsigned max_offdiag(const T t[6]) {
+__device__ __forceinline__ int max_offdiag(const T t[6]) {
     T m = 0;
-    unsigned im = 0;
-    for (unsigned k = 0; k < 3; ++k) {
+    int im = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
         T v = fabs(t[3 + k]);
         if (v > m) { m = v; im = k; }
     }
     return im + 3;
 }
 
-// jacobi(i, 0, 8, ...) of common.cl:257-295
+// jacobi(i, 0, 8, ...) of common.cl:257-295: eight rotations, each on the
+// largest remaining off-diagonal.
 template <typename T>
 __device__ void jacobi8(const T in[6], T eig[3], T p[9]) {
-    T p2[9], t[6], t2[6];
+    T t[6];
+#pragma unroll
     for (int k = 0; k < 9; ++k) p[k] = (k % 4 == 0) ? T(1) : T(0);
+#pragma unroll
     for (int k = 0; k < 6; ++k) t[k] = in[k];
-    unsigned im = max_offdiag(t);
-    for (int it = 0; it < 4; ++it) {
-        givens_rotate(t, p, im, t2, p2);
-        im = max_offdiag(t2);
-        givens_rotate(t2, p2, im, t, p);
-        im = max_offdiag(t);
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        switch (max_offdiag(t)) {
+        case 3: givens_rotate<T, 3>(t, p); break;
+        case 4: givens_rotate<T, 4>(t, p); break;
+        default: givens_rotate<T, 5>(t, p); break;
+        }
     }
+#pragma unroll
     for (int k = 0; k < 3; ++k) eig[k] = t[k];
 }
 
@@ -105,7 +130,7 @@ __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
     s[5] = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
     double eig[3], P[9], tmp[6], R[9];
     jacobi8(s, eig, P);
-    for (int k = 0; k < 3; ++k) eig[k] = 1.0 / sqrt(eig[k]);
+    for (int k = 0; k < 3; ++k) eig[k] = rsqrt(eig[k]);
     p_d_pt(eig, P, tmp);
     mul_as(A, tmp, R);
     for (int k = 0; k < 9; ++k) r[k] = (float)R[k];
