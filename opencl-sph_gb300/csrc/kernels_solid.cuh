@@ -36,36 +36,57 @@ struct GivensSkip<double> {
 };
 
 // One Givens rotation of the symmetric 6-vector s ([xx,yy,zz,xy,xz,yz])
-// zeroing the off-diagonal OFF, applied in place to s and to the columns
-// of the accumulated rotation p (row-major 3x3).  The index sets are those
-// of common.cl:95-99; the pivot is a compile-time constant so that s and p
-// stay in registers.
-template <typename T, int OFF>
-__device__ __forceinline__ void givens_rotate(T s[6], T p[9]) {
-    constexpr int XX = OFF == 5 ? 1 : 0, YY = OFF == 3 ? 1 : 2, EX = OFF == 3 ? 4 : 3, EY = OFF == 5 ? 4 : 5;
-    const T a = s[OFF], b = s[XX], c = s[YY];
+// zeroing the off-diagonal `off` (3, 4 or 5), applied in place to s and to
+// the columns of the accumulated rotation p (row-major 3x3).  The index
+// sets are those of common.cl:95-99.  The pivot's entries are picked and
+// written back with selects, so all lanes run one arithmetic path and s and
+// p stay in registers.
+template <typename T>
+__device__ __forceinline__ void givens_rotate(T s[6], T p[9], int off) {
+    const bool o3 = off == 3, o4 = off == 4, o5 = off == 5;
+    // xx = o5 ? 1 : 0, yy = o3 ? 1 : 2, (ex, ey) = o3 ? (4, 5) : o4 ? (3, 5) : (3, 4)
+    const T a = o3 ? s[3] : o4 ? s[4] : s[5];
+    const T b = o5 ? s[1] : s[0];
+    const T c = o3 ? s[1] : s[2];
+    const T ex = o3 ? s[4] : s[3];
+    const T ey = o5 ? s[4] : s[5];
     T cs = 1, sn = 0;
     if (fabs(a) > GivensSkip<T>::rel * (fabs(b) + fabs(c)) && a != T(0)) {
         // tau = (b - c) / (2a), t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
-        // multiplied through by 2|a|: one sqrt and one division
+        // multiplied through by 2|a|: one sqrt and one division.  Equal
+        // diagonals (tau = +-0) give t = sign(a) directly: there 4a^2 may
+        // underflow to 0 in FP32 while a does not.
         const T d = b - c;
-        const T r = sqrt(d * d + T(4) * a * a);
-        const T t = (d < T(0) ? -T(2) : T(2)) * a / (fabs(d) + r);
+        T t;
+        if (d == T(0)) {
+            t = copysign(T(1), a);
+        } else {
+            const T r = sqrt(d * d + T(4) * a * a);
+            t = (d < T(0) ? -T(2) : T(2)) * a / (fabs(d) + r);
+        }
         cs = rsqrt(T(1) + t * t);
         sn = t * cs;
     }
     const T c2 = cs * cs, s2 = sn * sn, csn = cs * sn;
-    s[XX] = b * c2 + c * s2 + T(2) * a * csn;
-    s[OFF] = -b * csn + c * csn + a * (c2 - s2);
-    s[YY] = b * s2 + c * c2 - T(2) * a * csn;
-    const T ex = s[EX], ey = s[EY];
-    s[EX] = ex * cs + ey * sn;
-    s[EY] = -ex * sn + ey * cs;
+    const T nb = b * c2 + c * s2 + T(2) * a * csn;
+    const T na = -b * csn + c * csn + a * (c2 - s2);
+    const T nc = b * s2 + c * c2 - T(2) * a * csn;
+    const T nex = ex * cs + ey * sn;
+    const T ney = -ex * sn + ey * cs;
+    s[0] = o5 ? s[0] : nb;
+    s[1] = o5 ? nb : o3 ? nc : s[1];
+    s[2] = o3 ? s[2] : nc;
+    s[3] = o3 ? na : nex;
+    s[4] = o4 ? na : o3 ? nex : ney;
+    s[5] = o5 ? na : ney;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-        const T px = p[3 * r + XX], py = p[3 * r + YY];
-        p[3 * r + XX] = px * cs + py * sn;
-        p[3 * r + YY] = -px * sn + py * cs;
+        T *row = p + 3 * r;
+        const T px = o5 ? row[1] : row[0], py = o3 ? row[1] : row[2];
+        const T nx = px * cs + py * sn, ny = -px * sn + py * cs;
+        row[0] = o5 ? row[0] : nx;
+        row[1] = o5 ? nx : o3 ? ny : row[1];
+        row[2] = o3 ? row[2] : ny;
     }
 }
 
@@ -91,13 +112,7 @@ __device__ void jacobi8(const T in[6], T eig[3], T p[9]) {
 #pragma unroll
     for (int k = 0; k < 6; ++k) t[k] = in[k];
 #pragma unroll 1
-    for (int it = 0; it < 8; ++it) {
-        switch (max_offdiag(t)) {
-        case 3: givens_rotate<T, 3>(t, p); break;
-        case 4: givens_rotate<T, 4>(t, p); break;
-        default: givens_rotate<T, 5>(t, p); break;
-        }
-    }
+    for (int it = 0; it < 8; ++it) givens_rotate(t, p, max_offdiag(t));
 #pragma unroll
     for (int k = 0; k < 3; ++k) eig[k] = t[k];
 }
