@@ -68,6 +68,7 @@ PHASE_BYTES = {
     "step_forward": (76, 0),
     # batched-form phases (bench_batched): the same figures per material
     "bins": (44, 20),                 # find/count/insert 44 per particle; zero, scan, copy per cell
+    # (the batched profile reports bins as bin_count, scan and insert)
     "fluid forces+step": (120, 8),
     "corotational passes": (452, 24), # rotations_and_strains 168 + stresses 48 + forces 160 + step 76
     "svk passes": (324, 16),          # deformations 64 + stresses 60 + forces 124 + step 76

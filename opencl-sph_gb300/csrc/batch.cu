@@ -457,8 +457,12 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
     for (unsigned r = 0; r < reps; ++r) {
         PhaseLog log{b->stream};
         Launch A = b->all;
-        log.mark("bins");
-        sph_launch_bins(A);
+        log.mark("bin_count");
+        sph_launch_bin_count(A);
+        log.mark("scan");
+        sph_launch_scan(A);
+        log.mark("insert");
+        sph_launch_insert(A);
         log.mark("gather");
         sph_launch_gather(A, true, false, true);
         log.mark("density");

@@ -59,9 +59,13 @@ void sph_launch_insert(const Launch &L) {
     k_sort_big_cells<<<32, 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
 }
 
-void sph_launch_bins(const Launch &L) {
+void sph_launch_bin_count(const Launch &L) {
     sph_launch_zero_cells(L);
     k_bin_count<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, 1);
+}
+
+void sph_launch_bins(const Launch &L) {
+    sph_launch_bin_count(L);
     sph_launch_scan(L);
     sph_launch_insert(L);
 }
@@ -179,8 +183,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
         if (mark) mark(ctx, name);
     };
     phase("bin_count");
-    sph_launch_zero_cells(L);
-    k_bin_count<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles, 1);
+    sph_launch_bin_count(L);
     phase("scan");
     sph_launch_scan(L);
     phase("insert");

@@ -214,33 +214,6 @@ __device__ __forceinline__ unsigned long long load_row_mask(const SceneDesc &S, 
     return ((unsigned long long)hi << 32) | lo;
 }
 
-// The candidates of particle k's recorded masks as one stream across the
-// rows, in order (for loops that fetch the next neighbour ahead).
-struct MaskWalk {
-    const SceneDesc *S;
-    unsigned k;
-    StencilRows rows;
-    int r;
-    unsigned rb;
-    unsigned long long m;
-    __device__ __forceinline__ MaskWalk(const SceneDesc &s, unsigned k_, const StencilRows &rows_)
-        : S(&s), k(k_), rows(rows_), r(0), rb(0), m(0) {}
-    __device__ __forceinline__ bool next(unsigned *kk) {
-        while (m == 0) {
-            if (r == 9) return false;
-            unsigned b, e;
-            rows.row(*S, r, &b, &e);
-            m = load_row_mask(*S, k, r, e - b);
-            rb = b;
-            ++r;
-        }
-        const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
-        m &= m - 1ull;
-        *kk = rb + t;
-        return true;
-    }
-};
-
 // Calls f(kk) for the candidates of particle k's recorded masks, in order.
 template <class F>
 __device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {

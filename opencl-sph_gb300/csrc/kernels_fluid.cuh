@@ -249,10 +249,9 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
 }
 
 // The fused-substep force pass: walks the candidate masks the density pass
-// recorded as one stream across the rows, reading each neighbour's
-// position and its velocity with the density in w (two float4 loads,
-// issued one neighbour ahead).  Lanes whose masks overflowed scan the
-// stencil.
+// recorded, row by row, reading each neighbour's position and its velocity
+// with the density in w (two float4 loads).  Lanes whose masks overflowed
+// scan the stencil.
 __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
@@ -263,31 +262,12 @@ __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, Blo
         const unsigned cell = S.gridcell[i];
         Kahan3 f;
         if (S.ncand[k] != SPH_NCAND_SCAN) {
-            // the next neighbour's loads are issued before this one's
-            // arithmetic, to overlap their latency
             const float4 *__restrict__ spos = S.spos;
             const float4 *__restrict__ svel = S.svel;
-            MaskWalk walk(S, k, StencilRows(S, cell));
-            unsigned kk = 0;
-            bool have = walk.next(&kk);
-            float4 p = make_float4(0.f, 0.f, 0.f, 0.f), v = p;
-            if (have) {
-                p = spos[kk];
-                v = svel[kk];
-            }
-            while (have) {
-                unsigned kn = 0;
-                const bool more = walk.next(&kn);
-                float4 pn = p, vn = v;
-                if (more) {
-                    pn = spos[kn];
-                    vn = svel[kn];
-                }
-                fluid_pair(I, xyz(p), xyz(v), v.w, f);
-                p = pn;
-                v = vn;
-                have = more;
-            }
+            for_each_masked(S, k, StencilRows(S, cell), [&](unsigned kk) {
+                const float4 v = svel[kk];
+                fluid_pair(I, xyz(spos[kk]), xyz(v), v.w, f);
+            });
         } else {
             fluid_scan(S, cell, I, f);
         }

@@ -4,17 +4,17 @@
 // force pass, kinematic bodies (kernels/rigidbody.cl) and the scene-init
 // kernels of common.cl.
 //
-// The 3x3 eigen-solver keeps the reference's scheme (common.cl:101-305):
-// eight Givens rotations, each zeroing the largest remaining off-diagonal
-// of the symmetric matrix.  The rotation for a pivot (a = off-diagonal,
-// b, c = its diagonal pair) is the one with tan(2 theta) = 2a / (b - c) and
-// |theta| <= pi/4, computed with Rutishauser's algebraic form
-// t = tan(theta) = sign(tau) / (|tau| + sqrt(1 + tau^2)), tau = (b - c)/(2a),
-// written as 2a sign(b - c) / (|b - c| + sqrt((b - c)^2 + 4a^2)), with
-// cos = rsqrt(1 + t^2), sin = t cos, instead of atan/cos/sin: one square
-// root, one division and one reciprocal square root per rotation, which
-// matters in FP64 on GB300.  A zero pivot gives the identity (the reference
-// evaluates atan(0/0) = NaN when b == c there).
+// The 3x3 symmetric eigen-solver (SVK's Aqq inverse, jacobiInvert) keeps
+// the reference's scheme (common.cl:101-305): eight Givens rotations, each
+// zeroing the largest remaining off-diagonal.  The rotation for a pivot
+// (a = off-diagonal, b, c = its diagonal pair) is the one with
+// tan(2 theta) = 2a / (b - c) and |theta| <= pi/4, computed with
+// Rutishauser's algebraic form t = tan(theta) = sign(tau) / (|tau| +
+// sqrt(1 + tau^2)), tau = (b - c)/(2a), written as 2a sign(b - c) /
+// (|b - c| + sqrt((b - c)^2 + 4a^2)), cos = rsqrt(1 + t^2), sin = t cos,
+// instead of atan/cos/sin.  A zero pivot gives the identity (the reference
+// evaluates atan(0/0) = NaN when b == c there).  The corotational rotation
+// itself is the FP64 polar factor (polar_rotation_fp64).
 #pragma once
 
 #include "kernels_common.cuh"
@@ -22,18 +22,6 @@
 #ifndef SPH_PI_F
 #define SPH_PI_F 3.1415926535f
 #endif
-
-// A pivot below this fraction of its diagonal pair is already zero to the
-// precision of T: its rotation (angle ~ the fraction) is skipped.  FP32
-// rotates whenever the pivot is nonzero, as the reference does.
-template <typename T>
-struct GivensSkip {
-    static constexpr T rel = T(0);
-};
-template <>
-struct GivensSkip<double> {
-    static constexpr double rel = 1e-15;
-};
 
 // One Givens rotation of the symmetric 6-vector s ([xx,yy,zz,xy,xz,yz])
 // zeroing the off-diagonal `off` (3, 4 or 5), applied in place to s and to
@@ -51,7 +39,7 @@ __device__ __forceinline__ void givens_rotate(T s[6], T p[9], int off) {
     const T ex = o3 ? s[4] : s[3];
     const T ey = o5 ? s[4] : s[5];
     T cs = 1, sn = 0;
-    if (fabs(a) > GivensSkip<T>::rel * (fabs(b) + fabs(c)) && a != T(0)) {
+    if (a != T(0)) {
         // tau = (b - c) / (2a), t = sign(tau) / (|tau| + sqrt(1 + tau^2)),
         // multiplied through by 2|a|: one sqrt and one division.  Equal
         // diagonals (tau = +-0) give t = sign(a) directly: there 4a^2 may
@@ -132,23 +120,43 @@ __device__ __forceinline__ void mul_as(const T a[9], const T s[6], T out[9]) {
         for (int c = 0; c < 3; ++c) out[3 * r + c] = a[3 * r] * S9[c] + a[3 * r + 1] * S9[3 + c] + a[3 * r + 2] * S9[6 + c];
 }
 
-// getR (common.cl:306-331) in FP64: R = A (A^T A)^(-1/2).
+// getR (common.cl:306-331): the rotation R of the polar decomposition
+// A = R U, in FP64.  The reference forms R = A (A^T A)^(-1/2) through its
+// 8-rotation Jacobi eigensolver.  Here Newton's polar iteration
+// X <- (X + X^-T) / 2 (Higham, 1986), started from A scaled to the
+// Frobenius norm of a rotation, converges quadratically to the same factor
+// -- to FP64 precision, where the 8 rotations stop at theirs -- with about
+// half the FP64 operations of the Jacobi form (GB300's FP64 pipe is narrow).
+// X^-T is the cofactor matrix over the determinant.  A singular A (NaN in
+// the reference) gives NaN here as well.
 __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
-    double A[9];
-    for (int k = 0; k < 9; ++k) A[k] = (double)apq[k];
-    double s[6];
-    s[0] = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
-    s[1] = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
-    s[2] = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
-    s[3] = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
-    s[4] = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
-    s[5] = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
-    double eig[3], P[9], tmp[6], R[9];
-    jacobi8(s, eig, P);
-    for (int k = 0; k < 3; ++k) eig[k] = rsqrt(eig[k]);
-    p_d_pt(eig, P, tmp);
-    mul_as(A, tmp, R);
-    for (int k = 0; k < 9; ++k) r[k] = (float)R[k];
+    double X[9];
+    double n2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        X[k] = (double)apq[k];
+        n2 += X[k] * X[k];
+    }
+    const double g = 1.7320508075688772 * rsqrt(n2);  // sqrt(3) / |A|_F
+#pragma unroll
+    for (int k = 0; k < 9; ++k) X[k] *= g;
+#pragma unroll 1
+    for (int it = 0; it < 16; ++it) {
+        const double C[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
+                             X[2] * X[7] - X[1] * X[8], X[0] * X[8] - X[2] * X[6], X[1] * X[6] - X[0] * X[7],
+                             X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
+        const double rd = 1.0 / (X[0] * C[0] + X[1] * C[1] + X[2] * C[2]);
+        double delta = 0.0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const double nx = 0.5 * (X[k] + C[k] * rd);
+            delta = fmax(delta, fabs(nx - X[k]));
+            X[k] = nx;
+        }
+        if (!(delta > 1e-15)) break;  // converged (or NaN: stop)
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r[k] = (float)X[k];
 }
 
 // jacobiInvert (common.cl:296-305) in FP32

@@ -38,6 +38,9 @@ void sph_launch_zero_cells(const Launch &L);
 void sph_launch_count(const Launch &L);
 void sph_launch_scan(const Launch &L);
 void sph_launch_insert(const Launch &L);  // scatter + per-cell ordering
+// zero_gridcount + find_particle_bins + count_particles_in_bins in one
+// pass, recording each particle's arrival slot
+void sph_launch_bin_count(const Launch &L);
 // All of compute_particle_bins: zero, bin+count, scan, insert.
 void sph_launch_bins(const Launch &L);
 // Cell-sorted copies (positions; velocities and densities on request).
