@@ -220,8 +220,10 @@ __global__ void k_sort_cells(const SceneDesc *__restrict__ scenes, BlockMap map)
 // one block bitonic-sorts each queued cell, padded to a power of two, in a
 // scratch region of the sorted-position buffer ([2*off, 2*off + L) of its
 // words, which cannot overlap another cell's region since L < 2*count).
+// grid (blocks per scene, scenes): blockIdx.y is the scene, so a batch of
+// many scenes without crowded cells costs one load per block.
 __global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
-    for (unsigned s = 0; s < num_scenes; ++s) {
+    for (unsigned s = blockIdx.y; s < num_scenes; s += gridDim.y) {
         const SceneDesc &S = scenes[s];
         if (scene_idle(S)) continue;
         const unsigned nbig = S.big_cells[0];
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__rest
 
 // Cell-sorted copies: spos[k] = position[cellparticles[k]] (and velocity,
 // density when asked; for solids also the rest position with the body
-// number, and density0 in the velocity copy's w).  Gathers once so the pair loops stream float4s.
+// number, and 1/density0 in the velocity copy's w).  Gathers once so the pair loops stream float4s.
 __global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int with_vel, int with_dens,
                          int with_solid) {
     SPH_FOR_WORK(map)
@@ -271,7 +273,7 @@ __global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int
         const bool solid = with_solid && S.spos0;
         if (with_vel || solid) {
             float3 v = ld3(S.velocity, i);
-            S.svel[item] = make_float4(v.x, v.y, v.z, solid ? S.density0[i] : 0.f);
+            S.svel[item] = make_float4(v.x, v.y, v.z, solid ? __frcp_rn(S.density0[i]) : 0.f);
         }
         if (with_dens) S.sdens[item] = S.density[i];
         if (solid) {

@@ -721,7 +721,7 @@ __global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap
         }
         for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)i + c] = o[c];
         S.sstress[2 * (size_t)k] = make_float4(o[0], o[1], o[2], o[3]);
-        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], 0.f, 0.f);
+        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], __fdiv_rn(*S.mass, S.sdens[k]), 0.f);
     }
     SPH_END_WORK
 }
@@ -730,34 +730,39 @@ __global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap
 // stress and rotation, and whether it belongs to a body.
 struct SolidSide {
     float3 pos, pos0, vel;
-    float rho0, rho;
+    float inv_rho0;  // 1 / density0, correctly rounded
+    float mrho;      // mass / density, correctly rounded
     float s[6], R[9];
     bool body;
 };
 
 template <bool COROT>
-__device__ __forceinline__ void side_from_fields(const SceneDesc &S, unsigned j, float3 pos, SolidSide &J) {
+__device__ __forceinline__ void side_from_fields(const SceneDesc &S, unsigned j, float3 pos, float mass,
+                                                 SolidSide &J) {
     J.pos = pos;
     J.pos0 = ld3(S.originalpos, j);
     J.vel = ld3(S.velocity, j);
-    J.rho0 = S.density0[j];
-    J.rho = S.density[j];
+    J.inv_rho0 = __frcp_rn(S.density0[j]);
+    J.mrho = __fdiv_rn(mass, S.density[j]);
     for (int c = 0; c < 6; ++c) J.s[c] = S.stress[6 * (size_t)j + c];
     if (COROT)
         for (int c = 0; c < 9; ++c) J.R[c] = S.rotation[9 * (size_t)j + c];
     J.body = S.body_number[j] > 0;
 }
 
+// The same values from the sorted copies: k_gather put 1/density0 in the
+// velocity copy's w, k_stresses_sorted put mass/density in the second
+// stress float4's z.
 template <bool COROT>
 __device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk, SolidSide &J) {
     const float4 p = S.spos[kk], p0 = S.spos0[kk], v = S.svel[kk];
     J.pos = xyz(p);
     J.pos0 = xyz(p0);
     J.vel = xyz(v);
-    J.rho0 = v.w;
-    J.rho = S.sdens[kk];
+    J.inv_rho0 = v.w;
     const float4 s0 = S.sstress[2 * (size_t)kk], s1 = S.sstress[2 * (size_t)kk + 1];
     J.s[0] = s0.x; J.s[1] = s0.y; J.s[2] = s0.z; J.s[3] = s0.w; J.s[4] = s1.x; J.s[5] = s1.y;
+    J.mrho = s1.z;
     if (COROT)
         for (int c = 0; c < 3; ++c) {
             const float4 r = S.srot[3 * (size_t)kk + c];
@@ -769,21 +774,24 @@ __device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk
 }
 
 // The direct pair term of compute_forces_solids (solid_corotation.cl:
-// 215-403, solid_svk.cl:182-367) without symmetry images.
+// 215-403, solid_svk.cl:182-367) without symmetry images.  The volume
+// factors come from per-particle reciprocals (m^2 / (rho0_i rho0_j) as
+// m^2 * (1/rho0_i) * (1/rho0_j)) and the Laplacian's distance from rsqrt,
+// so a pair costs no division or square root.
 template <bool COROT>
 __device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidSide &I, const SolidSide &J,
                                            Kahan3 &fe_s, Kahan3 &fv_s) {
     const float3 x = sub3(I.pos0, J.pos0);
     const float r2 = norm2(sub3(J.pos, I.pos));
     if (!(norm2(x) <= C.le || r2 <= C.le)) return;
-    const float vivj = C.mass * C.mass / I.rho0 / J.rho0;
-    const float mrj = C.mass / J.rho;
+    const float vivj = __fmul_rn(__fmul_rn(__fmul_rn(C.mass, C.mass), I.inv_rho0), J.inv_rho0);
     const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
     const float3 f_ji = sym_vec(I.s, gx) * (-vivj);
     const float3 f_ij = J.body ? -f_ji : sym_vec(J.s, -gx) * (-vivj);
     const float3 fe = COROT ? mat_vec(J.R, f_ij) - mat_vec(I.R, f_ji) : f_ij - f_ji;
-    const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
-    const float3 fv = (J.vel - I.vel) * (mrj * lap);
+    const float dist = r2 > 0.f ? __fmul_rn(r2, rsqrtf(r2)) : 0.f;
+    const float lap = r2 <= C.le ? C.kv * (C.h - dist) : 0.f;
+    const float3 fv = (J.vel - I.vel) * (J.mrho * lap);
     fe_s.add(fe);
     fv_s.add(fv);
 }
@@ -802,13 +810,13 @@ __global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap m
         const SolidConsts C = solid_consts(S);
         SolidSide I;
         if (MASKED) side_from_sorted<COROT>(S, k, I);
-        else side_from_fields<COROT>(S, i, xyz(S.spos[k]), I);
+        else side_from_fields<COROT>(S, i, xyz(S.spos[k]), C.mass, I);
         Kahan3 fe_s, fv_s;
         auto visit = [&](unsigned kk) {
             if (kk == k) return;
             SolidSide J;
             if (MASKED) side_from_sorted<COROT>(S, kk, J);
-            else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), J);
+            else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), C.mass, J);
             solid_pair<COROT>(C, I, J, fe_s, fv_s);
         };
         if (MASKED && S.ncand[k] != SPH_NCAND_SCAN)

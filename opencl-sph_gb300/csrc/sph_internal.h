@@ -91,8 +91,9 @@ struct SceneDesc {
     unsigned *nbmask;
     unsigned *ncand;
     // solids: cell-sorted copies for the fused substep's pair passes --
-    // rest position (w: body_number bits), stress (6 of 8 floats), rotation
-    // (3 rows of 4 floats); the velocity copy carries density0 in w
+    // rest position (w: body_number bits), stress (6 floats, then
+    // mass/density), rotation (3 rows of 4 floats); the velocity copy
+    // carries 1/density0 in w
     float4 *spos0, *sstress, *srot;
     // batched form only (null otherwise): substeps this scene still takes;
     // at 0 every kernel skips the scene, SPH_STEPS_UNLIMITED never expires
