@@ -24,16 +24,7 @@ cudaError_t sph_prepare_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
-    if (e != cudaSuccess) return e;
-    // the masked force passes keep a hit list per thread
-    size_t hwant = hitlist_smem_bytes(512);
-    if (max_optin > 0 && hwant > (size_t)max_optin) hwant = (size_t)max_optin;
-    e = cudaFuncSetAttribute(k_forces_fluids_masked, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hwant);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_forces_solids<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)hwant);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_forces_solids<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)hwant);
+    return e;
 }
 
 cudaError_t sph_check_launch(const char *what) {
@@ -96,9 +87,8 @@ void sph_launch_density(const Launch &L, bool original, bool mask) {
 
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
     if (masked)
-        k_forces_fluids_masked<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block,
-                                 hitlist_smem_bytes(L.pair_block), L.stream>>>(L.scenes, L.pair_particles,
-                                                                               fuse_step ? 1 : 0);
+        k_forces_fluids_masked<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+            L.scenes, L.pair_particles, fuse_step ? 1 : 0);
     else
         k_forces_fluids<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
             L.scenes, L.pair_particles, fuse_step ? 1 : 0);
@@ -142,14 +132,13 @@ void sph_launch_deformations(const Launch &L) {
 
 void sph_launch_forces_solids(const Launch &L, bool corot, bool masked) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    const size_t hs = hitlist_smem_bytes(L.pair_block);
     if (corot) {
-        if (masked) k_forces_solids<true, true><<<g, L.pair_block, hs, L.stream>>>(L.scenes, L.pair_particles);
+        if (masked) k_forces_solids<true, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
         else k_forces_solids<true, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
         if (!L.no_symmetry_planes)
             k_forces_solids_planes<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
     } else {
-        if (masked) k_forces_solids<false, true><<<g, L.pair_block, hs, L.stream>>>(L.scenes, L.pair_particles);
+        if (masked) k_forces_solids<false, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
         else k_forces_solids<false, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
         if (!L.no_symmetry_planes)
             k_forces_solids_planes<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);

@@ -214,35 +214,6 @@ __device__ __forceinline__ unsigned long long load_row_mask(const SceneDesc &S, 
     return ((unsigned long long)hi << 32) | lo;
 }
 
-// Hit lists: up to SPH_HITS of a particle's masked candidates gathered, in
-// order, into shared memory (entry t of thread x at list[t * blockDim.x +
-// x]), so that the walk over them runs in lockstep across the warp: the
-// warp then iterates the largest count of its lanes instead of the sum
-// over rows of each row's largest count.
-#define SPH_HITS 64
-
-__host__ __device__ constexpr size_t hitlist_smem_bytes(unsigned block) { return 4u * SPH_HITS * block; }
-
-// Fills the list; returns the number of masked candidates in all (which
-// may exceed SPH_HITS: the caller walks the rest in order).
-__device__ __forceinline__ unsigned gather_hits(const SceneDesc &S, unsigned k, const StencilRows &rows,
-                                                unsigned *list) {
-    unsigned n = 0;
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        unsigned b, e;
-        rows.row(S, r, &b, &e);
-        unsigned long long m = load_row_mask(S, k, r, e - b);
-        while (m) {
-            const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
-            m &= m - 1ull;
-            if (n < SPH_HITS) list[n * blockDim.x + threadIdx.x] = b + t;
-            ++n;
-        }
-    }
-    return n;
-}
-
 // Calls f(kk) for the candidates of particle k's recorded masks, in order.
 template <class F>
 __device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {

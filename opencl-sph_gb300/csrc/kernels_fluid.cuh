@@ -249,11 +249,10 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
 }
 
 // The fused-substep force pass: walks the candidate masks the density pass
-// recorded through a hit list, reading each neighbour's position and its
-// velocity with the density in w (two float4 loads).  Lanes whose masks
-// overflowed scan the stencil.
+// recorded, row by row, reading each neighbour's position and its velocity
+// with the density in w (two float4 loads).  Lanes whose masks overflowed
+// scan the stencil.
 __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
-    extern __shared__ unsigned hit_list[];  // hitlist_smem_bytes(blockDim.x)
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
         const unsigned k = item;
@@ -265,22 +264,10 @@ __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, Blo
         if (S.ncand[k] != SPH_NCAND_SCAN) {
             const float4 *__restrict__ spos = S.spos;
             const float4 *__restrict__ svel = S.svel;
-            auto visit = [&](unsigned kk) {
+            for_each_masked(S, k, StencilRows(S, cell), [&](unsigned kk) {
                 const float4 v = svel[kk];
                 fluid_pair(I, xyz(spos[kk]), xyz(v), v.w, f);
-            };
-            // the masked neighbours in lockstep from a shared-memory list;
-            // any past SPH_HITS follow in the same order
-            const StencilRows rows(S, cell);
-            const unsigned total = gather_hits(S, k, rows, hit_list);
-            const unsigned nl = total < SPH_HITS ? total : SPH_HITS;
-            for (unsigned t = 0; t < nl; ++t) visit(hit_list[t * blockDim.x + threadIdx.x]);
-            if (total > SPH_HITS) {
-                unsigned seen = 0;
-                for_each_masked(S, k, rows, [&](unsigned kk) {
-                    if (seen++ >= SPH_HITS) visit(kk);
-                });
-            }
+            });
         } else {
             fluid_scan(S, cell, I, f);
         }

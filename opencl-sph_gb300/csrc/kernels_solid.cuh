@@ -797,13 +797,11 @@ __device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidSide
 }
 
 // compute_forces_solids for plane-free scenes.  MASKED (a fused substep):
-// walks the masks of the substep's first pair pass through a hit list,
-// reading the sorted copies; otherwise (a named call) scans every
-// candidate, reading the fields.  Without images the cut-off force equals
-// the force.
+// walks the masks of the substep's first pair pass, reading the sorted
+// copies; otherwise (a named call) scans every candidate, reading the
+// fields.  Without images the cut-off force equals the force.
 template <bool COROT, bool MASKED>
 __global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    extern __shared__ unsigned hit_list[];  // MASKED: hitlist_smem_bytes(blockDim.x)
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || (MASKED && !S.sstress)) continue;
     if (item < active_count(S)) {
@@ -821,22 +819,10 @@ __global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap m
             else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), C.mass, J);
             solid_pair<COROT>(C, I, J, fe_s, fv_s);
         };
-        if (MASKED && S.ncand[k] != SPH_NCAND_SCAN) {
-            // the masked neighbours in lockstep from a shared-memory list;
-            // any past SPH_HITS follow in the same order
-            const StencilRows rows(S, S.gridcell[i]);
-            const unsigned total = gather_hits(S, k, rows, hit_list);
-            const unsigned nl = total < SPH_HITS ? total : SPH_HITS;
-            for (unsigned t = 0; t < nl; ++t) visit(hit_list[t * blockDim.x + threadIdx.x]);
-            if (total > SPH_HITS) {
-                unsigned seen = 0;
-                for_each_masked(S, k, rows, [&](unsigned kk) {
-                    if (seen++ >= SPH_HITS) visit(kk);
-                });
-            }
-        } else {
+        if (MASKED && S.ncand[k] != SPH_NCAND_SCAN)
+            for_each_masked(S, k, StencilRows(S, S.gridcell[i]), visit);
+        else
             for_each_neighbour(S, S.gridcell[i], visit);
-        }
         const float visc = *S.viscosity;
         const float3 fe = fe_s.get() * 0.5f, fv = fv_s.get() * visc;
         st3(S.force, i, fe + fv);
