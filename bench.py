@@ -423,6 +423,20 @@ def plain_step_model(sizes, steps=20):
     return model
 
 
+def _chunk_profile(log):
+    """Chunks binned by resident particles: particle-steps/s in each bin."""
+    bins = {}
+    for resident, scenes, chunk, advanced, dt in log:
+        key = "%dM" % min(8, int(resident / 1e6))
+        b = bins.setdefault(key, [0, 0.0, 0.0, 0])
+        b[0] += 1
+        b[1] += advanced
+        b[2] += dt
+        b[3] += scenes
+    return {k: {"chunks": v[0], "particle_steps_per_s": v[1] / v[2] if v[2] else 0.0,
+                "mean_scenes": v[3] / v[0]} for k, v in sorted(bins.items())}
+
+
 def bench_served(args):
     """Poisson arrivals at 50 requests/s; each request a scene of the batched
     mix with 2,000-262,144 particles (log-uniform) and 100-2,000 substeps
@@ -446,6 +460,7 @@ def bench_served(args):
             "throughput": st["throughput"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
             "makespan_s": st["makespan_s"], "peak_resident": st["peak_resident"],
             "peak_particles": st["peak_particles"], "chunks": st["chunks"], "gpu_busy_s": st["gpu_busy_s"],
+            "busy_throughput": st["busy_throughput"], "chunk_profile": _chunk_profile(st["chunk_log"]),
             "offered_load": demand, "saturated": bool(demand > st["throughput"]),
             "policy": "FIFO admission by 150 GB HBM budget and 8M resident particles; device-side substep "
                       "quotas; chunks of up to 25 substeps",

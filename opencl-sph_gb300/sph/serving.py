@@ -95,6 +95,7 @@ class Server(object):
 
         chunks = 0
         substeps = 0
+        log = []  # per chunk: resident particles, scenes, substeps, particle-steps advanced, seconds
         peak_resident = 0
         peak_particles = 0
         peak_bytes = 0
@@ -122,10 +123,13 @@ class Server(object):
             peak_particles = max(peak_particles, resident)
             peak_bytes = max(peak_bytes, batch.bytes)
             chunk = min(self.max_chunk, max(r.remaining for r in active.values()))
+            advanced = sum(r.scene.n * min(chunk, r.remaining) for r in active.values())
             c0 = time.perf_counter()
             batch.step(chunk)
             batch.synchronize()
-            busy += time.perf_counter() - c0
+            dt = time.perf_counter() - c0
+            busy += dt
+            log.append((resident, len(active), chunk, advanced, dt))
             chunks += 1
             substeps += chunk
             for sid, r in list(active.items()):
@@ -153,6 +157,10 @@ class Server(object):
             "chunks": chunks,
             "substeps": substeps,
             "gpu_busy_s": busy,
+            # particle-steps/s while chunks ran (finished scenes idling in
+            # their last chunk count as not advancing)
+            "busy_throughput": sum(c[3] for c in log) / busy if busy > 0 else 0.0,
+            "chunk_log": log,
             "peak_resident": peak_resident,
             "peak_particles": peak_particles,
             "peak_bytes": peak_bytes,
