@@ -249,9 +249,9 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
 }
 
 // The fused-substep force pass: walks the candidate masks the density pass
-// recorded, row by row, reading each neighbour's position and its velocity
-// with the density in w (two float4 loads).  Lanes whose masks overflowed
-// scan the stencil.
+// recorded, row by row and two neighbours at a time, reading each
+// neighbour's position and its velocity with the density in w (two float4
+// loads).  Lanes whose masks overflowed scan the stencil.
 __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
@@ -264,10 +264,29 @@ __global__ void k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, Blo
         if (S.ncand[k] != SPH_NCAND_SCAN) {
             const float4 *__restrict__ spos = S.spos;
             const float4 *__restrict__ svel = S.svel;
-            for_each_masked(S, k, StencilRows(S, cell), [&](unsigned kk) {
-                const float4 v = svel[kk];
-                fluid_pair(I, xyz(spos[kk]), xyz(v), v.w, f);
-            });
+            // two neighbours per iteration: both loads are in flight
+            // before the first pair's arithmetic (same order)
+            const StencilRows rows(S, cell);
+#pragma unroll 1
+            for (int r = 0; r < 9; ++r) {
+                unsigned b, e;
+                rows.row(S, r, &b, &e);
+                unsigned long long m = load_row_mask(S, k, r, e - b);
+                while (m) {
+                    const unsigned t1 = (unsigned)(__ffsll((long long)m) - 1);
+                    m &= m - 1ull;
+                    const float4 p1 = spos[b + t1], v1 = svel[b + t1];
+                    if (m) {
+                        const unsigned t2 = (unsigned)(__ffsll((long long)m) - 1);
+                        m &= m - 1ull;
+                        const float4 p2 = spos[b + t2], v2 = svel[b + t2];
+                        fluid_pair(I, xyz(p1), xyz(v1), v1.w, f);
+                        fluid_pair(I, xyz(p2), xyz(v2), v2.w, f);
+                    } else {
+                        fluid_pair(I, xyz(p1), xyz(v1), v1.w, f);
+                    }
+                }
+            }
         } else {
             fluid_scan(S, cell, I, f);
         }
