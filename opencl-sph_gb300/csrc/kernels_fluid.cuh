@@ -101,7 +101,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         };
         if (staged) {
             const float4 *src = wstage + (b - ub);
-#pragma unroll 2
+#pragma unroll 4
             for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
         } else {
             for (unsigned t = 0; t < len; ++t) visit(xyz(spos[b + t]), t);
