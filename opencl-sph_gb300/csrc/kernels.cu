@@ -24,13 +24,7 @@ cudaError_t sph_prepare_kernels() {
     cudaError_t e = cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
-    if (e != cudaSuccess) return e;
-    // the staged solid first passes
-    size_t swant = solid_stage_smem_bytes(512);
-    if (max_optin > 0 && swant > (size_t)max_optin) swant = (size_t)max_optin;
-    e = cudaFuncSetAttribute(k_rotations_and_strains, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)swant);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(k_deformations, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)swant);
+    return e;
 }
 
 cudaError_t sph_check_launch(const char *what) {
@@ -114,8 +108,7 @@ void sph_launch_init_original_position(const Launch &L) {
 
 void sph_launch_rotations_and_strains(const Launch &L) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_rotations_and_strains<<<g, L.pair_block, solid_stage_smem_bytes(L.pair_block), L.stream>>>(L.scenes,
-                                                                                                  L.pair_particles);
+    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
     if (!L.no_symmetry_planes)
         k_rotations_and_strains_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
@@ -133,7 +126,7 @@ void sph_launch_stresses(const Launch &L, bool corot, bool sorted) {
 
 void sph_launch_deformations(const Launch &L) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_deformations<<<g, L.pair_block, solid_stage_smem_bytes(L.pair_block), L.stream>>>(L.scenes, L.pair_particles);
+    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
     if (!L.no_symmetry_planes) k_deformations_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 

@@ -528,87 +528,47 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 // candidates, so the results are identical; the named force pass (whose
 // masks may be stale) scans.
 
-// A solid particle's stencil row [b, e) through the warp's staged copy:
-// the union of the lanes' ranges of spos and spos0 is copied once into
-// shared memory (coalesced float4 loads) and f(x_j, x0_j, t) is called for
-// each candidate t of this lane's row, in order.  A union wider than the
-// buffer is read from global memory.  Every lane of the warp must call it
-// (inactive lanes with b == e).
-#define SPH_SOLID_STAGE 256
-
-__host__ __device__ constexpr size_t solid_stage_smem_bytes(unsigned block) {
-    return 2 * sizeof(float4) * SPH_SOLID_STAGE * (block / 32);
-}
-
-template <class F>
-__device__ __forceinline__ void solid_row(const SceneDesc &S, unsigned b, unsigned e, unsigned lane, float4 *wp,
-                                          float4 *wq, F &&f) {
-    const unsigned ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
-    const unsigned ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
-    const float4 *__restrict__ spos = S.spos;
-    const float4 *__restrict__ spos0 = S.spos0;
-    if (ub < ue && ue - ub <= SPH_SOLID_STAGE) {
-        __syncwarp();
-        for (unsigned t = lane; t < ue - ub; t += 32) {
-            wp[t] = spos[ub + t];
-            wq[t] = spos0[ub + t];
-        }
-        __syncwarp();
-        const float4 *sp = wp + (b - ub), *sq = wq + (b - ub);
-#pragma unroll 4
-        for (unsigned t = 0; t < e - b; ++t) f(sp[t], sq[t], t);
-    } else {
-        for (unsigned t = 0; t < e - b; ++t) f(spos[b + t], spos0[b + t], t);
-    }
-}
-
 // compute_rotations_and_strains (solid_corotation.cl:28-195) for
 // plane-free scenes: pass 1 sums Apq over candidates with |p| <= h and
 // records the masks, R = polar(Apq) in FP64, pass 2 sums D over the masked
 // candidates with |q| <= h.  Body particles keep their rotation and strain
 // (their masks are still recorded).  Also writes the sorted rotation copy.
 __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    extern __shared__ float4 rsm[];  // solid_stage_smem_bytes(blockDim.x)
-    float4 *wp = rsm + (threadIdx.x >> 5) * (2 * SPH_SOLID_STAGE), *wq = wp + SPH_SOLID_STAGE;
-    const unsigned lane = threadIdx.x & 31u;
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
-    const bool active = item < active_count(S);
-    const unsigned k = item;
-    const unsigned i = active ? min(S.cellparticles[k], S.pnum - 1) : 0u;
-    const SolidConsts C = solid_consts(S);
-    const float4 p4 = active ? S.spos[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 q4 = active ? S.spos0[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float3 ipos = xyz(p4), ipos0 = xyz(q4);
-    const StencilRows rows(S, active ? S.gridcell[i] : 0u);
-    float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    unsigned total = 0;
-    bool overflow = false;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float4 p4 = S.spos[k], q4 = S.spos0[k];
+        const float3 ipos = xyz(p4), ipos0 = xyz(q4);
+        const StencilRows rows(S, S.gridcell[i]);
+        const float4 *__restrict__ spos = S.spos;
+        const float4 *__restrict__ spos0 = S.spos0;
+        float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        unsigned total = 0;
+        bool overflow = false;
 #pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        unsigned b = 0, e = 0;
-        if (active) rows.row(S, r, &b, &e);
-        unsigned long long bits = 0;
-        solid_row(S, b, e, lane, wp, wq, [&](float4 pj, float4 qj, unsigned t) {
-            if (b + t == k) return;
-            const float3 p = sub3(xyz(pj), ipos);
-            const float3 q = sub3(xyz(qj), ipos0);
-            const float r2 = norm2(p);
-            if (r2 <= C.le) {
-                const float d = fmaxf(C.h2 - r2, 0.f);
-                add_outer(p * (d * d * d), q, apq);
+        for (int r = 0; r < 9; ++r) {
+            unsigned b, e;
+            rows.row(S, r, &b, &e);
+            unsigned long long bits = 0;
+            for (unsigned t = 0; t < e - b; ++t) {
+                const unsigned kk = b + t;
+                if (kk == k) continue;
+                const float3 p = sub3(xyz(spos[kk]), ipos);
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
+                const float r2 = norm2(p);
+                if (r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    add_outer(p * (d * d * d), q, apq);
+                }
+                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
             }
-            if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
-        });
-        if (active) {
             store_row_mask(S, k, r, e - b, bits);
             overflow |= e - b > 64;
             total += e - b;
         }
-    }
-    if (active) {
-        const float4 *__restrict__ spos = S.spos;
-        const float4 *__restrict__ spos0 = S.spos0;
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         float R[9];
         if (__float_as_uint(q4.w) > 0) {
@@ -651,50 +611,46 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
 // compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
 // the sorted copies, recording the candidate masks.
 __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    extern __shared__ float4 dsm[];  // solid_stage_smem_bytes(blockDim.x)
-    float4 *wp = dsm + (threadIdx.x >> 5) * (2 * SPH_SOLID_STAGE), *wq = wp + SPH_SOLID_STAGE;
-    const unsigned lane = threadIdx.x & 31u;
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
-    const bool active = item < active_count(S);
-    const unsigned k = item;
-    const unsigned i = active ? min(S.cellparticles[k], S.pnum - 1) : 0u;
-    const SolidConsts C = solid_consts(S);
-    const float3 ipos = active ? xyz(S.spos[k]) : make_float3(0.f, 0.f, 0.f);
-    const float3 ipos0 = active ? xyz(S.spos0[k]) : make_float3(0.f, 0.f, 0.f);
-    const StencilRows rows(S, active ? S.gridcell[i] : 0u);
-    float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    float aqq[6] = {0, 0, 0, 0, 0, 0};
-    unsigned total = 0;
-    bool overflow = false;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float3 ipos = xyz(S.spos[k]), ipos0 = xyz(S.spos0[k]);
+        const StencilRows rows(S, S.gridcell[i]);
+        const float4 *__restrict__ spos = S.spos;
+        const float4 *__restrict__ spos0 = S.spos0;
+        float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        float aqq[6] = {0, 0, 0, 0, 0, 0};
+        unsigned total = 0;
+        bool overflow = false;
 #pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        unsigned b = 0, e = 0;
-        if (active) rows.row(S, r, &b, &e);
-        unsigned long long bits = 0;
-        solid_row(S, b, e, lane, wp, wq, [&](float4 pj, float4 qj, unsigned t) {
-            if (b + t == k) return;
-            const float3 p = sub3(xyz(pj), ipos);
-            const float3 q = sub3(xyz(qj), ipos0);
-            const float r2 = norm2(p);
-            if (r2 <= C.le) {
-                const float d = fmaxf(C.h2 - r2, 0.f);
-                const float w = d * d * d;
-                add_outer(p * w, q, apq);
-                const float3 wq3 = q * w;
-                aqq[0] += wq3.x * q.x; aqq[3] += wq3.x * q.y; aqq[4] += wq3.x * q.z;
-                aqq[1] += wq3.y * q.y; aqq[5] += wq3.y * q.z;
-                aqq[2] += wq3.z * q.z;
+        for (int r = 0; r < 9; ++r) {
+            unsigned b, e;
+            rows.row(S, r, &b, &e);
+            unsigned long long bits = 0;
+            for (unsigned t = 0; t < e - b; ++t) {
+                const unsigned kk = b + t;
+                if (kk == k) continue;
+                const float3 p = sub3(xyz(spos[kk]), ipos);
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
+                const float r2 = norm2(p);
+                if (r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    const float w = d * d * d;
+                    add_outer(p * w, q, apq);
+                    const float3 wq = q * w;
+                    aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
+                    aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
+                    aqq[2] += wq.z * q.z;
+                }
+                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
             }
-            if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
-        });
-        if (active) {
             store_row_mask(S, k, r, e - b, bits);
             overflow |= e - b > 64;
             total += e - b;
         }
-    }
-    if (active) {
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         float inv[6];
         sym_inverse(aqq, inv);
