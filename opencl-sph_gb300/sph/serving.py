@@ -37,6 +37,7 @@ class Request(object):
         self.done = None
         self.remaining = self.steps
         self.result = None
+        self.status = 0        # the scene's status word when it finished
 
     @property
     def work(self):
@@ -135,6 +136,7 @@ class Server(object):
             for sid, r in list(active.items()):
                 r.remaining -= min(chunk, r.remaining)
                 if r.remaining == 0:
+                    r.status = batch.status(sid)
                     if self.keep:
                         v = batch.read(sid)
                         r.result = {"position": np.array(v["position"][: r.scene.n]),
@@ -154,6 +156,7 @@ class Server(object):
             "throughput": work / makespan if makespan > 0 else 0.0,
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else 0.0,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else 0.0,
+            "status_failed": sum(1 for r in requests if r.status),
             "chunks": chunks,
             "substeps": substeps,
             "gpu_busy_s": busy,
