@@ -67,11 +67,26 @@ PHASE_BYTES = {
     "forces_solids": (160, 8),
     "step_forward": (76, 0),
     # batched-form phases (bench_batched): the same figures per material
-    "bins": (44, 20),                 # find/count/insert 44 per particle; zero, scan, copy per cell
-    # (the batched profile reports bins as bin_count, scan and insert)
     "fluid forces+step": (120, 8),
-    "corotational passes": (452, 24), # rotations_and_strains 168 + stresses 48 + forces 160 + step 76
-    "svk passes": (324, 16),          # deformations 64 + stresses 60 + forces 124 + step 76
+    "corotational rotations": (168, 16),
+    "corotational stresses": (48, 0),
+    "corotational forces": (160, 8),
+    "corotational step": (76, 0),
+    "svk deformations": (64, 8),
+    "svk stresses": (60, 0),
+    "svk forces": (124, 8),
+    "svk step": (76, 0),
+}
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+# the dominant phase's kernel, from one ncu capture of the same workload
+# (profiles/fluid_pair_passes_wcsph-1m.md, profiles/solid_pair_passes_batched-256.md).
+MEASURED_TRAFFIC = {
+    ("wcsph-1m", "forces_fluids+step"): 110.94e6,         # k_forces_fluids_masked
+    ("batched-256", "corotational rotations"): 170.85e6,  # k_rotations_and_strains
+    ("batched-256", "corotational forces"): 183.24e6,     # k_forces_solids<1, 1>
+    ("batched-256", "svk deformations"): 56.00e6,         # k_deformations
+    ("batched-256", "svk forces"): 138.18e6,              # k_forces_solids<0, 1>
 }
 
 
@@ -186,16 +201,18 @@ def _solid_setup(ps):
     ps.call_for_all_particles("compute_original_density")
 
 
-def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None):
+def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None, workload=None):
     """Roofline of the phase that takes longest: its algorithmic bytes (for
-    the particles and cells it processes) over its measured time."""
+    the particles and cells it processes) over its measured time; traffic is
+    the measured DRAM bytes of that phase's kernel where captured."""
     dom = max(phases, key=phases.get)
     bp, bc = PHASE_BYTES.get(dom, (0, 0))
     pn, pc = (counts or {}).get(dom, (n, cells))
     alg = bp * pn + bc * pc
     achieved = alg / (phases[dom] * 1e-3) / 1e9
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
-            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": MEASURED_TRAFFIC.get((workload, dom)),
             "algorithmic_bytes_per_launch": alg, "phase_ms": phases}
 
 
@@ -353,8 +370,11 @@ def bench_batched(args, torch, world):
         m = b.scenes[sid].scene.material
         by_mat[m][0] += b.scenes[sid].scene.n
         by_mat[m][1] += c
-    counts = {"fluid forces+step": tuple(by_mat["fluid"]), "corotational passes": tuple(by_mat["corot"]),
-              "svk passes": tuple(by_mat["svk"])}
+    counts = {"fluid forces+step": tuple(by_mat["fluid"])}
+    for ph in ("rotations", "stresses", "forces", "step"):
+        counts["corotational " + ph] = tuple(by_mat["corot"])
+    for ph in ("deformations", "stresses", "forces", "step"):
+        counts["svk " + ph] = tuple(by_mat["svk"])
     b.close()
     return {"scenes": scs, "n": n, "cells": cells, "counts": counts, "total_s": total_s, "clocks": clk,
             "phases": phases, "tuned": tuned,
@@ -606,7 +626,8 @@ def run_ours(args, rank, world, local_rank):
             p1 = bench_plain(args, sc1m, torch, 1)
             extra["plain_1m"] = {"workload": "wcsph-1m: " + d1m, "value": p1["n"] * args.steps / p1["total_s"],
                                  "ms_per_step": p1["total_s"] * 1e3 / args.steps,
-                                 "roofline": _phase_roofline(p1["phases"], p1["n"], p1["cells"], peak, peak_kind),
+                                 "roofline": _phase_roofline(p1["phases"], p1["n"], p1["cells"], peak, peak_kind,
+                                                             workload="wcsph-1m"),
                                  "e2e": p1["e2e"]}
     else:
         scene, desc = workload(args.workload, args.seed + rank)
@@ -648,7 +669,8 @@ def run_ours(args, rank, world, local_rank):
         "clocks": r["clocks"],
         "e2e": r["e2e"],
         "gpu_launches": r["kernels_per_step"] * args.steps,
-        "roofline": _phase_roofline(r["phases"], n, r["cells"], peak, peak_kind, r.get("counts")),
+        "roofline": _phase_roofline(r["phases"], n, r["cells"], peak, peak_kind, r.get("counts"),
+                                    workload=args.workload),
     }
     line.update(extra)
     return line

@@ -451,7 +451,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
     if (!b) return -1;
     if (b->dirty && !rebuild(b)) return -1;
     if (!b->graph) return 0;
-    static const char *kMat[3] = {"fluid forces+step", "corotational passes", "svk passes"};
+    static const char *kMat[3] = {"fluid forces+step", "corotational rotations", "svk deformations"};
     std::vector<double> acc;
     std::vector<const char *> names;
     for (unsigned r = 0; r < reps; ++r) {
@@ -475,10 +475,14 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
             if (m == MAT_FLUID) {
                 sph_launch_forces_fluids(G, true, true);
             } else {
-                if (m == MAT_COROT) sph_launch_rotations_and_strains(G);
+                const bool corot = m == MAT_COROT;
+                if (corot) sph_launch_rotations_and_strains(G);
                 else sph_launch_deformations(G);
-                sph_launch_stresses(G, m == MAT_COROT, true);
-                sph_launch_forces_solids(G, m == MAT_COROT, true);
+                log.mark(corot ? "corotational stresses" : "svk stresses");
+                sph_launch_stresses(G, corot, true);
+                log.mark(corot ? "corotational forces" : "svk forces");
+                sph_launch_forces_solids(G, corot, true);
+                log.mark(corot ? "corotational step" : "svk step");
                 sph_launch_step_forward(G);
             }
         }
