@@ -120,43 +120,55 @@ __device__ __forceinline__ void mul_as(const T a[9], const T s[6], T out[9]) {
         for (int c = 0; c < 3; ++c) out[3 * r + c] = a[3 * r] * S9[c] + a[3 * r + 1] * S9[3 + c] + a[3 * r + 2] * S9[6 + c];
 }
 
+// One step of Newton's polar iteration, X <- (X + X^-T) / 2, with X^-T the
+// cofactor matrix over the determinant; returns max |change|.
+template <typename T>
+__device__ __forceinline__ T newton_polar_step(T X[9]) {
+    const T C[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
+                    X[2] * X[7] - X[1] * X[8], X[0] * X[8] - X[2] * X[6], X[1] * X[6] - X[0] * X[7],
+                    X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
+    const T rd = T(1) / (X[0] * C[0] + X[1] * C[1] + X[2] * C[2]);
+    T delta = 0;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const T nx = T(0.5) * (X[k] + C[k] * rd);
+        delta = fmax(delta, fabs(nx - X[k]));
+        X[k] = nx;
+    }
+    return delta;
+}
+
 // getR (common.cl:306-331): the rotation R of the polar decomposition
 // A = R U, in FP64.  The reference forms R = A (A^T A)^(-1/2) through its
 // 8-rotation Jacobi eigensolver.  Here Newton's polar iteration
-// X <- (X + X^-T) / 2 (Higham, 1986), started from A scaled to the
-// Frobenius norm of a rotation, converges quadratically to the same factor
-// -- to FP64 precision, where the 8 rotations stop at theirs -- with about
-// half the FP64 operations of the Jacobi form (GB300's FP64 pipe is narrow).
-// X^-T is the cofactor matrix over the determinant.  A singular A (NaN in
+// X <- (X + X^-T) / 2 (Higham, 1986) converges quadratically to the same
+// factor -- to FP64 precision, where the 8 rotations stop at theirs.  It
+// starts from A scaled to the Frobenius norm of a rotation and runs in FP32
+// until the FP32 steps stall (about 1e-6), then takes two FP64 steps, which
+// carry an FP32-accurate X to FP64 precision (quadratic convergence): the
+// FP64 pipe, narrow on GB300, does two steps' work.  A singular A (NaN in
 // the reference) gives NaN here as well.
 __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
-    double X[9];
-    double n2 = 0.0;
+    float X[9];
+    float n2 = 0.f;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
-        X[k] = (double)apq[k];
+        X[k] = apq[k];
         n2 += X[k] * X[k];
     }
-    const double g = 1.7320508075688772 * rsqrt(n2);  // sqrt(3) / |A|_F
+    const float g = 1.7320508f * rsqrtf(n2);  // sqrt(3) / |A|_F
 #pragma unroll
     for (int k = 0; k < 9; ++k) X[k] *= g;
 #pragma unroll 1
-    for (int it = 0; it < 16; ++it) {
-        const double C[9] = {X[4] * X[8] - X[5] * X[7], X[5] * X[6] - X[3] * X[8], X[3] * X[7] - X[4] * X[6],
-                             X[2] * X[7] - X[1] * X[8], X[0] * X[8] - X[2] * X[6], X[1] * X[6] - X[0] * X[7],
-                             X[1] * X[5] - X[2] * X[4], X[2] * X[3] - X[0] * X[5], X[0] * X[4] - X[1] * X[3]};
-        const double rd = 1.0 / (X[0] * C[0] + X[1] * C[1] + X[2] * C[2]);
-        double delta = 0.0;
+    for (int it = 0; it < 24; ++it)
+        if (!(newton_polar_step(X) > 1e-6f)) break;  // converged to FP32 (or NaN: stop)
+    double D[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            const double nx = 0.5 * (X[k] + C[k] * rd);
-            delta = fmax(delta, fabs(nx - X[k]));
-            X[k] = nx;
-        }
-        if (!(delta > 1e-15)) break;  // converged (or NaN: stop)
-    }
+    for (int k = 0; k < 9; ++k) D[k] = (double)X[k];
+    newton_polar_step(D);
+    newton_polar_step(D);
 #pragma unroll
-    for (int k = 0; k < 9; ++k) r[k] = (float)X[k];
+    for (int k = 0; k < 9; ++k) r[k] = (float)D[k];
 }
 
 // jacobiInvert (common.cl:296-305) in FP32
@@ -603,7 +615,6 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
             st[4] = 0.5f * (D[2] + D[6]);
             st[5] = 0.5f * (D[5] + D[7]);
         }
-        for (int c = 0; c < 3; ++c) S.srot[3 * (size_t)k + c] = make_float4(R[3 * c], R[3 * c + 1], R[3 * c + 2], 0.f);
     }
     SPH_END_WORK
 }
@@ -701,8 +712,22 @@ __device__ __forceinline__ void svk_stress(const SceneDesc &S, const float f[9],
     o[5] = cau(1, 2);
 }
 
+// The corotational force pass uses a particle's rotation and stress only
+// as the product R sigma -- or, for a body particle, R alone (its pairs use
+// the partner's stress).  N = R sigma (row-major), or R for a body.
+__device__ __forceinline__ void corot_nmat(const float R[9], const float s[6], bool body, float N[9]) {
+    if (body) {
+        for (int c = 0; c < 9; ++c) N[c] = R[c];
+        return;
+    }
+    const float S9[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) N[3 * r + c] = R[3 * r] * S9[c] + R[3 * r + 1] * S9[3 + c] + R[3 * r + 2] * S9[6 + c];
+}
+
 // compute_stresses in a fused substep: per sorted particle k, the field
-// stress[i] and the sorted copy sstress[k].
+// stress[i] and the sorted copies sstress[k] (with mass/density) and, for
+// the corotational model, srot[k] = N (with mass/density in w).
 template <bool COROT>
 __global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
@@ -720,19 +745,29 @@ __global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap
             svk_stress(S, f, o);
         }
         for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)i + c] = o[c];
+        const float mrho = __fdiv_rn(*S.mass, S.sdens[k]);
         S.sstress[2 * (size_t)k] = make_float4(o[0], o[1], o[2], o[3]);
-        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], __fdiv_rn(*S.mass, S.sdens[k]), 0.f);
+        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], mrho, 0.f);
+        if (COROT && S.srot) {
+            float R[9], N[9];
+            for (int c = 0; c < 9; ++c) R[c] = S.rotation[9 * (size_t)i + c];
+            corot_nmat(R, o, S.body_number[i] > 0, N);
+            for (int c = 0; c < 3; ++c)
+                S.srot[3 * (size_t)k + c] = make_float4(N[3 * c], N[3 * c + 1], N[3 * c + 2], c == 0 ? mrho : 0.f);
+        }
     }
     SPH_END_WORK
 }
 
 // One side of a solid pair: position, rest position, velocity, densities,
-// stress and rotation, and whether it belongs to a body.
+// stress, and for the corotational model N (corot_nmat) -- the partner's
+// side of a pair needs N, this particle's side needs sigma and R sigma.
 struct SolidSide {
     float3 pos, pos0, vel;
     float inv_rho0;  // 1 / density0, correctly rounded
     float mrho;      // mass / density, correctly rounded
-    float s[6], R[9];
+    float s[6];      // stress
+    float N[9];      // corotational: R sigma, or R for a body particle
     bool body;
 };
 
@@ -745,50 +780,80 @@ __device__ __forceinline__ void side_from_fields(const SceneDesc &S, unsigned j,
     J.inv_rho0 = __frcp_rn(S.density0[j]);
     J.mrho = __fdiv_rn(mass, S.density[j]);
     for (int c = 0; c < 6; ++c) J.s[c] = S.stress[6 * (size_t)j + c];
-    if (COROT)
-        for (int c = 0; c < 9; ++c) J.R[c] = S.rotation[9 * (size_t)j + c];
     J.body = S.body_number[j] > 0;
+    if (COROT) {
+        float R[9];
+        for (int c = 0; c < 9; ++c) R[c] = S.rotation[9 * (size_t)j + c];
+        corot_nmat(R, J.s, J.body, J.N);
+    }
 }
 
 // The same values from the sorted copies: k_gather put 1/density0 in the
 // velocity copy's w, k_stresses_sorted put mass/density in the second
-// stress float4's z.
+// stress float4's z and N with mass/density in srot.  `need_s`: load the
+// stress too (the corotational partner side does without it).
 template <bool COROT>
-__device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk, SolidSide &J) {
+__device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk, bool need_s, SolidSide &J) {
     const float4 p = S.spos[kk], p0 = S.spos0[kk], v = S.svel[kk];
     J.pos = xyz(p);
     J.pos0 = xyz(p0);
     J.vel = xyz(v);
     J.inv_rho0 = v.w;
-    const float4 s0 = S.sstress[2 * (size_t)kk], s1 = S.sstress[2 * (size_t)kk + 1];
-    J.s[0] = s0.x; J.s[1] = s0.y; J.s[2] = s0.z; J.s[3] = s0.w; J.s[4] = s1.x; J.s[5] = s1.y;
-    J.mrho = s1.z;
+    J.body = __float_as_uint(p0.w) > 0;
+    if (!COROT || need_s) {
+        const float4 s0 = S.sstress[2 * (size_t)kk], s1 = S.sstress[2 * (size_t)kk + 1];
+        J.s[0] = s0.x; J.s[1] = s0.y; J.s[2] = s0.z; J.s[3] = s0.w; J.s[4] = s1.x; J.s[5] = s1.y;
+        J.mrho = s1.z;
+    }
     if (COROT)
         for (int c = 0; c < 3; ++c) {
             const float4 r = S.srot[3 * (size_t)kk + c];
-            J.R[3 * c] = r.x;
-            J.R[3 * c + 1] = r.y;
-            J.R[3 * c + 2] = r.z;
+            J.N[3 * c] = r.x;
+            J.N[3 * c + 1] = r.y;
+            J.N[3 * c + 2] = r.z;
+            if (c == 0) J.mrho = r.w;
         }
-    J.body = __float_as_uint(p0.w) > 0;
 }
 
+__device__ __forceinline__ float3 mat3_vec(const float m[9], float3 v) {
+    return make_float3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+                       m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+
+// Particle i's side of the pair term: its stress, R sigma and (corotational
+// body particles pair with) its stress again.
+struct SolidI {
+    SolidSide side;
+    float M[9];  // R_i sigma_i (corotational)
+};
+
 // The direct pair term of compute_forces_solids (solid_corotation.cl:
-// 215-403, solid_svk.cl:182-367) without symmetry images.  The volume
-// factors come from per-particle reciprocals (m^2 / (rho0_i rho0_j) as
-// m^2 * (1/rho0_i) * (1/rho0_j)) and the Laplacian's distance from rsqrt,
-// so a pair costs no division or square root.
+// 215-403, solid_svk.cl:182-367) without symmetry images, gathered per
+// partner type:
+//   f_ji = -v sigma_i gW,  f_ij = -f_ji for a body partner, else v sigma_j gW
+//   (v = m^2 / (rho0_i rho0_j), gW = spiky gradient at x0_i - x0_j);
+//   corotational fe = R_j f_ij - R_i f_ji = v (M_i + M_j) gW, or
+//   v (R_j sigma_i gW + M_i gW) for a body partner (M = R sigma);
+//   SVK fe = f_ij - f_ji = v (sigma_i + sigma_j) gW, or 2 v sigma_i gW.
+// The volume factor comes from per-particle reciprocals and the Laplacian's
+// distance from rsqrt, so a pair costs no division or square root.
 template <bool COROT>
-__device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidSide &I, const SolidSide &J,
+__device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidI &II, const SolidSide &J,
                                            Kahan3 &fe_s, Kahan3 &fv_s) {
+    const SolidSide &I = II.side;
     const float3 x = sub3(I.pos0, J.pos0);
     const float r2 = norm2(sub3(J.pos, I.pos));
     if (!(norm2(x) <= C.le || r2 <= C.le)) return;
     const float vivj = __fmul_rn(__fmul_rn(__fmul_rn(C.mass, C.mass), I.inv_rho0), J.inv_rho0);
     const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
-    const float3 f_ji = sym_vec(I.s, gx) * (-vivj);
-    const float3 f_ij = J.body ? -f_ji : sym_vec(J.s, -gx) * (-vivj);
-    const float3 fe = COROT ? mat_vec(J.R, f_ij) - mat_vec(I.R, f_ji) : f_ij - f_ji;
+    float3 fe;
+    if (COROT) {
+        const float3 mi = mat3_vec(II.M, gx);
+        fe = J.body ? (mat3_vec(J.N, sym_vec(I.s, gx)) + mi) * vivj : (mat3_vec(J.N, gx) + mi) * vivj;
+    } else {
+        const float3 si = sym_vec(I.s, gx);
+        fe = J.body ? si * (2.f * vivj) : (sym_vec(J.s, gx) + si) * vivj;
+    }
     const float dist = r2 > 0.f ? __fmul_rn(r2, rsqrtf(r2)) : 0.f;
     const float lap = r2 <= C.le ? C.kv * (C.h - dist) : 0.f;
     const float3 fv = (J.vel - I.vel) * (J.mrho * lap);
@@ -808,14 +873,19 @@ __global__ void k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap m
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
         const SolidConsts C = solid_consts(S);
-        SolidSide I;
-        if (MASKED) side_from_sorted<COROT>(S, k, I);
-        else side_from_fields<COROT>(S, i, xyz(S.spos[k]), C.mass, I);
+        SolidI I;
+        if (MASKED) side_from_sorted<COROT>(S, k, true, I.side);
+        else side_from_fields<COROT>(S, i, xyz(S.spos[k]), C.mass, I.side);
+        if (COROT) {
+            float R[9];
+            for (int c = 0; c < 9; ++c) R[c] = S.rotation[9 * (size_t)i + c];
+            corot_nmat(R, I.side.s, false, I.M);
+        }
         Kahan3 fe_s, fv_s;
         auto visit = [&](unsigned kk) {
             if (kk == k) return;
             SolidSide J;
-            if (MASKED) side_from_sorted<COROT>(S, kk, J);
+            if (MASKED) side_from_sorted<COROT>(S, kk, false, J);
             else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), C.mass, J);
             solid_pair<COROT>(C, I, J, fe_s, fv_s);
         };
