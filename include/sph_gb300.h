@@ -266,6 +266,10 @@ unsigned int sph_batch_steps_left(sph_batch *batch, int id);
 int sph_batch_read(sph_batch *batch, int id, psdata *out);
 /* Copies one named field of a scene into the same field of `out`. */
 int sph_batch_read_field(sph_batch *batch, int id, const char *field, psdata *out);
+/* The same copy enqueued on the batch's stream without waiting: `out` is
+ * current after sph_batch_synchronize (and asynchronous only when its
+ * blob is pinned, e.g. by cudaHostRegister). */
+int sph_batch_read_field_async(sph_batch *batch, int id, const char *field, psdata *out);
 /* Runs `reps` substeps of the batch as individual launches with CUDA events
  * between phases (material branches one after another) and writes each
  * phase's mean device time in ms and its name; returns the phase count. */

@@ -415,20 +415,26 @@ extern "C" int sph_batch_read(sph_batch *b, int id, psdata *out) {
     return 0;
 }
 
-extern "C" int sph_batch_read_field(sph_batch *b, int id, const char *field, psdata *out) {
-    BatchScene *sc = scene_of(b, id, "sph_batch_read_field");
+static int read_field(sph_batch *b, int id, const char *field, psdata *out, bool wait, const char *what) {
+    BatchScene *sc = scene_of(b, id, what);
     if (!sc) return -1;
     int f = out && field ? get_field_psdata(*out, field) : -1;
     if (f < 0 || psdata_data_size(*out) != sc->blob_size) {
-        sph_set_error("sph_batch_read_field: no field '%s' in a store of the scene's layout", field ? field : "");
+        sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field ? field : "");
         return -1;
     }
     size_t off = out->data_offsets[f], sz = out->data_sizes[f];
-    if (!ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost, b->stream),
-            "sph_batch_read_field") ||
-        !ok(cudaStreamSynchronize(b->stream), "sph_batch_read_field"))
+    if (!ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost, b->stream), what))
         return -1;
-    return 0;
+    return !wait || ok(cudaStreamSynchronize(b->stream), what) ? 0 : -1;
+}
+
+extern "C" int sph_batch_read_field(sph_batch *b, int id, const char *field, psdata *out) {
+    return read_field(b, id, field, out, true, "sph_batch_read_field");
+}
+
+extern "C" int sph_batch_read_field_async(sph_batch *b, int id, const char *field, psdata *out) {
+    return read_field(b, id, field, out, false, "sph_batch_read_field_async");
 }
 
 namespace {

@@ -565,6 +565,7 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
             unsigned b, e;
             rows.row(S, r, &b, &e);
             unsigned long long bits = 0;
+#pragma unroll 4
             for (unsigned t = 0; t < e - b; ++t) {
                 const unsigned kk = b + t;
                 if (kk == k) continue;
@@ -641,6 +642,7 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
             unsigned b, e;
             rows.row(S, r, &b, &e);
             unsigned long long bits = 0;
+#pragma unroll 4
             for (unsigned t = 0; t < e - b; ++t) {
                 const unsigned kk = b + t;
                 if (kk == k) continue;

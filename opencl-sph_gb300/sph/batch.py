@@ -37,7 +37,12 @@ class Batch(object):
         ps = init_data_cpu(scene.spec)
         v = bnd.store_views(ps)
         for k, val in scene.init.items():
-            v[k][...] = val
+            arr = np.asarray(val)
+            if arr.size > 1:
+                # fewer rows than the store's capacity fill its leading part
+                v[k][tuple(slice(None, d) for d in arr.shape)] = arr
+            else:
+                v[k][...] = arr
         return ps
 
     @staticmethod
@@ -96,6 +101,16 @@ class Batch(object):
         if bnd.sph_batch_read_field(self.handle, sid, name, ctypes.byref(s.psdata)) != 0:
             raise bnd.SphError(bnd.last_error())
         return s.views[name]
+
+    def read_fields(self, sids, name):
+        """Copies one field of several scenes back with a single wait; returns
+        their host views (sid -> array)."""
+        for sid in sids:
+            s = self.scenes[sid]
+            if bnd.sph_batch_read_field_async(self.handle, sid, name, ctypes.byref(s.psdata)) != 0:
+                raise bnd.SphError(bnd.last_error())
+        self.synchronize()
+        return {sid: self.scenes[sid].views[name] for sid in sids}
 
     def profile(self, reps=3):
         """Mean device ms per phase of a substep (phases run one by one)."""

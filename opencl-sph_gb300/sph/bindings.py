@@ -213,6 +213,7 @@ _SIGS = {
     "sph_batch_read": ([c_void_p, c_int, POINTER(psdata)], c_int),
     "sph_batch_synchronize": ([c_void_p], c_int),
     "sph_batch_read_field": ([c_void_p, c_int, String, POINTER(psdata)], c_int),
+    "sph_batch_read_field_async": ([c_void_p, c_int, String, POINTER(psdata)], c_int),
     "sph_batch_profile": ([c_void_p, c_uint, POINTER(c_float), POINTER(c_char_p), c_uint], c_int),
     "sph_batch_bytes": ([c_void_p], c_size_t),
     "sph_batch_size": ([c_void_p], c_uint),

@@ -159,3 +159,52 @@ def test_step_quota_idles_scene():
     v = b.read(ids[0])
     assert np.array_equal(v["position"][: scs[0].n], pos) and np.array_equal(v["velocity"][: scs[0].n], vel)
     b.close()
+
+
+def test_read_fields_async_equals_read():
+    scs = mix(seed=50)
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    b.step(4)
+    want = {sid: np.array(b.read(sid)["position"]) for sid in ids}
+    b.step(3)
+    got = b.read_fields(ids, "velocity")
+    for sid in ids:
+        assert np.array_equal(got[sid], b.read(sid)["velocity"])
+    got = b.read_fields(ids, "position")
+    for sid, s in zip(ids, scs):
+        assert not np.array_equal(got[sid][: s.n], want[sid][: s.n])  # it moved on
+        assert np.array_equal(got[sid], b.read(sid)["position"])
+    b.close()
+
+
+def test_ragged_and_empty_scenes_in_a_batch():
+    """Scenes with fewer active particles than their capacity, and with none,
+    run beside full ones: the ragged scene equals itself alone, the empty
+    one is left as it was."""
+    full = scenes.wcsph_block(8, 6, 8, seed=61, name="full")
+    ragged = scenes.wcsph_block(9, 6, 9, seed=62, name="ragged", pnum=600)
+    ragged.init = dict(ragged.init, n=400)
+    empty = scenes.wcsph_block(6, 6, 6, seed=63, name="empty")
+    empty.init = dict(empty.init, n=0)
+    b = Batch()
+    ids = [b.add(s) for s in (full, ragged, empty)]
+    b.step(10)
+    pos, _ = alone(ragged, 10)
+    assert np.array_equal(b.read(ids[1])["position"][:400], pos[:400])
+    e = b.read(ids[2])["position"]
+    assert np.array_equal(e[: empty.n], np.asarray(empty.init["position"], np.float32).reshape(e[: empty.n].shape))
+    assert all(b.status(i) == 0 for i in ids)
+    b.close()
+
+
+def test_empty_store_fused_substeps():
+    sc = scenes.wcsph_block(6, 6, 6, seed=64)
+    sc.init = dict(sc.init, n=0)
+    ps = sc.system()
+    ps.update_fused(5)
+    ps.sync_device_to_host()
+    assert ps.status() == 0
+    assert np.array_equal(ps.get_fields("position")[0][: sc.n],
+                          np.asarray(sc.init["position"], np.float32).reshape(-1, 3))
+    ps.close()
