@@ -202,7 +202,7 @@ bool rebuild(sph_batch *b) {
     if (!ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture")) return false;
     sph_launch_bins(A);
     sph_launch_gather(A, true, false, true);
-    sph_launch_density(A, false, true);  // masks for the fluid scenes only
+    sph_launch_density(A, false, true, true);  // masks for the fluid scenes only
     cudaEventRecord(b->fork, b->stream);
     for (int m = 0; m < 3; ++m) {
         GroupLaunch &G = b->group[m];
@@ -211,8 +211,8 @@ bool rebuild(sph_batch *b) {
         if (m == MAT_FLUID) {
             sph_launch_forces_fluids(G.L, true, true);
         } else {
-            if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L);
-            else sph_launch_deformations(G.L);
+            if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L, true);
+            else sph_launch_deformations(G.L, true);
             sph_launch_stresses(G.L, m == MAT_COROT, true);
             sph_launch_forces_solids(G.L, m == MAT_COROT, true);
             sph_launch_step_forward(G.L);
@@ -472,7 +472,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
         log.mark("gather");
         sph_launch_gather(A, true, false, true);
         log.mark("density");
-        sph_launch_density(A, false, true);
+        sph_launch_density(A, false, true, true);
         for (int m = 0; m < 3; ++m) {
             if (!b->group[m].present) continue;
             Launch G = b->group[m].L;
@@ -482,8 +482,8 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
                 sph_launch_forces_fluids(G, true, true);
             } else {
                 const bool corot = m == MAT_COROT;
-                if (corot) sph_launch_rotations_and_strains(G);
-                else sph_launch_deformations(G);
+                if (corot) sph_launch_rotations_and_strains(G, true);
+                else sph_launch_deformations(G, true);
                 log.mark(corot ? "corotational stresses" : "svk stresses");
                 sph_launch_stresses(G, corot, true);
                 log.mark(corot ? "corotational forces" : "svk forces");

@@ -76,13 +76,14 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid) {
                                                                           dens ? 1 : 0, solid ? 1 : 0);
 }
 
-void sph_launch_density(const Launch &L, bool original, bool mask) {
+void sph_launch_density(const Launch &L, bool original, bool mask, bool skip_solids) {
     const size_t smem = density_smem_bytes(L.pair_block);
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_density<false><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0);
+    k_density<false><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0,
+                                                          skip_solids ? 1 : 0);
     if (!L.no_symmetry_planes)
         k_density<true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0,
-                                                             mask ? 1 : 0);
+                                                             mask ? 1 : 0, 0);
 }
 
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
@@ -106,9 +107,9 @@ void sph_launch_init_original_position(const Launch &L) {
     k_init_original_position<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
 }
 
-void sph_launch_rotations_and_strains(const Launch &L) {
+void sph_launch_rotations_and_strains(const Launch &L, bool with_density) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0);
     if (!L.no_symmetry_planes)
         k_rotations_and_strains_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
@@ -124,9 +125,9 @@ void sph_launch_stresses(const Launch &L, bool corot, bool sorted) {
     }
 }
 
-void sph_launch_deformations(const Launch &L) {
+void sph_launch_deformations(const Launch &L, bool with_density) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0);
     if (!L.no_symmetry_planes) k_deformations_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 
@@ -191,8 +192,11 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     sph_launch_insert(L);
     phase("gather");
     sph_launch_gather(L, mat == MAT_FLUID, false, mat != MAT_FLUID);
-    phase("density");
-    sph_launch_density(L, false, mat == MAT_FLUID);
+    if (mat == MAT_FLUID || !L.no_symmetry_planes) {
+        // a plane-free solid's density is summed by its first solid pass
+        phase("density");
+        sph_launch_density(L, false, mat == MAT_FLUID, mat != MAT_FLUID);
+    }
     if (mat == MAT_FLUID) {
         phase("forces_fluids+step");
         sph_launch_forces_fluids(L, true, true);
@@ -205,10 +209,10 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     }
     if (mat == MAT_COROT) {
         phase("rotations_and_strains");
-        sph_launch_rotations_and_strains(L);
+        sph_launch_rotations_and_strains(L, true);
     } else {
         phase("deformations");
-        sph_launch_deformations(L);
+        sph_launch_deformations(L, true);
     }
     phase("stresses");
     sph_launch_stresses(L, mat == MAT_COROT, true);

@@ -9,6 +9,15 @@
 #include "sph_internal.h"
 
 #define SPH_FULL_MASK 0xffffffffu
+#define SPH_PI_F 3.1415926535f
+
+// rho = m * sum * 315 / (64 pi h^9): the poly6 normalisation applied once
+// to a particle's sum of (h^2 - r^2)^3 (common.cl:78-80, 610-690).
+__device__ __forceinline__ float poly6_density(float sum, float h2, float h, float mass) {
+    const float h3 = h2 * h;
+    const float coef = 315.0f / (64.0f * SPH_PI_F * h3 * h3 * h3);
+    return sum * coef * mass;
+}
 
 // A batched scene whose substep quota is used up: every kernel leaves it
 // (fields, grid tables and scratch) untouched.

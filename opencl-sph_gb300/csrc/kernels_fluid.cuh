@@ -10,7 +10,6 @@
 #include "kernels_common.cuh"
 #include "kernels_rigid.cuh"
 
-#define SPH_PI_F 3.1415926535f
 
 // compute_density (common.cl:610-690) and compute_original_density
 // (solids.cl:99-170): rho_i = m * sum_j W_poly6(|x_j - x_i|), j = i
@@ -113,10 +112,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         }
     }
     if (active) {
-        // poly6 normalisation 315 / (64 pi h^9), applied once
-        const float h3 = h2 * h;
-        const float coef = 315.0f / (64.0f * SPH_PI_F * h3 * h3 * h3);
-        const float value = rho.s * coef * (*S.mass);
+        const float value = poly6_density(rho.s, h2, h, *S.mass);
         if (original) {
             S.density0[i] = value;
         } else {
@@ -137,12 +133,14 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
 // plane-free loop free of its registers.
 template <bool PLANES>
 __global__ void __launch_bounds__(512, 2)
-    k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask) {
+    k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask, int skip_solids) {
     extern __shared__ float4 sm_stage[];
     float4 *wstage = sm_stage + (threadIdx.x >> 5) * SPH_STAGE;
     const unsigned lane = threadIdx.x & 31u;
     SPH_FOR_WORK(map)
     if ((S.num_symmetry_planes != 0) != PLANES) continue;
+    // in a fused substep a plane-free solid's first solid pass sums its density
+    if (skip_solids && !PLANES && (S.programs & (PROG_COROT | PROG_SVK))) continue;
     const unsigned n = active_count(S);
     if (want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original)
         density_one<PLANES, true>(S, n, item, lane, wstage, original);

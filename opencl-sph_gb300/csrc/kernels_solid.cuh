@@ -19,9 +19,6 @@
 
 #include "kernels_common.cuh"
 
-#ifndef SPH_PI_F
-#define SPH_PI_F 3.1415926535f
-#endif
 
 // One Givens rotation of the symmetric 6-vector s ([xx,yy,zz,xy,xz,yz])
 // zeroing the off-diagonal `off` (3, 4 or 5), applied in place to s and to
@@ -545,7 +542,7 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 // records the masks, R = polar(Apq) in FP64, pass 2 sums D over the masked
 // candidates with |q| <= h.  Body particles keep their rotation and strain
 // (their masks are still recorded).  Also writes the sorted rotation copy.
-__global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
     if (item < active_count(S)) {
@@ -558,8 +555,9 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
         const float4 *__restrict__ spos = S.spos;
         const float4 *__restrict__ spos0 = S.spos0;
         float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        unsigned total = 0;
+        unsigned total = 0, count = 0;
         bool overflow = false;
+        Kahan rho;
 #pragma unroll 1
         for (int r = 0; r < 9; ++r) {
             unsigned b, e;
@@ -568,10 +566,16 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
 #pragma unroll 4
             for (unsigned t = 0; t < e - b; ++t) {
                 const unsigned kk = b + t;
-                if (kk == k) continue;
                 const float3 p = sub3(xyz(spos[kk]), ipos);
-                const float3 q = sub3(xyz(spos0[kk]), ipos0);
                 const float r2 = norm2(p);
+                // the density pass's sum, in its order (j = i included)
+                if (with_density && r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    rho.add(d * d * d);
+                    count += r2 <= C.lt;
+                }
+                if (kk == k) continue;
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
                 if (r2 <= C.le) {
                     const float d = fmaxf(C.h2 - r2, 0.f);
                     add_outer(p * (d * d * d), q, apq);
@@ -583,6 +587,12 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
             total += e - b;
         }
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        if (with_density) {
+            const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
+            S.density[i] = value;
+            S.num_neighbours[i] = count;
+            S.sdens[k] = value;
+        }
         float R[9];
         if (__float_as_uint(q4.w) > 0) {
             // a body particle: rotation and strain stay as they are
@@ -622,7 +632,7 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
 
 // compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
 // the sorted copies, recording the candidate masks.
-__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
     if (item < active_count(S)) {
@@ -635,8 +645,9 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
         const float4 *__restrict__ spos0 = S.spos0;
         float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         float aqq[6] = {0, 0, 0, 0, 0, 0};
-        unsigned total = 0;
+        unsigned total = 0, count = 0;
         bool overflow = false;
+        Kahan rho;
 #pragma unroll 1
         for (int r = 0; r < 9; ++r) {
             unsigned b, e;
@@ -645,10 +656,16 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
 #pragma unroll 4
             for (unsigned t = 0; t < e - b; ++t) {
                 const unsigned kk = b + t;
-                if (kk == k) continue;
                 const float3 p = sub3(xyz(spos[kk]), ipos);
-                const float3 q = sub3(xyz(spos0[kk]), ipos0);
                 const float r2 = norm2(p);
+                // the density pass's sum, in its order (j = i included)
+                if (with_density && r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    rho.add(d * d * d);
+                    count += r2 <= C.lt;
+                }
+                if (kk == k) continue;
+                const float3 q = sub3(xyz(spos0[kk]), ipos0);
                 if (r2 <= C.le) {
                     const float d = fmaxf(C.h2 - r2, 0.f);
                     const float w = d * d * d;
@@ -665,6 +682,12 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
             total += e - b;
         }
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        if (with_density) {
+            const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
+            S.density[i] = value;
+            S.num_neighbours[i] = count;
+            S.sdens[k] = value;
+        }
         float inv[6];
         sym_inverse(aqq, inv);
         float F[9];

@@ -46,15 +46,18 @@ void sph_launch_bins(const Launch &L);
 // Cell-sorted copies (positions; velocities and densities on request).
 void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid = false);
 
-void sph_launch_density(const Launch &L, bool original, bool mask = false);
+// skip_solids: a fused substep, where a plane-free solid's first solid pass
+// sums its density
+void sph_launch_density(const Launch &L, bool original, bool mask = false, bool skip_solids = false);
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked = false);
 void sph_launch_step_forward(const Launch &L);
 void sph_launch_plane_constraints(const Launch &L);
 void sph_launch_init_original_position(const Launch &L);
-void sph_launch_rotations_and_strains(const Launch &L);
+// with_density: also the density pass's sums (fused substeps)
+void sph_launch_rotations_and_strains(const Launch &L, bool with_density = false);
 // sorted: a fused substep's stress pass, which also fills the sorted copy
 void sph_launch_stresses(const Launch &L, bool corot, bool sorted = false);
-void sph_launch_deformations(const Launch &L);
+void sph_launch_deformations(const Launch &L, bool with_density = false);
 // masked: a fused substep's force pass over the first pair pass's masks
 void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false);
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
