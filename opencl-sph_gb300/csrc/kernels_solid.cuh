@@ -141,10 +141,12 @@ __device__ __forceinline__ T newton_polar_step(T X[9]) {
 // X <- (X + X^-T) / 2 (Higham, 1986) converges quadratically to the same
 // factor -- to FP64 precision, where the 8 rotations stop at theirs.  It
 // starts from A scaled to the Frobenius norm of a rotation and runs in FP32
-// until the FP32 steps stall (about 1e-6), then takes two FP64 steps, which
-// carry an FP32-accurate X to FP64 precision (quadratic convergence): the
-// FP64 pipe, narrow on GB300, does two steps' work.  A singular A (NaN in
-// the reference) gives NaN here as well.
+// until the FP32 steps stall (about 1e-6), then takes one FP64 step, which
+// carries the FP32-accurate X (error ~1e-7) to ~1e-14 (quadratic
+// convergence) -- far below the float rounding of the stored R, which is
+// thus the FP64 polar factor rounded to float.  The FP64 pipe, narrow on
+// GB300, does one step's work.  A singular A (NaN in the reference) gives
+// NaN here as well.
 __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
     float X[9];
     float n2 = 0.f;
@@ -162,7 +164,6 @@ __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
     double D[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) D[k] = (double)X[k];
-    newton_polar_step(D);
     newton_polar_step(D);
 #pragma unroll
     for (int k = 0; k < 9; ++k) r[k] = (float)D[k];
