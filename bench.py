@@ -541,6 +541,34 @@ def fp64_error_sample(scs, steps):
     return {"substeps": steps, "per_material": out}
 
 
+def fp64_error_configs():
+    """The plain drop-in (FP32, fused CUDA-graph substeps) against the
+    all-FP64 oracle run of the same scene, on the two configurations the
+    accuracy target is stated for: the 8,000-particle dam break after 1,000
+    substeps and the 4,000-particle corotational beam after 2,000."""
+    from sph import bindings as bnd
+    from sph import free_data_cpu
+    from oracle.oracle import OracleScene
+    out = {}
+    for name, steps in (("dam-8k", 1000), ("beam-4k", 2000)):
+        sc, _ = workload(name, 0)
+        ps = sc.system()
+        o = OracleScene(bnd.store_views(ps.psdata), "f64", nthreads=os.cpu_count() or 1)
+        if sc.material != "fluid":
+            _solid_setup(ps)
+            o.setup_solid()
+        ps.update_fused(steps)
+        o.run(sc.material, steps)
+        ps.sync_device_to_host()
+        p = np.asarray(ps.get_fields("position")[0][: sc.n], dtype=np.float64)
+        q = o.a["position"][: sc.n]
+        out[name] = {"substeps": steps, "particles": sc.n,
+                     "rel_l2": float(np.linalg.norm(p - q) / np.linalg.norm(q)),
+                     "max_abs_m": float(np.max(np.abs(p - q)))}
+        ps.close()
+    return out
+
+
 def cpu_sample(scene, material, steps, nthreads, reference):
     """Times the CPU oracle (or the reference's own kernels) on `steps`
     substeps of the scene; returns particle-steps/s."""
@@ -642,6 +670,7 @@ def run_ours(args, rank, world, local_rank):
             extra["batched_vs_plain"] = batched / pl["graph"]
             extra["batched_vs_plain_synced"] = batched / pl["synced"]
             extra["fp64_error"] = fp64_error_sample(r["scenes"], 100)
+            extra["fp64_error_configs"] = fp64_error_configs()
             extra["served"] = bench_served(args)
             sc1m, d1m = workload("wcsph-1m", args.seed)
             p1 = bench_plain(args, sc1m, torch, 1)
