@@ -142,37 +142,43 @@ def ball(radius, spacing, center):
 
 def rigid_body_scene(radius=0.05, spacing=0.01, h=0.02, center=(0.2, 0.2, 0.2), velocity=(0.0, 0.0, 0.0),
                      omega=(0.0, 0.0, 0.0), fluid=None, box=(0.0, 0.4), gravity=(0.0, -9.8, 0.0), dt=1e-4,
-                     restdens=1000.0, stiffness=3.0, viscosity=0.2, jitter=1e-4, seed=0, walls=True, name=None):
-    """A rigid ball (body 1, body_dynamic = 2: the rigid-body extension) of
-    lattice particles, optionally in a WCSPH fluid block `fluid` = (nx, ny,
-    nz) filling the low corner of the box.  The ball starts with linear
-    velocity `velocity` and angular velocity `omega` about its centre.  The
-    ball's particles come after the fluid's; they carry the store's particle
-    mass, so the ball is as dense as the fluid."""
+                     restdens=1000.0, stiffness=3.0, viscosity=0.2, jitter=1e-4, seed=0, walls=True, name=None,
+                     balls=None):
+    """Rigid balls (body_dynamic = 2: the rigid-body extension) of lattice
+    particles, optionally in a WCSPH fluid block `fluid` = (nx, ny, nz)
+    filling the low corner of the box.  One ball of `radius` at `center`
+    with linear velocity `velocity` and angular velocity `omega` about its
+    centre, or several: `balls` = [(radius, center, velocity, omega), ...],
+    body 1, 2, ... in that order.  The balls' particles come after the
+    fluid's; they carry the store's particle mass, so a ball is as dense as
+    the fluid."""
     rng = np.random.default_rng(seed)
-    parts, body = [], []
+    parts, body, vels = [], [], []
     if fluid is not None:
         f = lattice(*fluid, spacing, origin=(box[0] + spacing / 2,) * 3, jitter=jitter, rng=rng)
         parts.append(f)
         body.append(np.zeros(len(f), np.uint32))
-    b = ball(radius, spacing, center)
-    parts.append(b)
-    body.append(np.ones(len(b), np.uint32))
+        vels.append(np.zeros((len(f), 3)))
+    for k, (rad, cen, v0, w0) in enumerate(balls or [(radius, center, velocity, omega)]):
+        b = ball(rad, spacing, cen)
+        parts.append(b)
+        body.append(np.full(len(b), k + 1, np.uint32))
+        r = b.astype(np.float64) - np.asarray(cen, dtype=np.float64)
+        vels.append(np.asarray(v0, dtype=np.float64) + np.cross(np.asarray(w0, dtype=np.float64), r))
+    nb = len(balls or [0])
     pos = np.concatenate(parts).astype(np.float32)
     bn = np.concatenate(body)
+    vel = np.concatenate(vels).astype(np.float32)
     n = len(pos)
-    vel = np.zeros((n, 3), np.float32)
-    r = b.astype(np.float64) - np.asarray(center, dtype=np.float64)
-    vel[bn == 1] = (np.asarray(velocity, dtype=np.float64) + np.cross(np.asarray(omega, dtype=np.float64), r))
     mass = restdens * spacing ** 3
     gb = [box[0], box[1]] * 3
-    entries = _common_entries(n, mass, dt, h, gravity, gb)
+    entries = _common_entries(n, mass, dt, h, gravity, gb, body_count=nb)
     entries += [("restdens", "1", "float", restdens), ("stiffness", "1", "float", stiffness),
                 ("viscosity", "1", "float", viscosity), ("body_position", "3, body_count", "float", None)]
     if walls:
         entries.append(("wallbounds", "6", "float", gb))
     init = {"position": pos, "n": n, "velocity": vel, "body_number": bn,
-            "body_dynamic": np.array([2], np.uint32)}
+            "body_dynamic": np.full(nb, 2, np.uint32)}
     return Scene(name or "rigid-%d" % n, "fluid", FLUID_KERNELS, entries, init, n)
 
 

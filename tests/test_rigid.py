@@ -157,3 +157,48 @@ def test_gpu_rigid_scene_in_batch_equals_alone():
         assert np.array_equal(v["position"][: sc.n], want["position"]), sc.name
         assert np.array_equal(v["velocity"][: sc.n], want["velocity"]), sc.name
     b.close()
+
+
+def three_balls(**kw):
+    args = dict(spacing=0.01, gravity=(0.0, 0.0, 0.0), viscosity=0.0, jitter=0.0,
+                balls=[(0.025, (0.1, 0.2, 0.2), (0.2, 0.0, 0.0), (0.0, 0.0, 2.0)),
+                       (0.035, (0.3, 0.2, 0.2), (0.0, 0.1, 0.0), (1.0, 0.0, 0.0)),
+                       (0.03, (0.2, 0.3, 0.1), (0.0, 0.0, -0.1), (0.0, 3.0, 0.0))])
+    args.update(kw)
+    return scenes.rigid_body_scene(**args)
+
+
+def test_oracle_several_bodies_move_independently():
+    sc = three_balls()
+    o = _oracle(sc)
+    bn = np.asarray(sc.init["body_number"])
+    d0 = [_pair_dists(o.a["position"][bn == b]) for b in (1, 2, 3)]
+    P0 = [_momenta(o, bn == b)[0] for b in (1, 2, 3)]
+    o.run("fluid", 100)
+    for b in (1, 2, 3):
+        P1, _, _ = _momenta(o, bn == b)
+        assert np.linalg.norm(P1 - P0[b - 1]) <= 1e-9 * np.linalg.norm(P0[b - 1])
+        assert np.max(np.abs(_pair_dists(o.a["position"][bn == b]) - d0[b - 1])) <= 1e-12
+    assert np.all(o.rigid_state[:, 0] == 2.0)
+
+
+@pytest.mark.gpu
+def test_gpu_several_bodies_match_oracle():
+    """Three balls dropping onto a fluid block (surface at y = 0.065) within
+    the smoothing length: each body's reduction is its own."""
+    sc = three_balls(fluid=(12, 6, 12), gravity=(0.0, -9.8, 0.0), viscosity=0.2, jitter=1e-4,
+                     balls=[(0.02, (0.03, 0.09, 0.03), (0.0, -0.5, 0.0), (0.0, 0.0, 2.0)),
+                            (0.025, (0.09, 0.095, 0.04), (0.0, -0.3, 0.1), (1.0, 0.0, 0.0)),
+                            (0.02, (0.06, 0.09, 0.1), (0.1, -0.4, 0.0), (0.0, 3.0, 0.0))])
+    steps = 40
+    g = _gpu_run(sc, steps)
+    o = _oracle(sc, "f32")
+    o.run("fluid", steps)
+    assert rel_err(g["position"], o.a["position"][: sc.n]) < 1e-5
+    assert rel_err(g["velocity"], o.a["velocity"][: sc.n]) < 1e-3
+    bn = np.asarray(sc.init["body_number"])
+    x0 = np.asarray(sc.init["position"])
+    for b in (1, 2, 3):
+        d0 = _pair_dists(x0[bn == b])
+        assert np.max(np.abs(_pair_dists(g["position"][bn == b]) - d0)) <= 2e-6
+    assert np.max(np.abs(g["position"][bn == 0] - x0[bn == 0])) > 1e-5  # the fluid felt them
