@@ -1,5 +1,5 @@
 // kernels_solid.cuh -- elastic solids on sm_103a: the corotational linear
-// model (kernels/solid_corotation.cl) with its polar decomposition in FP64,
+// model (kernels/solid_corotation.cl) with its polar decomposition,
 // the St. Venant-Kirchhoff model (kernels/solid_svk.cl), the shared solid
 // force pass, kinematic bodies (kernels/rigidbody.cl) and the scene-init
 // kernels of common.cl.
@@ -14,7 +14,7 @@
 // (|b - c| + sqrt((b - c)^2 + 4a^2)), cos = rsqrt(1 + t^2), sin = t cos,
 // instead of atan/cos/sin.  A zero pivot gives the identity (the reference
 // evaluates atan(0/0) = NaN when b == c there).  The corotational rotation
-// itself is the FP64 polar factor (polar_rotation_fp64).
+// itself is the polar factor from Newton's iteration (polar_rotation_fp64).
 #pragma once
 
 #include "kernels_common.cuh"
@@ -136,17 +136,19 @@ __device__ __forceinline__ T newton_polar_step(T X[9]) {
 }
 
 // getR (common.cl:306-331): the rotation R of the polar decomposition
-// A = R U, in FP64.  The reference forms R = A (A^T A)^(-1/2) through its
-// 8-rotation Jacobi eigensolver.  Here Newton's polar iteration
+// A = R U.  The reference forms R = A (A^T A)^(-1/2) through its 8-rotation
+// Jacobi eigensolver in FP64.  Here Newton's polar iteration
 // X <- (X + X^-T) / 2 (Higham, 1986) converges quadratically to the same
-// factor -- to FP64 precision, where the 8 rotations stop at theirs.  It
-// starts from A scaled to the Frobenius norm of a rotation and runs in FP32
-// until the FP32 steps stall (about 1e-6), then takes one FP64 step, which
-// carries the FP32-accurate X (error ~1e-7) to ~1e-14 (quadratic
-// convergence) -- far below the float rounding of the stored R, which is
-// thus the FP64 polar factor rounded to float.  The FP64 pipe, narrow on
-// GB300, does one step's work.  A singular A (NaN in the reference) gives
-// NaN here as well.
+// factor.  It starts from A scaled to the Frobenius norm of a rotation and
+// runs in FP32 until the steps stall (about 1e-6), then takes one FP64
+// step.  Write X = R (I + H + K), H symmetric, K skew: a Newton step
+// squares H away but keeps K to first order, so the FP64 step leaves X
+// orthogonal to ~1e-14 while the FP32 steps' rounding along the rotation
+// (K, ~5e-8) stays.  R is thus an exact rotation within about one float
+// ulp of the exact polar factor of A (max 9e-8 over 2,000 seeded
+// near-rotations times stretches).  The FP64 pipe, narrow on GB300, does
+// one step's work (about 1% of the pass).  A singular A (NaN in the
+// reference) gives NaN here as well.
 __device__ void polar_rotation_fp64(const float apq[9], float r[9]) {
     float X[9];
     float n2 = 0.f;
@@ -538,10 +540,65 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 // candidates, so the results are identical; the named force pass (whose
 // masks may be stale) scans.
 
+// Pass 1 of the plane-free solid passes over particle k's stencil rows,
+// from the cell-sorted copies.  Each row is taken in chunks of 64
+// candidates: a tight loop over the chunk adds the density term (j = i
+// included, in the density pass's order), records the mask bits and the
+// bits of the chunk's current neighbours (j != i, |p| <= h); then
+// sum(p, q, w) runs for those neighbours in candidate order, w = (h^2 -
+// |p|^2)^3.  The sums therefore see the neighbours in the order a plain
+// scan would, while the scan loop itself stays free of the sums' work,
+// which otherwise every lane would issue whenever any lane of its warp
+// met a neighbour.  Only a row's first 64 candidates have mask bits;
+// `overflow` records a longer row.
+template <class Sum>
+__device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, const StencilRows &rows,
+                                                float3 ipos, float3 ipos0, const SolidConsts &C,
+                                                int with_density, Kahan &rho, unsigned &count, unsigned &total,
+                                                bool &overflow, Sum &&sum) {
+    const float4 *__restrict__ spos = S.spos;
+    const float4 *__restrict__ spos0 = S.spos0;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        unsigned b, e;
+        rows.row(S, r, &b, &e);
+        const unsigned len = e - b;
+#pragma unroll 1
+        for (unsigned c0 = 0; c0 < len; c0 += 64) {
+            const unsigned cb = b + c0, cn = min(len - c0, 64u);
+            unsigned long long bits = 0, near = 0;
+#pragma unroll 4
+            for (unsigned t = 0; t < cn; ++t) {
+                const unsigned kk = cb + t;
+                const float r2 = norm2(sub3(xyz(spos[kk]), ipos));
+                if (with_density && r2 <= C.le) {
+                    const float d = fmaxf(C.h2 - r2, 0.f);
+                    rho.add(d * d * d);
+                    count += r2 <= C.lt;
+                }
+                const float q2 = norm2(sub3(xyz(spos0[kk]), ipos0));
+                const unsigned long long bit = kk == k ? 0ull : 1ull << t;
+                if (r2 <= C.le) near |= bit;
+                if (r2 <= C.le || q2 <= C.le) bits |= bit;
+            }
+            if (c0 == 0) store_row_mask(S, k, r, len, bits);
+            while (near) {
+                const unsigned kk = cb + (unsigned)(__ffsll((long long)near) - 1);
+                near &= near - 1ull;
+                const float3 p = sub3(xyz(spos[kk]), ipos);
+                const float d = fmaxf(C.h2 - norm2(p), 0.f);
+                sum(p, sub3(xyz(spos0[kk]), ipos0), d * d * d);
+            }
+        }
+        overflow |= len > 64;
+        total += len;
+    }
+}
+
 // compute_rotations_and_strains (solid_corotation.cl:28-195) for
-// plane-free scenes: pass 1 sums Apq over candidates with |p| <= h and
-// records the masks, R = polar(Apq) in FP64, pass 2 sums D over the masked
-// candidates with |q| <= h.  Body particles keep their rotation and strain
+// plane-free scenes: pass 1 (scan_solid_rows) sums Apq over candidates
+// with |p| <= h and records the masks, R = polar(Apq), pass 2 sums D over
+// the masked candidates with |q| <= h.  Body particles keep their rotation and strain
 // (their masks are still recorded).  Also writes the sorted rotation copy.
 __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density) {
     SPH_FOR_WORK(map)
@@ -559,34 +616,8 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
         unsigned total = 0, count = 0;
         bool overflow = false;
         Kahan rho;
-#pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
-            unsigned b, e;
-            rows.row(S, r, &b, &e);
-            unsigned long long bits = 0;
-#pragma unroll 4
-            for (unsigned t = 0; t < e - b; ++t) {
-                const unsigned kk = b + t;
-                const float3 p = sub3(xyz(spos[kk]), ipos);
-                const float r2 = norm2(p);
-                // the density pass's sum, in its order (j = i included)
-                if (with_density && r2 <= C.le) {
-                    const float d = fmaxf(C.h2 - r2, 0.f);
-                    rho.add(d * d * d);
-                    count += r2 <= C.lt;
-                }
-                if (kk == k) continue;
-                const float3 q = sub3(xyz(spos0[kk]), ipos0);
-                if (r2 <= C.le) {
-                    const float d = fmaxf(C.h2 - r2, 0.f);
-                    add_outer(p * (d * d * d), q, apq);
-                }
-                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
-            }
-            store_row_mask(S, k, r, e - b, bits);
-            overflow |= e - b > 64;
-            total += e - b;
-        }
+        scan_solid_rows(S, k, rows, ipos, ipos0, C, with_density, rho, count, total, overflow,
+                        [&](float3 p, float3 q, float w) { add_outer(p * w, q, apq); });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         if (with_density) {
             const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
@@ -642,46 +673,19 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
         const SolidConsts C = solid_consts(S);
         const float3 ipos = xyz(S.spos[k]), ipos0 = xyz(S.spos0[k]);
         const StencilRows rows(S, S.gridcell[i]);
-        const float4 *__restrict__ spos = S.spos;
-        const float4 *__restrict__ spos0 = S.spos0;
         float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
         float aqq[6] = {0, 0, 0, 0, 0, 0};
         unsigned total = 0, count = 0;
         bool overflow = false;
         Kahan rho;
-#pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
-            unsigned b, e;
-            rows.row(S, r, &b, &e);
-            unsigned long long bits = 0;
-#pragma unroll 4
-            for (unsigned t = 0; t < e - b; ++t) {
-                const unsigned kk = b + t;
-                const float3 p = sub3(xyz(spos[kk]), ipos);
-                const float r2 = norm2(p);
-                // the density pass's sum, in its order (j = i included)
-                if (with_density && r2 <= C.le) {
-                    const float d = fmaxf(C.h2 - r2, 0.f);
-                    rho.add(d * d * d);
-                    count += r2 <= C.lt;
-                }
-                if (kk == k) continue;
-                const float3 q = sub3(xyz(spos0[kk]), ipos0);
-                if (r2 <= C.le) {
-                    const float d = fmaxf(C.h2 - r2, 0.f);
-                    const float w = d * d * d;
-                    add_outer(p * w, q, apq);
-                    const float3 wq = q * w;
-                    aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
-                    aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
-                    aqq[2] += wq.z * q.z;
-                }
-                if ((r2 <= C.le || norm2(q) <= C.le) && t < 64) bits |= 1ull << t;
-            }
-            store_row_mask(S, k, r, e - b, bits);
-            overflow |= e - b > 64;
-            total += e - b;
-        }
+        scan_solid_rows(S, k, rows, ipos, ipos0, C, with_density, rho, count, total, overflow,
+                        [&](float3 p, float3 q, float w) {
+                            add_outer(p * w, q, apq);
+                            const float3 wq = q * w;
+                            aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
+                            aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
+                            aqq[2] += wq.z * q.z;
+                        });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         if (with_density) {
             const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
