@@ -191,10 +191,12 @@ __device__ __forceinline__ float3 sym_vec(const float s[6], float3 v) {
     return make_float3(s[0] * v.x + s[3] * v.y + s[4] * v.z, s[3] * v.x + s[1] * v.y + s[5] * v.z,
                        s[4] * v.x + s[5] * v.y + s[2] * v.z);
 }
+// m += a b^T, one fused multiply-add per entry, written out so that every
+// copy of a sum rounds alike whatever the compiler would contract.
 __device__ __forceinline__ void add_outer(float3 a, float3 b, float m[9]) {
-    m[0] += a.x * b.x; m[1] += a.x * b.y; m[2] += a.x * b.z;
-    m[3] += a.y * b.x; m[4] += a.y * b.y; m[5] += a.y * b.z;
-    m[6] += a.z * b.x; m[7] += a.z * b.y; m[8] += a.z * b.z;
+    m[0] = __fmaf_rn(a.x, b.x, m[0]); m[1] = __fmaf_rn(a.x, b.y, m[1]); m[2] = __fmaf_rn(a.x, b.z, m[2]);
+    m[3] = __fmaf_rn(a.y, b.x, m[3]); m[4] = __fmaf_rn(a.y, b.y, m[4]); m[5] = __fmaf_rn(a.y, b.z, m[5]);
+    m[6] = __fmaf_rn(a.z, b.x, m[6]); m[7] = __fmaf_rn(a.z, b.y, m[7]); m[8] = __fmaf_rn(a.z, b.z, m[8]);
 }
 
 // Spiky gradient dir(d) * -45/(pi h^6) * (h - |d|)^2, zero beyond h
@@ -541,21 +543,25 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 // masks may be stale) scans.
 
 // Pass 1 of the plane-free solid passes over particle k's stencil rows,
-// from the cell-sorted copies.  Each row is taken in chunks of 64
-// candidates: a tight loop over the chunk adds the density term (j = i
-// included, in the density pass's order), records the mask bits and the
-// bits of the chunk's current neighbours (j != i, |p| <= h); then
-// sum(p, q, w) runs for those neighbours in candidate order, w = (h^2 -
-// |p|^2)^3.  The sums therefore see the neighbours in the order a plain
-// scan would, while the scan loop itself stays free of the sums' work,
-// which otherwise every lane would issue whenever any lane of its warp
-// met a neighbour.  Only a row's first 64 candidates have mask bits;
-// `overflow` records a longer row.
+// from the cell-sorted copies.  Each row is taken in chunks of 32
+// candidates, one mask word each: a tight loop over the chunk adds the
+// density term (j = i included, in the density pass's order), records the
+// mask bits and the bits of the chunk's current neighbours (|p| <= h);
+// particle k's own bit is cleared afterwards.  Then sum(p, q, w) runs for
+// the neighbours in candidate order, w = (h^2 - |p|^2)^3.  The sums see
+// the neighbours in the order a plain scan would, while the scan loop stays
+// free of their work, which otherwise every lane would issue whenever any
+// lane of its warp met a neighbour.  Only a row's first 64 candidates have
+// mask bits; `overflow` records a longer row.
+//
+// The density terms are summed whether or not the caller stores them: a
+// flag tested inside the loop lets the compiler emit one copy of the loop
+// per value, and copies may contract the sums' products differently, which
+// would break the equality of the named and fused passes.
 template <class Sum>
 __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, const StencilRows &rows,
-                                                float3 ipos, float3 ipos0, const SolidConsts &C,
-                                                int with_density, Kahan &rho, unsigned &count, unsigned &total,
-                                                bool &overflow, Sum &&sum) {
+                                                float3 ipos, float3 ipos0, const SolidConsts &C, Kahan &rho,
+                                                unsigned &count, unsigned &total, bool &overflow, Sum &&sum) {
     const float4 *__restrict__ spos = S.spos;
     const float4 *__restrict__ spos0 = S.spos0;
 #pragma unroll 1
@@ -564,27 +570,33 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
         rows.row(S, r, &b, &e);
         const unsigned len = e - b;
 #pragma unroll 1
-        for (unsigned c0 = 0; c0 < len; c0 += 64) {
-            const unsigned cb = b + c0, cn = min(len - c0, 64u);
-            unsigned long long bits = 0, near = 0;
+        for (unsigned c0 = 0; c0 < len; c0 += 32) {
+            const unsigned cb = b + c0, cn = min(len - c0, 32u);
+            unsigned bits = 0, near = 0;
 #pragma unroll 4
             for (unsigned t = 0; t < cn; ++t) {
                 const unsigned kk = cb + t;
                 const float r2 = norm2(sub3(xyz(spos[kk]), ipos));
-                if (with_density && r2 <= C.le) {
+                if (r2 <= C.le) {
                     const float d = fmaxf(C.h2 - r2, 0.f);
                     rho.add(d * d * d);
                     count += r2 <= C.lt;
                 }
                 const float q2 = norm2(sub3(xyz(spos0[kk]), ipos0));
-                const unsigned long long bit = kk == k ? 0ull : 1ull << t;
+                const unsigned bit = 1u << t;
                 if (r2 <= C.le) near |= bit;
                 if (r2 <= C.le || q2 <= C.le) bits |= bit;
             }
-            if (c0 == 0) store_row_mask(S, k, r, len, bits);
+            if (k - cb < cn) {  // k itself is in this chunk
+                const unsigned self = ~(1u << (k - cb));
+                bits &= self;
+                near &= self;
+            }
+            // mask words 2r and 2r + 1 (store_row_mask's layout)
+            if (c0 < 64) S.nbmask[(size_t)(2 * r + (c0 >> 5)) * S.pnum + k] = bits;
             while (near) {
-                const unsigned kk = cb + (unsigned)(__ffsll((long long)near) - 1);
-                near &= near - 1ull;
+                const unsigned kk = cb + (unsigned)(__ffs(near) - 1);
+                near &= near - 1u;
                 const float3 p = sub3(xyz(spos[kk]), ipos);
                 const float d = fmaxf(C.h2 - norm2(p), 0.f);
                 sum(p, sub3(xyz(spos0[kk]), ipos0), d * d * d);
@@ -616,7 +628,7 @@ __global__ void k_rotations_and_strains(const SceneDesc *__restrict__ scenes, Bl
         unsigned total = 0, count = 0;
         bool overflow = false;
         Kahan rho;
-        scan_solid_rows(S, k, rows, ipos, ipos0, C, with_density, rho, count, total, overflow,
+        scan_solid_rows(S, k, rows, ipos, ipos0, C, rho, count, total, overflow,
                         [&](float3 p, float3 q, float w) { add_outer(p * w, q, apq); });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         if (with_density) {
@@ -678,13 +690,16 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
         unsigned total = 0, count = 0;
         bool overflow = false;
         Kahan rho;
-        scan_solid_rows(S, k, rows, ipos, ipos0, C, with_density, rho, count, total, overflow,
+        scan_solid_rows(S, k, rows, ipos, ipos0, C, rho, count, total, overflow,
                         [&](float3 p, float3 q, float w) {
                             add_outer(p * w, q, apq);
                             const float3 wq = q * w;
-                            aqq[0] += wq.x * q.x; aqq[3] += wq.x * q.y; aqq[4] += wq.x * q.z;
-                            aqq[1] += wq.y * q.y; aqq[5] += wq.y * q.z;
-                            aqq[2] += wq.z * q.z;
+                            aqq[0] = __fmaf_rn(wq.x, q.x, aqq[0]);
+                            aqq[1] = __fmaf_rn(wq.y, q.y, aqq[1]);
+                            aqq[2] = __fmaf_rn(wq.z, q.z, aqq[2]);
+                            aqq[3] = __fmaf_rn(wq.x, q.y, aqq[3]);
+                            aqq[4] = __fmaf_rn(wq.x, q.z, aqq[4]);
+                            aqq[5] = __fmaf_rn(wq.y, q.z, aqq[5]);
                         });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
         if (with_density) {
