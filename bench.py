@@ -304,11 +304,6 @@ def run_e2e(ps, scene, steps, torch):
             "d2h_bytes_per_step": 12 * scene.n, "host_memory": "pinned" if registered else "pageable"}
 
 
-def bnd_size(ps):
-    from sph import bindings as bnd
-    return bnd.psdata_data_size(ps)
-
-
 def batched_scenes(seed, workload="batched-256"):
     from sph import scenes
     if workload == "large-scene":
@@ -362,15 +357,13 @@ def bench_batched(args, torch, world):
     total_s = sum(a.elapsed_time(e) for a, e in zip(starts, ends)) / 1e3
     phases = b.profile(reps=max(3, min(args.steps, 10)))
     # end to end: per step, one batched substep and every scene's positions
-    # downloaded into its host store (the stores pinned for the run, the
-    # copies enqueued together and waited for once)
-    cudart = torch.cuda.cudart()
+    # downloaded into its host store (the stores pinned through the batch,
+    # one copy kernel writing all of them, one wait)
     pinned = []
     for sid in ids:
-        ps = b.scenes[sid].psdata
         try:
-            if int(cudart.cudaHostRegister(ps.data, bnd_size(ps), 0)) == 0:
-                pinned.append(ps.data)
+            b.pin(sid)
+            pinned.append(sid)
         except Exception:
             pass
     t0 = time.perf_counter()
@@ -378,8 +371,8 @@ def bench_batched(args, torch, world):
         b.step(1)
         b.read_fields(ids, "position")
     e2e_s = time.perf_counter() - t0
-    for ptr in pinned:
-        cudart.cudaHostUnregister(ptr)
+    for sid in pinned:
+        b.unpin(sid)
     status = sum(1 for sid in ids if b.status(sid) != 0)
     cells = 0
     by_mat = {"fluid": [0, 0], "corot": [0, 0], "svk": [0, 0]}

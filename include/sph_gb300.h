@@ -270,6 +270,19 @@ int sph_batch_read_field(sph_batch *batch, int id, const char *field, psdata *ou
  * current after sph_batch_synchronize (and asynchronous only when its
  * blob is pinned, e.g. by cudaHostRegister). */
 int sph_batch_read_field_async(sph_batch *batch, int id, const char *field, psdata *out);
+/* Page-locks the host store `store` (of the scene's layout) for reads of
+ * scene `id` (cudaHostRegister, mapped; a store the caller registered
+ * already is used as it is).  Reads into it by sph_batch_read_field_many
+ * then go through one copy kernel that writes the store directly.  The
+ * registration ends with sph_batch_unpin_host, sph_batch_remove or
+ * sph_batch_free, which must come before the store is freed. */
+int sph_batch_pin_host(sph_batch *batch, int id, psdata *store);
+int sph_batch_unpin_host(sph_batch *batch, int id);
+/* Copies one named field of `count` scenes into the same field of their
+ * stores outs[k] and waits: one kernel launch for all stores pinned with
+ * sph_batch_pin_host, one cudaMemcpyAsync for each other store. */
+int sph_batch_read_field_many(sph_batch *batch, const int *ids, unsigned int count, const char *field,
+                              psdata *const *outs);
 /* Runs `reps` substeps of the batch as individual launches with CUDA events
  * between phases (material branches one after another) and writes each
  * phase's mean device time in ms and its name; returns the phase count. */

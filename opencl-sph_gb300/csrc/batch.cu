@@ -27,6 +27,11 @@ struct BatchScene {
     size_t bytes = 0;
     size_t blob_size = 0;
     SceneDesc desc{};
+    // the host store page-locked by sph_batch_pin_host, and its device
+    // address (written by sph_batch_read_field_many's copy kernel)
+    char *host = nullptr;
+    char *host_dev = nullptr;
+    bool host_owned = false;  // registered here (else by the caller)
 };
 
 bool ok(cudaError_t e, const char *what) {
@@ -56,6 +61,8 @@ struct sph_batch {
     unsigned graph_kernels = 0;
     unsigned block = 256, pair_block = 128, grid_cap = 0;
     size_t bytes = 0;
+    CopySeg *copy_segs = nullptr;  // device table of sph_batch_read_field_many
+    unsigned copy_cap = 0;
 };
 
 namespace {
@@ -274,16 +281,27 @@ extern "C" sph_batch *sph_batch_create(void) {
     return b;
 }
 
+// Ends sph_batch_pin_host's registration (after the stream's work).
+static void unpin_host(sph_batch *b, BatchScene *s) {
+    if (!s->host) return;
+    cudaStreamSynchronize(b->stream);
+    if (s->host_owned) cudaHostUnregister(s->host);
+    s->host = s->host_dev = nullptr;
+    s->host_owned = false;
+}
+
 extern "C" void sph_batch_free(sph_batch *b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     release_graph(b);
     for (BatchScene *s : b->slots)
         if (s) {
+            unpin_host(b, s);
             if (s->mem) cudaFreeAsync(s->mem, b->stream);
             delete s;
         }
     if (b->tables) cudaFreeAsync(b->tables, b->stream);
+    if (b->copy_segs) cudaFreeAsync(b->copy_segs, b->stream);
     if (b->stream) cudaStreamSynchronize(b->stream);
     for (cudaEvent_t e : {b->fork, b->join[0], b->join[1]})
         if (e) cudaEventDestroy(e);
@@ -368,6 +386,7 @@ extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list)
 extern "C" int sph_batch_remove(sph_batch *b, int id) {
     BatchScene *sc = scene_of(b, id, "sph_batch_remove");
     if (!sc) return -1;
+    unpin_host(b, sc);
     cudaFreeAsync(sc->mem, b->stream);
     b->bytes -= sc->bytes;
     delete sc;
@@ -435,6 +454,94 @@ extern "C" int sph_batch_read_field(sph_batch *b, int id, const char *field, psd
 
 extern "C" int sph_batch_read_field_async(sph_batch *b, int id, const char *field, psdata *out) {
     return read_field(b, id, field, out, false, "sph_batch_read_field_async");
+}
+
+extern "C" int sph_batch_pin_host(sph_batch *b, int id, psdata *store) {
+    const char *what = "sph_batch_pin_host";
+    BatchScene *sc = scene_of(b, id, what);
+    if (!sc) return -1;
+    if (!store || !store->data || psdata_data_size(*store) != sc->blob_size) {
+        sph_set_error("%s: the host store's layout differs from the scene's", what);
+        return -1;
+    }
+    char *host = static_cast<char *>(store->data);
+    if (sc->host == host) return 0;
+    unpin_host(b, sc);
+    bool owned = true;
+    cudaError_t e = cudaHostRegister(host, sc->blob_size, cudaHostRegisterMapped);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) {
+        cudaGetLastError();  // registered by the caller: use it, leave it registered
+        owned = false;
+    } else if (!ok(e, what)) {
+        cudaGetLastError();
+        return -1;
+    }
+    void *dev = nullptr;
+    e = cudaHostGetDevicePointer(&dev, host, 0);
+    if (e != cudaSuccess || !dev) {
+        cudaGetLastError();
+        if (owned) cudaHostUnregister(host);
+        sph_set_error("%s: no device address for the host store (%s)", what, cudaGetErrorString(e));
+        return -1;
+    }
+    sc->host = host;
+    sc->host_dev = static_cast<char *>(dev);
+    sc->host_owned = owned;
+    return 0;
+}
+
+extern "C" int sph_batch_unpin_host(sph_batch *b, int id) {
+    BatchScene *sc = scene_of(b, id, "sph_batch_unpin_host");
+    if (!sc) return -1;
+    unpin_host(b, sc);
+    return 0;
+}
+
+extern "C" int sph_batch_read_field_many(sph_batch *b, const int *ids, unsigned int count, const char *field,
+                                         psdata *const *outs) {
+    const char *what = "sph_batch_read_field_many";
+    if (!b || (count && (!ids || !outs))) {
+        sph_set_error("%s: no batch, ids or stores", what);
+        return -1;
+    }
+    std::vector<CopySeg> segs;
+    unsigned long long max_bytes = 0;
+    for (unsigned k = 0; k < count; ++k) {
+        BatchScene *sc = scene_of(b, ids[k], what);
+        if (!sc) return -1;
+        psdata *out = outs[k];
+        const int f = out && field ? get_field_psdata(*out, field) : -1;
+        if (f < 0 || psdata_data_size(*out) != sc->blob_size) {
+            sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field ? field : "");
+            return -1;
+        }
+        const size_t off = out->data_offsets[f], sz = out->data_sizes[f];
+        if (sc->host && sc->host == static_cast<char *>(out->data)) {
+            segs.push_back(CopySeg{sc->mem + off, sc->host_dev + off, (unsigned long long)sz});
+            if (sz > max_bytes) max_bytes = sz;
+        } else if (!ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost,
+                                       b->stream),
+                       what)) {
+            return -1;
+        }
+    }
+    if (!segs.empty()) {
+        if (segs.size() > b->copy_cap) {
+            if (b->copy_segs) cudaFreeAsync(b->copy_segs, b->stream);
+            b->copy_segs = nullptr;
+            b->copy_cap = 0;
+            const unsigned cap = (unsigned)segs.size() * 2;
+            if (!ok(cudaMallocAsync((void **)&b->copy_segs, cap * sizeof(CopySeg), b->stream), what)) return -1;
+            b->copy_cap = cap;
+        }
+        if (!ok(cudaMemcpyAsync(b->copy_segs, segs.data(), segs.size() * sizeof(CopySeg), cudaMemcpyHostToDevice,
+                                b->stream),
+                what))
+            return -1;
+        sph_launch_copy_segments(b->copy_segs, (unsigned)segs.size(), max_bytes, b->stream);
+        if (sph_check_launch(what) != cudaSuccess) return -1;
+    }
+    return ok(cudaStreamSynchronize(b->stream), what) ? 0 : -1;
 }
 
 namespace {

@@ -288,3 +288,38 @@ void sph_launch_record(const RecordPlan &p, cudaStream_t stream) {
     k_record_copy<<<g ? g : 1, 256, 0, stream>>>(p);
     k_record_tick<<<1, 1, 0, stream>>>(p);
 }
+
+// Segment copy: block row y copies segment y, in 16-byte words where both
+// ends allow, else 4-byte words, else bytes (a grid-stride loop each).
+__global__ void k_copy_segments(const CopySeg *__restrict__ segs, unsigned first) {
+    const CopySeg g = segs[first + blockIdx.y];
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uintptr_t align = (uintptr_t)g.src | (uintptr_t)g.dst;
+    size_t done = 0;
+    if (align % 16 == 0) {
+        const size_t n = g.bytes / 16;
+        const uint4 *s = reinterpret_cast<const uint4 *>(g.src);
+        uint4 *d = reinterpret_cast<uint4 *>(g.dst);
+        for (size_t w = t0; w < n; w += stride) d[w] = s[w];
+        done = n * 16;
+    } else if (align % 4 == 0) {
+        const size_t n = g.bytes / 4;
+        const unsigned *s = reinterpret_cast<const unsigned *>(g.src);
+        unsigned *d = reinterpret_cast<unsigned *>(g.dst);
+        for (size_t w = t0; w < n; w += stride) d[w] = s[w];
+        done = n * 4;
+    }
+    for (size_t c = done + t0; c < g.bytes; c += stride) g.dst[c] = g.src[c];
+}
+
+void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long long max_bytes,
+                              cudaStream_t stream) {
+    const unsigned long long per_block = 256ull * 16 * 4;  // four 16-byte words per thread
+    unsigned gx = (unsigned)((max_bytes + per_block - 1) / per_block);
+    gx = gx < 1 ? 1 : gx > 256 ? 256 : gx;
+    for (unsigned first = 0; first < count; first += 65535u) {
+        const unsigned gy = count - first < 65535u ? count - first : 65535u;
+        k_copy_segments<<<dim3(gx, gy), 256, 0, stream>>>(segs, first);
+    }
+}

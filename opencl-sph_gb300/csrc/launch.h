@@ -88,6 +88,17 @@ void sph_launch_rigid_reset(const Launch &L);
 void sph_launch_count_down(const Launch &L);
 void sph_launch_set_steps(unsigned *steps_left, unsigned steps, cudaStream_t stream);
 
+// One byte range to copy (device to device or to mapped host memory).
+struct CopySeg {
+    const char *src;
+    char *dst;
+    unsigned long long bytes;
+};
+// Copies segs[0 .. count) (a device table) in one launch per 65,535
+// segments; `max_bytes` is the largest segment.
+void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long long max_bytes,
+                              cudaStream_t stream);
+
 // One substep of a material's recipe for every scene of the launch.  All
 // scenes of L must share the material (batches launch one Launch per
 // material group).  `mark`, when given, is called with each phase's name

@@ -31,6 +31,7 @@ class Batch(object):
         if not self.handle:
             raise bnd.SphError(bnd.last_error())
         self.scenes = {}
+        self._reads = None
 
     @staticmethod
     def host_store(scene):
@@ -67,6 +68,7 @@ class Batch(object):
     def remove(self, sid):
         if bnd.sph_batch_remove(self.handle, sid) != 0:
             raise bnd.SphError(bnd.last_error())
+        self._reads = None
         free_data_cpu(self.scenes.pop(sid).psdata)
 
     def step(self, steps=1):
@@ -102,15 +104,31 @@ class Batch(object):
             raise bnd.SphError(bnd.last_error())
         return s.views[name]
 
+    def pin(self, sid):
+        """Page-locks scene `sid`'s host store, so that read_fields writes it
+        from one copy kernel; removing the scene or closing the batch ends
+        it."""
+        if bnd.sph_batch_pin_host(self.handle, sid, ctypes.byref(self.scenes[sid].psdata)) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def unpin(self, sid):
+        if bnd.sph_batch_unpin_host(self.handle, sid) != 0:
+            raise bnd.SphError(bnd.last_error())
+
     def read_fields(self, sids, name):
-        """Copies one field of several scenes back with a single wait; returns
-        their host views (sid -> array)."""
-        for sid in sids:
-            s = self.scenes[sid]
-            if bnd.sph_batch_read_field_async(self.handle, sid, name, ctypes.byref(s.psdata)) != 0:
-                raise bnd.SphError(bnd.last_error())
-        self.synchronize()
-        return {sid: self.scenes[sid].views[name] for sid in sids}
+        """Copies one field of several scenes back with a single wait (one
+        kernel for the pinned stores); returns their host views (sid ->
+        array)."""
+        key = tuple(sids)
+        if self._reads is None or self._reads[0] != key:
+            # the argument arrays, kept while the same scenes are read
+            ids = (ctypes.c_int * len(key))(*key)
+            outs = (ctypes.POINTER(bnd.psdata) * len(key))(*[ctypes.pointer(self.scenes[s].psdata) for s in key])
+            self._reads = (key, ids, outs)
+        _, ids, outs = self._reads
+        if bnd.sph_batch_read_field_many(self.handle, ids, len(key), name, outs) != 0:
+            raise bnd.SphError(bnd.last_error())
+        return {sid: self.scenes[sid].views[name] for sid in key}
 
     def profile(self, reps=3):
         """Mean device ms per phase of a substep (phases run one by one)."""
@@ -151,6 +169,7 @@ class Batch(object):
         for s in self.scenes.values():
             free_data_cpu(s.psdata)
         self.scenes = {}
+        self._reads = None
 
     def __del__(self):
         try:

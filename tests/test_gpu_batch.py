@@ -178,6 +178,35 @@ def test_read_fields_async_equals_read():
     b.close()
 
 
+def test_pinned_read_fields_one_kernel():
+    """Pinned stores are written by one copy kernel, the others by copies:
+    either way each store's field equals a full read, and the other fields
+    of a pinned store are left alone.  Removing a pinned scene unpins it."""
+    scs = mix(seed=51)
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    for sid in ids[::2]:
+        b.pin(sid)
+    b.pin(ids[0])  # pinning twice is harmless
+    b.step(5)
+    before = {sid: np.array(b.scenes[sid].views["velocity"]) for sid in ids}
+    got = b.read_fields(ids, "position")
+    for sid in ids:
+        assert np.array_equal(b.scenes[sid].views["velocity"], before[sid])
+    for sid in ids:
+        want = np.array(got[sid])
+        assert np.array_equal(want, b.read(sid)["position"])
+    b.step(2)
+    b.unpin(ids[2])
+    got = b.read_fields(ids[:3], "velocity")
+    for sid in ids[:3]:
+        assert np.array_equal(np.array(got[sid]), b.read(sid)["velocity"])
+    b.remove(ids[0])
+    got = b.read_fields(ids[1:], "position")
+    assert all(np.isfinite(v).all() for v in got.values())
+    b.close()
+
+
 def test_ragged_and_empty_scenes_in_a_batch():
     """Scenes with fewer active particles than their capacity, and with none,
     run beside full ones: the ragged scene equals itself alone, the empty
