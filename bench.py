@@ -357,21 +357,24 @@ def bench_batched(args, torch, world):
     total_s = sum(a.elapsed_time(e) for a, e in zip(starts, ends)) / 1e3
     phases = b.profile(reps=max(3, min(args.steps, 10)))
     # end to end: per step, one batched substep and every scene's positions
-    # downloaded into its host store (the stores pinned through the batch,
-    # one copy kernel writing all of them, one wait)
-    pinned = []
+    # written into its host store.  The stores are pinned through the batch;
+    # each step's positions are snapshot on the device and written to the
+    # host while the next substep runs, and the loop waits for step s - 1's
+    # positions to be on the host before it enqueues step s + 1.
     for sid in ids:
-        try:
-            b.pin(sid)
-            pinned.append(sid)
-        except Exception:
-            pass
+        b.pin(sid)
+    b.wait_read(b.read_fields_async(ids, "position"))  # allocates the read buffers
     t0 = time.perf_counter()
+    prev = None
     for _ in range(args.steps):
         b.step(1)
-        b.read_fields(ids, "position")
+        t = b.read_fields_async(ids, "position")
+        if prev is not None:
+            b.wait_read(prev)
+        prev = t
+    b.wait_read(prev)
     e2e_s = time.perf_counter() - t0
-    for sid in pinned:
+    for sid in ids:
         b.unpin(sid)
     status = sum(1 for sid in ids if b.status(sid) != 0)
     cells = 0
@@ -393,8 +396,10 @@ def bench_batched(args, torch, world):
             "kernels_per_step": kernels_per_step, "status_scenes": status,
             "e2e": {"value": n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 12 * n,
-                    "host_memory": "pinned" if len(pinned) == len(ids) else "pageable (%d of %d pinned)" % (
-                        len(pinned), len(ids))}}
+                    "host_memory": "pinned (sph_batch_pin_host)",
+                    "reads": "per step: device snapshot of every scene's positions, written to the host stores "
+                             "beside the next substep (sph_batch_read_field_many_async); step s - 1's positions "
+                             "are on the host before step s + 1 is enqueued"}}
 
 
 def bench_plain_loop(scs, steps):

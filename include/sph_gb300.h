@@ -283,6 +283,18 @@ int sph_batch_unpin_host(sph_batch *batch, int id);
  * sph_batch_pin_host, one cudaMemcpyAsync for each other store. */
 int sph_batch_read_field_many(sph_batch *batch, const int *ids, unsigned int count, const char *field,
                               psdata *const *outs);
+/* The same read without waiting, for stores pinned with sph_batch_pin_host:
+ * the field is copied to a device snapshot in stream order (after the
+ * substeps enqueued so far), and a side stream copies the snapshot into the
+ * stores (one cudaMemcpyAsync each) while later substeps run.  Returns a ticket (>= 0), or -1.  The
+ * stores hold the snapshot after sph_batch_wait_read(ticket); a later read
+ * overwrites them.  Two reads are in flight at most: a third waits, on the
+ * device, for the first to finish. */
+long long sph_batch_read_field_many_async(sph_batch *batch, const int *ids, unsigned int count, const char *field,
+                                          psdata *const *outs);
+int sph_batch_wait_read(sph_batch *batch, long long ticket);
+/* Waits for every read enqueued so far. */
+int sph_batch_wait_reads(sph_batch *batch);
 /* Runs `reps` substeps of the batch as individual launches with CUDA events
  * between phases (material branches one after another) and writes each
  * phase's mean device time in ms and its name; returns the phase count. */

@@ -63,6 +63,18 @@ struct sph_batch {
     size_t bytes = 0;
     CopySeg *copy_segs = nullptr;  // device table of sph_batch_read_field_many
     unsigned copy_cap = 0;
+    // sph_batch_read_field_many_async: reads take turns over two snapshot
+    // buffers and segment tables; the stream `reads` copies a snapshot into
+    // the pinned host stores while later substeps run on `stream`
+    cudaStream_t reads = nullptr;
+    cudaEvent_t snap_done[2] = {nullptr, nullptr}, read_done[2] = {nullptr, nullptr};
+    char *snap[2] = {nullptr, nullptr};
+    size_t snap_cap[2] = {0, 0};
+    CopySeg *snap_segs[2] = {nullptr, nullptr};
+    unsigned snap_seg_cap[2] = {0, 0};
+    CopySeg *seg_host[2] = {nullptr, nullptr};  // pinned: the upload must not wait for the stream
+    size_t seg_host_cap[2] = {0, 0};
+    long long tickets = 0;  // reads enqueued so far
 };
 
 namespace {
@@ -281,9 +293,15 @@ extern "C" sph_batch *sph_batch_create(void) {
     return b;
 }
 
-// Ends sph_batch_pin_host's registration (after the stream's work).
+// Waits for the asynchronous reads in flight (they write host stores).
+static bool drain_reads(sph_batch *b, const char *what) {
+    return !b->reads || ok(cudaStreamSynchronize(b->reads), what);
+}
+
+// Ends sph_batch_pin_host's registration (after the streams' work).
 static void unpin_host(sph_batch *b, BatchScene *s) {
     if (!s->host) return;
+    drain_reads(b, "unpin");
     cudaStreamSynchronize(b->stream);
     if (s->host_owned) cudaHostUnregister(s->host);
     s->host = s->host_dev = nullptr;
@@ -302,10 +320,17 @@ extern "C" void sph_batch_free(sph_batch *b) {
         }
     if (b->tables) cudaFreeAsync(b->tables, b->stream);
     if (b->copy_segs) cudaFreeAsync(b->copy_segs, b->stream);
+    for (int t = 0; t < 2; ++t) {
+        if (b->snap[t]) cudaFreeAsync(b->snap[t], b->stream);
+        if (b->snap_segs[t]) cudaFreeAsync(b->snap_segs[t], b->stream);
+    }
     if (b->stream) cudaStreamSynchronize(b->stream);
-    for (cudaEvent_t e : {b->fork, b->join[0], b->join[1]})
+    for (int t = 0; t < 2; ++t)
+        if (b->seg_host[t]) cudaFreeHost(b->seg_host[t]);
+    for (cudaEvent_t e : {b->fork, b->join[0], b->join[1], b->snap_done[0], b->snap_done[1], b->read_done[0],
+                          b->read_done[1]})
         if (e) cudaEventDestroy(e);
-    for (cudaStream_t s : {b->stream, b->side[0], b->side[1]})
+    for (cudaStream_t s : {b->stream, b->side[0], b->side[1], b->reads})
         if (s) cudaStreamDestroy(s);
     delete b;
 }
@@ -428,7 +453,8 @@ extern "C" int sph_batch_read(sph_batch *b, int id, psdata *out) {
         sph_set_error("sph_batch_read: the host store's layout differs from the scene's");
         return -1;
     }
-    if (!ok(cudaMemcpyAsync(out->data, sc->mem, sc->blob_size, cudaMemcpyDeviceToHost, b->stream), "sph_batch_read") ||
+    if (!drain_reads(b, "sph_batch_read") ||
+        !ok(cudaMemcpyAsync(out->data, sc->mem, sc->blob_size, cudaMemcpyDeviceToHost, b->stream), "sph_batch_read") ||
         !ok(cudaStreamSynchronize(b->stream), "sph_batch_read"))
         return -1;
     return 0;
@@ -443,7 +469,8 @@ static int read_field(sph_batch *b, int id, const char *field, psdata *out, bool
         return -1;
     }
     size_t off = out->data_offsets[f], sz = out->data_sizes[f];
-    if (!ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost, b->stream), what))
+    if (!drain_reads(b, what) ||
+        !ok(cudaMemcpyAsync((char *)out->data + off, sc->mem + off, sz, cudaMemcpyDeviceToHost, b->stream), what))
         return -1;
     return !wait || ok(cudaStreamSynchronize(b->stream), what) ? 0 : -1;
 }
@@ -504,6 +531,7 @@ extern "C" int sph_batch_read_field_many(sph_batch *b, const int *ids, unsigned 
         sph_set_error("%s: no batch, ids or stores", what);
         return -1;
     }
+    if (!drain_reads(b, what)) return -1;
     std::vector<CopySeg> segs;
     unsigned long long max_bytes = 0;
     for (unsigned k = 0; k < count; ++k) {
@@ -542,6 +570,114 @@ extern "C" int sph_batch_read_field_many(sph_batch *b, const int *ids, unsigned 
         if (sph_check_launch(what) != cudaSuccess) return -1;
     }
     return ok(cudaStreamSynchronize(b->stream), what) ? 0 : -1;
+}
+
+// Grows a stream-ordered buffer (on `stream`, after what it ordered).
+template <class T>
+static bool grow(T **p, size_t *cap, size_t want, cudaStream_t stream, const char *what) {
+    if (want <= *cap) return true;
+    if (*p) cudaFreeAsync(*p, stream);
+    *p = nullptr;
+    *cap = 0;
+    const size_t c = want + want / 2;
+    if (!ok(cudaMallocAsync((void **)p, c * sizeof(T), stream), what)) return false;
+    *cap = c;
+    return true;
+}
+
+extern "C" long long sph_batch_read_field_many_async(sph_batch *b, const int *ids, unsigned int count,
+                                                     const char *field, psdata *const *outs) {
+    const char *what = "sph_batch_read_field_many_async";
+    if (!b || !count || !ids || !outs) {
+        sph_set_error("%s: no batch, ids or stores", what);
+        return -1;
+    }
+    if (!b->reads) {
+        bool good = ok(cudaStreamCreateWithFlags(&b->reads, cudaStreamNonBlocking), what);
+        for (int t = 0; good && t < 2; ++t)
+            good = ok(cudaEventCreateWithFlags(&b->snap_done[t], cudaEventDisableTiming), what) &&
+                   ok(cudaEventCreateWithFlags(&b->read_done[t], cudaEventDisableTiming), what);
+        if (!good) return -1;
+    }
+    std::vector<CopySeg> segs(count);
+    std::vector<size_t> at(count);
+    std::vector<char *> dst(count);
+    size_t total = 0;
+    unsigned long long max_bytes = 0;
+    for (unsigned k = 0; k < count; ++k) {
+        BatchScene *sc = scene_of(b, ids[k], what);
+        if (!sc) return -1;
+        psdata *out = outs[k];
+        const int f = out && field ? get_field_psdata(*out, field) : -1;
+        if (f < 0 || psdata_data_size(*out) != sc->blob_size) {
+            sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field ? field : "");
+            return -1;
+        }
+        if (!sc->host || sc->host != static_cast<char *>(out->data)) {
+            sph_set_error("%s: scene %d's store is not pinned (sph_batch_pin_host)", what, ids[k]);
+            return -1;
+        }
+        const size_t off = out->data_offsets[f], sz = out->data_sizes[f];
+        segs[k] = CopySeg{sc->mem + off, nullptr, (unsigned long long)sz};
+        dst[k] = sc->host + off;
+        at[k] = total;
+        total += (sz + 15) / 16 * 16;
+        if (sz > max_bytes) max_bytes = sz;
+    }
+    const int t = (int)(b->tickets & 1);
+    // turn t's buffers are free once the read two tickets back has written
+    // the host stores (an event never recorded counts as complete)
+    if (!ok(cudaStreamWaitEvent(b->stream, b->read_done[t], 0), what)) return -1;
+    size_t seg_cap = b->snap_seg_cap[t];
+    if (!grow(&b->snap[t], &b->snap_cap[t], total ? total : 16, b->stream, what) ||
+        !grow(&b->snap_segs[t], &seg_cap, segs.size(), b->stream, what))
+        return -1;
+    b->snap_seg_cap[t] = (unsigned)seg_cap;
+    for (unsigned k = 0; k < count; ++k) segs[k].dst = b->snap[t] + at[k];
+    // turn t's pinned table was last uploaded before the snapshot two
+    // tickets back
+    if (!ok(cudaEventSynchronize(b->snap_done[t]), what)) return -1;
+    if (segs.size() > b->seg_host_cap[t]) {
+        if (b->seg_host[t]) cudaFreeHost(b->seg_host[t]);
+        b->seg_host[t] = nullptr;
+        b->seg_host_cap[t] = 0;
+        const size_t c = segs.size() * 2;
+        if (!ok(cudaMallocHost((void **)&b->seg_host[t], c * sizeof(CopySeg)), what)) return -1;
+        b->seg_host_cap[t] = c;
+    }
+    std::copy(segs.begin(), segs.end(), b->seg_host[t]);
+    if (!ok(cudaMemcpyAsync(b->snap_segs[t], b->seg_host[t], segs.size() * sizeof(CopySeg), cudaMemcpyHostToDevice,
+                            b->stream),
+            what))
+        return -1;
+    // the snapshot, in stream order after the substeps enqueued so far
+    sph_launch_copy_segments(b->snap_segs[t], count, max_bytes, b->stream);
+    if (!ok(cudaEventRecord(b->snap_done[t], b->stream), what) ||
+        !ok(cudaStreamWaitEvent(b->reads, b->snap_done[t], 0), what))
+        return -1;
+    // the host stores, written by the copy engines beside later substeps
+    // (a copy kernel's slow writes to host memory would hold SM slots the
+    // substeps need)
+    for (unsigned k = 0; k < count; ++k)
+        if (!ok(cudaMemcpyAsync(dst[k], b->snap[t] + at[k], segs[k].bytes, cudaMemcpyDeviceToHost, b->reads), what))
+            return -1;
+    if (!ok(cudaEventRecord(b->read_done[t], b->reads), what) || sph_check_launch(what) != cudaSuccess) return -1;
+    return b->tickets++;
+}
+
+extern "C" int sph_batch_wait_read(sph_batch *b, long long ticket) {
+    if (!b || ticket < 0 || ticket >= b->tickets) {
+        sph_set_error("sph_batch_wait_read: no such read");
+        return -1;
+    }
+    // the turn's event covers this read or a later one of the same turn,
+    // which the stream ordered after it
+    return ok(cudaEventSynchronize(b->read_done[ticket & 1]), "sph_batch_wait_read") ? 0 : -1;
+}
+
+extern "C" int sph_batch_wait_reads(sph_batch *b) {
+    if (!b) return -1;
+    return drain_reads(b, "sph_batch_wait_reads") ? 0 : -1;
 }
 
 namespace {

@@ -119,16 +119,37 @@ class Batch(object):
         """Copies one field of several scenes back with a single wait (one
         kernel for the pinned stores); returns their host views (sid ->
         array)."""
+        key, ids, outs = self._read_args(sids)
+        if bnd.sph_batch_read_field_many(self.handle, ids, len(key), name, outs) != 0:
+            raise bnd.SphError(bnd.last_error())
+        return {sid: self.scenes[sid].views[name] for sid in key}
+
+    def read_fields_async(self, sids, name):
+        """Enqueues a read of one field of several pinned scenes: a device
+        snapshot in stream order, written into their host stores while later
+        substeps run.  Returns a ticket for wait_read()."""
+        key, ids, outs = self._read_args(sids)
+        t = bnd.sph_batch_read_field_many_async(self.handle, ids, len(key), name, outs)
+        if t < 0:
+            raise bnd.SphError(bnd.last_error())
+        return t
+
+    def wait_read(self, ticket):
+        if bnd.sph_batch_wait_read(self.handle, ticket) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def wait_reads(self):
+        if bnd.sph_batch_wait_reads(self.handle) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def _read_args(self, sids):
         key = tuple(sids)
         if self._reads is None or self._reads[0] != key:
             # the argument arrays, kept while the same scenes are read
             ids = (ctypes.c_int * len(key))(*key)
             outs = (ctypes.POINTER(bnd.psdata) * len(key))(*[ctypes.pointer(self.scenes[s].psdata) for s in key])
             self._reads = (key, ids, outs)
-        _, ids, outs = self._reads
-        if bnd.sph_batch_read_field_many(self.handle, ids, len(key), name, outs) != 0:
-            raise bnd.SphError(bnd.last_error())
-        return {sid: self.scenes[sid].views[name] for sid in key}
+        return self._reads
 
     def profile(self, reps=3):
         """Mean device ms per phase of a substep (phases run one by one)."""

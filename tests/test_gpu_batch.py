@@ -207,6 +207,45 @@ def test_pinned_read_fields_one_kernel():
     b.close()
 
 
+def test_async_reads_are_snapshots():
+    """An asynchronous read holds the field as of its place in the stream,
+    although later substeps run while it is written; an unpinned store is
+    refused."""
+    from sph import bindings as bnd
+    scs = mix(seed=52)
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    for sid in ids:
+        b.pin(sid)
+    b.step(2)
+    t1 = b.read_fields_async(ids, "position")
+    b.step(3)
+    b.wait_read(t1)
+    snap = {sid: np.array(b.scenes[sid].views["position"]) for sid in ids}
+    ref = Batch()
+    rids = [ref.add(s) for s in scs]
+    ref.step(2)
+    want = ref.read_fields(rids, "position")
+    for sid, rid in zip(ids, rids):
+        assert np.array_equal(snap[sid], want[rid])
+    ref.close()
+    # several reads in flight, then all waited for
+    tickets = [b.read_fields_async(ids, "position")]
+    b.step(1)
+    tickets.append(b.read_fields_async(ids, "velocity"))
+    tickets.append(b.read_fields_async(ids, "position"))
+    b.wait_reads()
+    got = {sid: (np.array(b.scenes[sid].views["position"]), np.array(b.scenes[sid].views["velocity"])) for sid in ids}
+    for sid in ids:
+        full = b.read(sid)
+        assert np.array_equal(got[sid][0], full["position"])
+        assert np.array_equal(got[sid][1], full["velocity"])
+    b.unpin(ids[1])
+    with pytest.raises(bnd.SphError):
+        b.read_fields_async(ids, "position")
+    b.close()
+
+
 def test_ragged_and_empty_scenes_in_a_batch():
     """Scenes with fewer active particles than their capacity, and with none,
     run beside full ones: the ragged scene equals itself alone, the empty
