@@ -80,16 +80,16 @@ PHASE_BYTES = {
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
 # the dominant phase's kernel, from one ncu capture of the same workload
-# (profiles/fluid_pair_passes_wcsph-1m.md, profiles/solid_pair_passes_batched-256.md,
-# profiles/fluid_pair_passes_batched-256.md).
+# (profiles/fluid_pair_passes_wcsph-1m.md, profiles/fluid_pair_passes_batched-256.md,
+# profiles/solid_scan_passes_batched-256.md, profiles/solid_force_passes_batched-256.md).
 MEASURED_TRAFFIC = {
     ("wcsph-1m", "forces_fluids+step"): 110.94e6,         # k_forces_fluids_masked
-    ("batched-256", "density"): 319.52e6,                 # k_density<false> (writes the candidate masks too)
-    ("batched-256", "fluid forces+step"): 344.01e6,       # k_forces_fluids_masked
-    ("batched-256", "corotational rotations"): 170.85e6,  # k_rotations_and_strains
-    ("batched-256", "corotational forces"): 183.24e6,     # k_forces_solids<1, 1>
-    ("batched-256", "svk deformations"): 56.00e6,         # k_deformations
-    ("batched-256", "svk forces"): 138.18e6,              # k_forces_solids<0, 1>
+    ("batched-256", "density"): 245.84e6,                 # k_density<false> (writes the candidate masks too)
+    ("batched-256", "fluid forces+step"): 344.56e6,       # k_forces_fluids_masked
+    ("batched-256", "corotational rotations"): 140.75e6,  # k_rotations_and_strains
+    ("batched-256", "corotational forces"): 214.80e6,     # k_forces_solids<1, 1>
+    ("batched-256", "svk deformations"): 61.81e6,         # k_deformations
+    ("batched-256", "svk forces"): 138.10e6,              # k_forces_solids<0, 1>
 }
 
 
