@@ -88,6 +88,16 @@ __device__ __forceinline__ DistBounds dist_bounds(float h) {
 }
 
 // Kahan-compensated float accumulator.
+// 1/x from the special-function unit (rcp.approx.ftz.f32: at most 1 ulp
+// from the rounded reciprocal, denormals flushed).  One instruction in place
+// of the IEEE-rounded reciprocal's sequence; deterministic, so every walk of
+// a pair sum that uses it rounds alike.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 struct Kahan {
     float s = 0.f, c = 0.f;
     __device__ __forceinline__ void add(float x) {

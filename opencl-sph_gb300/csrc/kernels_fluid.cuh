@@ -203,7 +203,7 @@ __device__ __forceinline__ void fluid_pair(const FluidI &I, float3 jpos, float3 
     const float dist = __fmul_rn(r2, rinv);
     const float din = __fsub_rn(I.h, dist);
     const float pj = __fmul_rn(__fsub_rn(rhoj, I.rho0), I.stiff);
-    const float inv_didj = __frcp_rn(__fmul_rn(I.rhoi, rhoj));
+    const float inv_didj = rcp_approx(__fmul_rn(I.rhoi, rhoj));
     const float vterm = __fmul_rn(__fmul_rn(I.visc, din), I.kv);
     const float pterm = __fmul_rn(
         __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(-__fadd_rn(I.pi, pj), 0.5f), rinv), din), din), I.kv);
