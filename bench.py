@@ -61,21 +61,24 @@ PHASE_BYTES = {
     "gather": (0, 0),                 # no reference counterpart
     "density": (24, 8),               # compute_density + one stencil pass over the tables
     "forces_fluids+step": (120, 8),   # compute_forces_fluids 44 + step_forward 76
-    "rotations_and_strains": (168, 16),
-    "deformations": (64, 8),
+    # fused solid phases: the first pass also applies the stress law, the
+    # force pass also steps (separate stress and step phases only for
+    # scenes with symmetry planes)
+    "rotations_and_strains": (216, 16),  # 168 + compute_stresses 48
+    "deformations": (124, 8),            # 64 + compute_stresses 60
     "stresses": (48, 0),
-    "forces_solids": (160, 8),
+    "forces_solids+step": (236, 8),      # compute_forces_solids 160 + step_forward 76
     "step_forward": (76, 0),
     # batched-form phases (bench_batched): the same figures per material
     "fluid forces+step": (120, 8),
-    "corotational rotations": (168, 16),
+    "corotational rotations": (216, 16),
     "corotational stresses": (48, 0),
-    "corotational forces": (160, 8),
-    "corotational step": (76, 0),
-    "svk deformations": (64, 8),
+    "corotational forces+step": (236, 8),
+    "corotational step (planes)": (76, 0),
+    "svk deformations": (124, 8),
     "svk stresses": (60, 0),
-    "svk forces": (124, 8),
-    "svk step": (76, 0),
+    "svk forces+step": (200, 8),         # 124 + 76
+    "svk step (planes)": (76, 0),
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
@@ -86,10 +89,6 @@ MEASURED_TRAFFIC = {
     ("wcsph-1m", "forces_fluids+step"): 110.94e6,         # k_forces_fluids_masked
     ("batched-256", "density"): 245.84e6,                 # k_density<false> (writes the candidate masks too)
     ("batched-256", "fluid forces+step"): 344.56e6,       # k_forces_fluids_masked
-    ("batched-256", "corotational rotations"): 140.75e6,  # k_rotations_and_strains
-    ("batched-256", "corotational forces"): 214.80e6,     # k_forces_solids<1, 1>
-    ("batched-256", "svk deformations"): 61.81e6,         # k_deformations
-    ("batched-256", "svk forces"): 138.10e6,              # k_forces_solids<0, 1>
 }
 
 
@@ -386,9 +385,9 @@ def bench_batched(args, torch, world):
         by_mat[m][0] += b.scenes[sid].scene.n
         by_mat[m][1] += c
     counts = {"fluid forces+step": tuple(by_mat["fluid"])}
-    for ph in ("rotations", "stresses", "forces", "step"):
+    for ph in ("rotations", "stresses", "forces+step", "step (planes)"):
         counts["corotational " + ph] = tuple(by_mat["corot"])
-    for ph in ("deformations", "stresses", "forces", "step"):
+    for ph in ("deformations", "stresses", "forces+step", "step (planes)"):
         counts["svk " + ph] = tuple(by_mat["svk"])
     b.close()
     return {"scenes": scs, "n": n, "cells": cells, "counts": counts, "total_s": total_s, "clocks": clk,

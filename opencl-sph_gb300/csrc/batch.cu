@@ -230,11 +230,7 @@ bool rebuild(sph_batch *b) {
         if (m == MAT_FLUID) {
             sph_launch_forces_fluids(G.L, true, true);
         } else {
-            if (m == MAT_COROT) sph_launch_rotations_and_strains(G.L, true);
-            else sph_launch_deformations(G.L, true);
-            sph_launch_stresses(G.L, m == MAT_COROT, true);
-            sph_launch_forces_solids(G.L, m == MAT_COROT, true);
-            sph_launch_step_forward(G.L);
+            sph_launch_solid_passes(G.L, m == MAT_COROT);
         }
         if (m > 0) {
             cudaEventRecord(b->join[m - 1], G.L.stream);
@@ -695,6 +691,27 @@ struct PhaseLog {
 };
 }  // namespace
 
+// Phase names of the batched solid passes, by material: the first pass
+// goes under the material's name already marked.
+struct SolidMarks {
+    PhaseLog *log;
+    bool corot;
+    int seen;
+};
+static void solid_mark(void *ctx, const char *name) {
+    SolidMarks *m = static_cast<SolidMarks *>(ctx);
+    if (m->seen++ == 0 || !name) return;
+    static const char *kCorot[][2] = {{"stresses", "corotational stresses"},
+                                      {"forces_solids+step", "corotational forces+step"},
+                                      {"step_forward", "corotational step (planes)"}};
+    static const char *kSvk[][2] = {{"stresses", "svk stresses"},
+                                    {"forces_solids+step", "svk forces+step"},
+                                    {"step_forward", "svk step (planes)"}};
+    const char *(*names)[2] = m->corot ? kCorot : kSvk;
+    for (int k = 0; k < 3; ++k)
+        if (!strcmp(names[k][0], name)) m->log->mark(names[k][1]);
+}
+
 extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, const char **phase_names,
                                  unsigned max_phases) {
     if (!b) return -1;
@@ -725,14 +742,9 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
                 sph_launch_forces_fluids(G, true, true);
             } else {
                 const bool corot = m == MAT_COROT;
-                if (corot) sph_launch_rotations_and_strains(G, true);
-                else sph_launch_deformations(G, true);
-                log.mark(corot ? "corotational stresses" : "svk stresses");
-                sph_launch_stresses(G, corot, true);
-                log.mark(corot ? "corotational forces" : "svk forces");
-                sph_launch_forces_solids(G, corot, true);
-                log.mark(corot ? "corotational step" : "svk step");
-                sph_launch_step_forward(G);
+                // the first phase is named by kMat; the others by the material
+                SolidMarks sm{&log, corot, 0};
+                sph_launch_solid_passes(G, corot, solid_mark, &sm);
             }
         }
         if (A.num_rigid) {

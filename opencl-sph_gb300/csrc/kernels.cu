@@ -95,8 +95,9 @@ void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
             L.scenes, L.pair_particles, fuse_step ? 1 : 0);
 }
 
-void sph_launch_step_forward(const Launch &L) {
-    k_step_forward<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+void sph_launch_step_forward(const Launch &L, bool planes_only) {
+    k_step_forward<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles,
+                                                                                planes_only ? 1 : 0);
 }
 
 void sph_launch_plane_constraints(const Launch &L) {
@@ -107,42 +108,65 @@ void sph_launch_init_original_position(const Launch &L) {
     k_init_original_position<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
 }
 
-void sph_launch_rotations_and_strains(const Launch &L, bool with_density) {
+void sph_launch_rotations_and_strains(const Launch &L, bool with_density, bool with_stress) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0);
+    k_rotations_and_strains<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0,
+                                                              with_density && with_stress ? 1 : 0);
     if (!L.no_symmetry_planes)
         k_rotations_and_strains_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 
-void sph_launch_stresses(const Launch &L, bool corot, bool sorted) {
+void sph_launch_stresses(const Launch &L, bool corot, bool sorted, bool planes_only) {
     const unsigned g = grid_for(L.particles, L.grid_cap);
     if (sorted) {
-        if (corot) k_stresses_sorted<true><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
-        else k_stresses_sorted<false><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
+        if (corot) k_stresses_sorted<true><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles, planes_only ? 1 : 0);
+        else k_stresses_sorted<false><<<g, L.block, 0, L.stream>>>(L.scenes, L.particles, planes_only ? 1 : 0);
     } else {
         if (corot) k_stresses_corot<<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
         else k_stresses_svk<<<g, L.block, 0, L.stream>>>(L.scenes, L.particles);
     }
 }
 
-void sph_launch_deformations(const Launch &L, bool with_density) {
+void sph_launch_deformations(const Launch &L, bool with_density, bool with_stress) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0);
+    k_deformations<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, with_density ? 1 : 0,
+                                                     with_density && with_stress ? 1 : 0);
     if (!L.no_symmetry_planes) k_deformations_planes<<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
 }
 
-void sph_launch_forces_solids(const Launch &L, bool corot, bool masked) {
+void sph_launch_forces_solids(const Launch &L, bool corot, bool masked, bool fuse_step) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    const int step = masked && fuse_step ? 1 : 0;
     if (corot) {
-        if (masked) k_forces_solids<true, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
-        else k_forces_solids<true, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        if (masked) k_forces_solids<true, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        else k_forces_solids<true, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, 0);
         if (!L.no_symmetry_planes)
             k_forces_solids_planes<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
     } else {
-        if (masked) k_forces_solids<false, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
-        else k_forces_solids<false, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+        if (masked) k_forces_solids<false, true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        else k_forces_solids<false, false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, 0);
         if (!L.no_symmetry_planes)
             k_forces_solids_planes<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles);
+    }
+}
+
+void sph_launch_solid_passes(const Launch &L, bool corot, PhaseMark mark, void *ctx) {
+    auto phase = [&](const char *name) {
+        if (mark) mark(ctx, name);
+    };
+    const bool planes = !L.no_symmetry_planes;
+    phase(corot ? "rotations_and_strains" : "deformations");
+    if (corot) sph_launch_rotations_and_strains(L, true, true);
+    else sph_launch_deformations(L, true, true);
+    if (planes) {
+        phase("stresses");
+        sph_launch_stresses(L, corot, true, true);
+    }
+    phase("forces_solids+step");
+    sph_launch_forces_solids(L, corot, true, true);
+    if (planes) {
+        phase("step_forward");
+        sph_launch_step_forward(L, true);
     }
 }
 
@@ -207,19 +231,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
         phase(nullptr);
         return;
     }
-    if (mat == MAT_COROT) {
-        phase("rotations_and_strains");
-        sph_launch_rotations_and_strains(L, true);
-    } else {
-        phase("deformations");
-        sph_launch_deformations(L, true);
-    }
-    phase("stresses");
-    sph_launch_stresses(L, mat == MAT_COROT, true);
-    phase("forces_solids");
-    sph_launch_forces_solids(L, mat == MAT_COROT, true);
-    phase("step_forward");
-    sph_launch_step_forward(L);
+    sph_launch_solid_passes(L, mat == MAT_COROT, mark, ctx);
     if (L.num_rigid) {
         phase("rigid_bodies");
         sph_launch_rigid(L);

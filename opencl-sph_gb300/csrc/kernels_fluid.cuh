@@ -325,8 +325,10 @@ __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3
     st3(S.velocity, i, vn);
 }
 
-__global__ void k_step_forward(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void k_step_forward(const SceneDesc *__restrict__ scenes, BlockMap map, int planes_only) {
     SPH_FOR_WORK(map)
+    // a fused substep's plane-free solids were stepped by their force pass
+    if (planes_only && !S.num_symmetry_planes) continue;
     if (item < active_count(S)) {
         const unsigned i = item;
         integrate(S, i, ld3(S.force, i), ld3(S.velocity, i), ld3(S.position, i));

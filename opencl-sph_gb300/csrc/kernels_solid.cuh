@@ -323,23 +323,101 @@ __global__ void k_rotations_and_strains_planes(const SceneDesc *__restrict__ sce
     SPH_END_WORK
 }
 
+// Stress laws (solid_corotation.cl:197-208; solid_svk.cl:45-80).  Every
+// rounding is written out: the laws run in the named stress pass and inside
+// the fused first solid pass, and both must give the same bits.
+__device__ __forceinline__ float dot3_rn(float a0, float b0, float a1, float b1, float a2, float b2) {
+    return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, __fmul_rn(a0, b0)));
+}
+
+struct Lame {
+    float lam, mu2;  // lambda and 2 mu
+};
+__device__ __forceinline__ Lame lame(const SceneDesc &S) {
+    const float E = *S.youngs_modulus, nu = *S.poisson;
+    Lame L;
+    L.lam = __fdiv_rn(__fdiv_rn(__fmul_rn(E, nu), __fadd_rn(1.0f, nu)), __fsub_rn(1.0f, __fmul_rn(2.0f, nu)));
+    L.mu2 = __fmul_rn(2.0f, __fdiv_rn(__fdiv_rn(E, 2.0f), __fadd_rn(1.0f, nu)));
+    return L;
+}
+
+__device__ __forceinline__ void corot_stress(const SceneDesc &S, const float e[6], float o[6]) {
+    const Lame L = lame(S);
+    const float lt = __fmul_rn(L.lam, __fadd_rn(__fadd_rn(e[0], e[1]), e[2]));
+    for (int c = 0; c < 3; ++c) o[c] = __fmaf_rn(L.mu2, e[c], lt);
+    for (int c = 3; c < 6; ++c) o[c] = __fmul_rn(L.mu2, e[c]);
+}
+
+__device__ __forceinline__ void svk_stress(const SceneDesc &S, const float f[9], float o[6]) {
+    const Lame L = lame(S);
+    // Green strain G = (F^T F - I) / 2
+    auto ftf = [&](int r, int c) { return dot3_rn(f[r], f[c], f[3 + r], f[3 + c], f[6 + r], f[6 + c]); };
+    const float g[6] = {__fmaf_rn(0.5f, ftf(0, 0), -0.5f), __fmaf_rn(0.5f, ftf(1, 1), -0.5f),
+                        __fmaf_rn(0.5f, ftf(2, 2), -0.5f), __fmul_rn(0.5f, ftf(0, 1)),
+                        __fmul_rn(0.5f, ftf(0, 2)), __fmul_rn(0.5f, ftf(1, 2))};
+    const float first = __fmul_rn(L.lam, __fadd_rn(__fadd_rn(g[0], g[1]), g[2]));
+    const float sv[6] = {__fmaf_rn(L.mu2, g[0], first), __fmaf_rn(L.mu2, g[1], first), __fmaf_rn(L.mu2, g[2], first),
+                         __fmul_rn(L.mu2, g[3]), __fmul_rn(L.mu2, g[4]), __fmul_rn(L.mu2, g[5])};
+    // F S (S symmetric), then the Cauchy stress (F S F^T) / det F
+    const float S9[9] = {sv[0], sv[3], sv[4], sv[3], sv[1], sv[5], sv[4], sv[5], sv[2]};
+    float fs[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            fs[3 * r + c] = dot3_rn(f[3 * r], S9[c], f[3 * r + 1], S9[3 + c], f[3 * r + 2], S9[6 + c]);
+    const float c0 = __fsub_rn(__fmul_rn(f[4], f[8]), __fmul_rn(f[5], f[7]));
+    const float c1 = __fsub_rn(__fmul_rn(f[3], f[8]), __fmul_rn(f[5], f[6]));
+    const float c2 = __fsub_rn(__fmul_rn(f[3], f[7]), __fmul_rn(f[4], f[6]));
+    const float det = __fadd_rn(__fsub_rn(__fmul_rn(f[0], c0), __fmul_rn(f[1], c1)), __fmul_rn(f[2], c2));
+    const float rdet = __fdiv_rn(1.0f, det);
+    auto cau = [&](int r, int c) {
+        return __fmul_rn(dot3_rn(fs[3 * r], f[3 * c], fs[3 * r + 1], f[3 * c + 1], fs[3 * r + 2], f[3 * c + 2]), rdet);
+    };
+    o[0] = cau(0, 0);
+    o[1] = cau(1, 1);
+    o[2] = cau(2, 2);
+    o[3] = cau(0, 1);
+    o[4] = cau(0, 2);
+    o[5] = cau(1, 2);
+}
+
+// The corotational force pass uses a particle's rotation and stress only
+// as the product R sigma -- or, for a body particle, R alone (its pairs use
+// the partner's stress).  N = R sigma (row-major), or R for a body.
+__device__ __forceinline__ void corot_nmat(const float R[9], const float s[6], bool body, float N[9]) {
+    if (body) {
+        for (int c = 0; c < 9; ++c) N[c] = R[c];
+        return;
+    }
+    const float S9[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) N[3 * r + c] = dot3_rn(R[3 * r], S9[c], R[3 * r + 1], S9[3 + c], R[3 * r + 2], S9[6 + c]);
+}
+
+// A particle's stress into the field and the sorted copies: sstress[k]
+// (sigma with mass/density) and, for the corotational model, srot[k] = N
+// (with mass/density in w).
+__device__ __forceinline__ void store_stress(const SceneDesc &S, unsigned i, unsigned k, const float o[6], float mrho,
+                                             const float *R, bool body) {
+    for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)i + c] = o[c];
+    S.sstress[2 * (size_t)k] = make_float4(o[0], o[1], o[2], o[3]);
+    S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], mrho, 0.f);
+    if (R && S.srot) {
+        float N[9];
+        corot_nmat(R, o, body, N);
+        for (int c = 0; c < 3; ++c)
+            S.srot[3 * (size_t)k + c] = make_float4(N[3 * c], N[3 * c + 1], N[3 * c + 2], c == 0 ? mrho : 0.f);
+    }
+}
+
 // compute_stresses, corotational (solid_corotation.cl:9-26,197-208):
 // isotropic Hooke's law with the Lame constants.
 __global__ void k_stresses_corot(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
-        const float E = *S.youngs_modulus, nu = *S.poisson;
-        const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
-        const float mu = E / 2.0f / (1.0f + nu);
-        const float *e = S.strain + 6 * (size_t)item;
-        float *o = S.stress + 6 * (size_t)item;
-        const float tr = e[0] + e[1] + e[2];
-        o[0] = lam * tr + 2.0f * mu * e[0];
-        o[1] = lam * tr + 2.0f * mu * e[1];
-        o[2] = lam * tr + 2.0f * mu * e[2];
-        o[3] = 2.0f * mu * e[3];
-        o[4] = 2.0f * mu * e[4];
-        o[5] = 2.0f * mu * e[5];
+        float e[6], o[6];
+        for (int c = 0; c < 6; ++c) e[c] = S.strain[6 * (size_t)item + c];
+        corot_stress(S, e, o);
+        for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)item + c] = o[c];
     }
     SPH_END_WORK
 }
@@ -405,31 +483,10 @@ __global__ void k_deformations_planes(const SceneDesc *__restrict__ scenes, Bloc
 __global__ void k_stresses_svk(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
-        const float E = *S.youngs_modulus, nu = *S.poisson;
-        const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
-        const float mu = E / 2.0f / (1.0f + nu);
-        const float *F = S.deformation + 9 * (size_t)item;
-        float f[9];
-        for (int c = 0; c < 9; ++c) f[c] = F[c];
-        auto ftf = [&](int r, int c) { return f[r] * f[c] + f[3 + r] * f[3 + c] + f[6 + r] * f[6 + c]; };
-        float g[6] = {0.5f * ftf(0, 0) - 0.5f, 0.5f * ftf(1, 1) - 0.5f, 0.5f * ftf(2, 2) - 0.5f,
-                      0.5f * ftf(0, 1), 0.5f * ftf(0, 2), 0.5f * ftf(1, 2)};
-        const float first = lam * (g[0] + g[1] + g[2]);
-        float sv[6] = {first + 2.0f * mu * g[0], first + 2.0f * mu * g[1], first + 2.0f * mu * g[2],
-                       2.0f * mu * g[3], 2.0f * mu * g[4], 2.0f * mu * g[5]};
-        float fs[9];
-        mul_as(f, sv, fs);
-        const float det = f[0] * (f[4] * f[8] - f[5] * f[7]) - f[1] * (f[3] * f[8] - f[5] * f[6]) +
-                          f[2] * (f[3] * f[7] - f[4] * f[6]);
-        const float rdet = 1.0f / det;
-        auto cau = [&](int r, int c) { return (fs[3 * r] * f[3 * c] + fs[3 * r + 1] * f[3 * c + 1] + fs[3 * r + 2] * f[3 * c + 2]) * rdet; };
-        float *o = S.stress + 6 * (size_t)item;
-        o[0] = cau(0, 0);
-        o[1] = cau(1, 1);
-        o[2] = cau(2, 2);
-        o[3] = cau(0, 1);
-        o[4] = cau(0, 2);
-        o[5] = cau(1, 2);
+        float f[9], o[6];
+        for (int c = 0; c < 9; ++c) f[c] = S.deformation[9 * (size_t)item + c];
+        svk_stress(S, f, o);
+        for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)item + c] = o[c];
     }
     SPH_END_WORK
 }
@@ -615,7 +672,7 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
 // At most 80 registers (96 unbounded; 32 bytes spill to L1): six blocks per
 // SM instead of five (0.707 -> 0.670 ms on batched-256).
 __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map,
-                                                        int with_density) {
+                                                        int with_density, int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
     if (item < active_count(S)) {
@@ -673,13 +730,22 @@ __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restr
             st[4] = 0.5f * (D[2] + D[6]);
             st[5] = 0.5f * (D[5] + D[7]);
         }
+        if (with_stress && S.sstress) {
+            // compute_stresses for this particle, as k_stresses_sorted<true>
+            // would (a body particle keeps its strain)
+            float e[6], o[6];
+            for (int c = 0; c < 6; ++c) e[c] = S.strain[6 * (size_t)i + c];
+            corot_stress(S, e, o);
+            store_stress(S, i, k, o, __fdiv_rn(C.mass, S.sdens[k]), R, __float_as_uint(q4.w) > 0);
+        }
     }
     SPH_END_WORK
 }
 
 // compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
 // the sorted copies, recording the candidate masks.
-__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density) {
+__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density,
+                               int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
     if (item < active_count(S)) {
@@ -716,69 +782,24 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
         float F[9];
         mul_as(apq, inv, F);
         for (int c = 0; c < 9; ++c) S.deformation[9 * (size_t)i + c] = F[c];
+        if (with_stress && S.sstress) {
+            // compute_stresses for this particle, as k_stresses_sorted<false> would
+            float o[6];
+            svk_stress(S, F, o);
+            store_stress(S, i, k, o, __fdiv_rn(C.mass, S.sdens[k]), nullptr, false);
+        }
     }
     SPH_END_WORK
-}
-
-// Stress laws (solid_corotation.cl:197-208; solid_svk.cl:45-80).
-__device__ __forceinline__ void corot_stress(const SceneDesc &S, const float e[6], float o[6]) {
-    const float E = *S.youngs_modulus, nu = *S.poisson;
-    const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
-    const float mu = E / 2.0f / (1.0f + nu);
-    const float tr = e[0] + e[1] + e[2];
-    o[0] = lam * tr + 2.0f * mu * e[0];
-    o[1] = lam * tr + 2.0f * mu * e[1];
-    o[2] = lam * tr + 2.0f * mu * e[2];
-    o[3] = 2.0f * mu * e[3];
-    o[4] = 2.0f * mu * e[4];
-    o[5] = 2.0f * mu * e[5];
-}
-
-__device__ __forceinline__ void svk_stress(const SceneDesc &S, const float f[9], float o[6]) {
-    const float E = *S.youngs_modulus, nu = *S.poisson;
-    const float lam = E * nu / (1.0f + nu) / (1.0f - 2.0f * nu);
-    const float mu = E / 2.0f / (1.0f + nu);
-    auto ftf = [&](int r, int c) { return f[r] * f[c] + f[3 + r] * f[3 + c] + f[6 + r] * f[6 + c]; };
-    float g[6] = {0.5f * ftf(0, 0) - 0.5f, 0.5f * ftf(1, 1) - 0.5f, 0.5f * ftf(2, 2) - 0.5f,
-                  0.5f * ftf(0, 1), 0.5f * ftf(0, 2), 0.5f * ftf(1, 2)};
-    const float first = lam * (g[0] + g[1] + g[2]);
-    float sv[6] = {first + 2.0f * mu * g[0], first + 2.0f * mu * g[1], first + 2.0f * mu * g[2],
-                   2.0f * mu * g[3], 2.0f * mu * g[4], 2.0f * mu * g[5]};
-    float fs[9];
-    mul_as(f, sv, fs);
-    const float det = f[0] * (f[4] * f[8] - f[5] * f[7]) - f[1] * (f[3] * f[8] - f[5] * f[6]) +
-                      f[2] * (f[3] * f[7] - f[4] * f[6]);
-    const float rdet = 1.0f / det;
-    auto cau = [&](int r, int c) {
-        return (fs[3 * r] * f[3 * c] + fs[3 * r + 1] * f[3 * c + 1] + fs[3 * r + 2] * f[3 * c + 2]) * rdet;
-    };
-    o[0] = cau(0, 0);
-    o[1] = cau(1, 1);
-    o[2] = cau(2, 2);
-    o[3] = cau(0, 1);
-    o[4] = cau(0, 2);
-    o[5] = cau(1, 2);
-}
-
-// The corotational force pass uses a particle's rotation and stress only
-// as the product R sigma -- or, for a body particle, R alone (its pairs use
-// the partner's stress).  N = R sigma (row-major), or R for a body.
-__device__ __forceinline__ void corot_nmat(const float R[9], const float s[6], bool body, float N[9]) {
-    if (body) {
-        for (int c = 0; c < 9; ++c) N[c] = R[c];
-        return;
-    }
-    const float S9[9] = {s[0], s[3], s[4], s[3], s[1], s[5], s[4], s[5], s[2]};
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) N[3 * r + c] = R[3 * r] * S9[c] + R[3 * r + 1] * S9[3 + c] + R[3 * r + 2] * S9[6 + c];
 }
 
 // compute_stresses in a fused substep: per sorted particle k, the field
 // stress[i] and the sorted copies sstress[k] (with mass/density) and, for
 // the corotational model, srot[k] = N (with mass/density in w).
 template <bool COROT>
-__global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap map, int planes_only) {
     SPH_FOR_WORK(map)
+    // a plane-free scene's first pass stored its stresses already
+    if (planes_only && !S.num_symmetry_planes) continue;
     if (item < active_count(S) && S.sstress) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
@@ -792,16 +813,13 @@ __global__ void k_stresses_sorted(const SceneDesc *__restrict__ scenes, BlockMap
             for (int c = 0; c < 9; ++c) f[c] = S.deformation[9 * (size_t)i + c];
             svk_stress(S, f, o);
         }
-        for (int c = 0; c < 6; ++c) S.stress[6 * (size_t)i + c] = o[c];
         const float mrho = __fdiv_rn(*S.mass, S.sdens[k]);
-        S.sstress[2 * (size_t)k] = make_float4(o[0], o[1], o[2], o[3]);
-        S.sstress[2 * (size_t)k + 1] = make_float4(o[4], o[5], mrho, 0.f);
-        if (COROT && S.srot) {
-            float R[9], N[9];
+        if (COROT) {
+            float R[9];
             for (int c = 0; c < 9; ++c) R[c] = S.rotation[9 * (size_t)i + c];
-            corot_nmat(R, o, S.body_number[i] > 0, N);
-            for (int c = 0; c < 3; ++c)
-                S.srot[3 * (size_t)k + c] = make_float4(N[3 * c], N[3 * c + 1], N[3 * c + 2], c == 0 ? mrho : 0.f);
+            store_stress(S, i, k, o, mrho, R, S.body_number[i] > 0);
+        } else {
+            store_stress(S, i, k, o, mrho, nullptr, false);
         }
     }
     SPH_END_WORK
@@ -917,7 +935,7 @@ __device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidI &I
 // SM instead of five keep more gathers in flight in this latency-bound pass
 // (corotational 0.415 -> 0.383 ms, SVK 0.379 -> 0.344 ms on batched-256).
 template <bool COROT, bool MASKED>
-__global__ void __maxnreg__(80) k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map) {
+__global__ void __maxnreg__(80) k_forces_solids(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || (MASKED && !S.sstress)) continue;
     if (item < active_count(S)) {
@@ -950,6 +968,9 @@ __global__ void __maxnreg__(80) k_forces_solids(const SceneDesc *__restrict__ sc
         st3(S.force_elastic, i, fe);
         st3(S.force_viscous, i, fv);
         st3(S.cutoff_force, i, fe_s.get() * 0.5f + fv_s.get() * visc);
+        // step_forward for this particle, from the sorted copies of its
+        // position and velocity, which nothing has changed since the gather
+        if (MASKED && fuse_step) integrate(S, i, fe + fv, I.side.vel, I.side.pos);
     }
     SPH_END_WORK
 }

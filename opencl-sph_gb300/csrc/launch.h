@@ -50,16 +50,24 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid = false)
 // sums its density
 void sph_launch_density(const Launch &L, bool original, bool mask = false, bool skip_solids = false);
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked = false);
-void sph_launch_step_forward(const Launch &L);
+// planes_only: skip plane-free scenes (a fused substep's solid force pass
+// stepped them)
+void sph_launch_step_forward(const Launch &L, bool planes_only = false);
 void sph_launch_plane_constraints(const Launch &L);
 void sph_launch_init_original_position(const Launch &L);
-// with_density: also the density pass's sums (fused substeps)
-void sph_launch_rotations_and_strains(const Launch &L, bool with_density = false);
-// sorted: a fused substep's stress pass, which also fills the sorted copy
-void sph_launch_stresses(const Launch &L, bool corot, bool sorted = false);
-void sph_launch_deformations(const Launch &L, bool with_density = false);
-// masked: a fused substep's force pass over the first pair pass's masks
-void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false);
+// with_density: also the density pass's sums (fused substeps); with_stress:
+// also the stress law and the sorted stress copies of plane-free scenes
+// (fused substeps, with_density too)
+void sph_launch_rotations_and_strains(const Launch &L, bool with_density = false, bool with_stress = false);
+// sorted: a fused substep's stress pass, which also fills the sorted copy;
+// planes_only: only scenes with symmetry planes (the first pass stored the
+// others' stresses)
+void sph_launch_stresses(const Launch &L, bool corot, bool sorted = false, bool planes_only = false);
+void sph_launch_deformations(const Launch &L, bool with_density = false, bool with_stress = false);
+// masked: a fused substep's force pass over the first pair pass's masks;
+// fuse_step: also step_forward for the plane-free scenes it covers
+void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false, bool fuse_step = false);
+
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);
 void sph_launch_populate_cuboid(const Launch &L, const float c1[3], const float c2[3], const unsigned size[3]);
@@ -105,6 +113,11 @@ void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long
 // before the phase is enqueued and with nullptr after the last one.
 typedef void (*PhaseMark)(void *ctx, const char *phase);
 void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark = nullptr, void *ctx = nullptr);
+// A fused substep's solid passes after the density pass: the first pass
+// (with the density sums and the stresses), the forces with the step, and
+// the separate stress and step passes for scenes with symmetry planes.
+// `mark` names each phase.
+void sph_launch_solid_passes(const Launch &L, bool corot, PhaseMark mark = nullptr, void *ctx = nullptr);
 
 // One-time kernel attributes (call outside any stream capture).
 cudaError_t sph_prepare_kernels();

@@ -246,6 +246,30 @@ def test_async_reads_are_snapshots():
     b.close()
 
 
+def test_solids_with_and_without_planes_in_one_batch():
+    """A solid with symmetry planes takes the separate stress and step
+    passes; the plane-free solids beside it in the same launches take the
+    fused ones.  Each scene equals itself alone."""
+    pl = scenes.solid_lattice(5, 5, 7, material="corot", youngs_modulus=3e4, jitter=1e-4, seed=71, clamp_layers=1,
+                              name="planes")
+    pl.entries = [("symmetry_planes", "3, 2, 3", "float", None) if e[0] == "symmetry_planes" else e
+                  for e in pl.entries]
+    sp = np.zeros((3, 2, 3), np.float32)
+    for k in range(3):
+        sp[k, 1, k] = 1.0
+    pl.init = dict(pl.init, symmetry_planes=sp)
+    scs = [pl] + mix(seed=72)
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    b.step(12)
+    for sc, sid in zip(scs, ids):
+        pos, vel = alone(sc, 12)
+        v = b.read(sid)
+        assert np.array_equal(v["position"][: sc.n], pos), sc.name
+        assert np.array_equal(v["velocity"][: sc.n], vel), sc.name
+    b.close()
+
+
 def test_ragged_and_empty_scenes_in_a_batch():
     """Scenes with fewer active particles than their capacity, and with none,
     run beside full ones: the ragged scene equals itself alone, the empty

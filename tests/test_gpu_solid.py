@@ -108,13 +108,16 @@ def test_solid_kernels(material, planes):
     ps.close()
 
 
+@pytest.mark.parametrize("planes", [False, True])
 @pytest.mark.parametrize("material", ["corot", "svk"])
-def test_solid_trajectory(material):
-    sc, ps = _solid(material, False, jitter=1e-4)
-    ps2 = sc.system()
+def test_solid_trajectory(material, planes):
+    """The named recipe and the fused substep (first pass with the density
+    and the stresses, forces with the step; separate stress and step passes
+    for scenes with planes) agree bit for bit, and with the oracle."""
+    sc, ps = _solid(material, planes, jitter=1e-4)
+    _, ps2 = _solid(material, planes, jitter=1e-4)
     orc = oracle_of(ps)
     _setup_both(ps, orc)
-    ps2.set_fields(velocity=ps.get_fields("velocity")[0])
     ps2.call_for_all_particles("init_original_position")
     ps2.compute_particle_bins()
     ps2.call_for_all_particles("compute_original_density")
