@@ -46,15 +46,13 @@ void sph_launch_count(const Launch &L) {
 }
 
 void sph_launch_scan(const Launch &L) {
-    k_scan_tiles<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
-    unsigned g = L.num_scenes < L.grid_cap ? L.num_scenes : L.grid_cap;
-    k_scan_sums<<<g ? g : 1, 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
-    k_scan_add<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
+    k_scan_reduce<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
+    k_scan_down<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
 }
 
 void sph_launch_insert(const Launch &L) {
     k_scatter<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
-    k_sort_cells<<<grid_for(L.cells, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.cells);
+    k_rank_cells<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
     // crowded cells are rare: a few blocks per scene walk its queue
     const unsigned gy = L.num_scenes < 65535u ? (L.num_scenes ? L.num_scenes : 1u) : 65535u;
     k_sort_big_cells<<<dim3(L.num_scenes > 1 ? 4 : 32, gy), 1024, 0, L.stream>>>(L.scenes, L.num_scenes);

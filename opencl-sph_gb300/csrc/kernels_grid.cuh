@@ -85,7 +85,7 @@ __global__ void k_count_only(const SceneDesc *__restrict__ scenes, BlockMap map)
 }
 
 // ---- segmented exclusive scan of gridcount -> celloffset (prefix_sum,
-// common.cl:409-515, restated as a correct three-phase scan) -----------------
+// common.cl:409-515, restated as a correct two-phase scan) -------------------
 
 // Block-wide exclusive scan of one value per thread; returns the exclusive
 // prefix and writes the block total to *total.
@@ -115,102 +115,106 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned *t
     return before + x - v;
 }
 
-// Phase 1: each block scans SPH_SCAN_TILE cells locally.
-__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_tiles(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// Phase 1: each tile's total, from coalesced loads.
+__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_reduce(const SceneDesc *__restrict__ scenes,
+                                                                  BlockMap map) {
     for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
         const BlockWork bw = map.work[vb];
         const SceneDesc &S = scenes[bw.scene];
         if (scene_idle(S)) continue;
-        const unsigned per = SPH_SCAN_TILE / SPH_SCAN_THREADS;
-        const unsigned c0 = bw.first + threadIdx.x * per;
-        unsigned v[SPH_SCAN_TILE / SPH_SCAN_THREADS];
+        const unsigned end = min(bw.first + SPH_SCAN_TILE, S.num_cells);
         unsigned sum = 0;
-        for (unsigned k = 0; k < per; ++k) {
-            unsigned c = c0 + k;
-            v[k] = c < S.num_cells ? S.gridcount[c] : 0u;
-            sum += v[k];
-        }
+        for (unsigned c = bw.first + threadIdx.x; c < end; c += blockDim.x) sum += S.gridcount[c];
         unsigned total;
-        unsigned run = block_exclusive_scan(sum, &total);
-        for (unsigned k = 0; k < per; ++k) {
-            unsigned c = c0 + k;
-            if (c < S.num_cells) S.celloffset[c] = run;
-            run += v[k];
-        }
+        block_exclusive_scan(sum, &total);
         if (threadIdx.x == 0) S.scan_sums[bw.first / SPH_SCAN_TILE] = total;
     }
 }
 
-// Phase 2: one block per scene scans that scene's tile totals in place.
-__global__ void __launch_bounds__(1024) k_scan_sums(const SceneDesc *__restrict__ scenes, unsigned num_scenes) {
-    for (unsigned s = blockIdx.x; s < num_scenes; s += gridDim.x) {
-        const SceneDesc &S = scenes[s];
-        if (scene_idle(S)) continue;
-        unsigned carry = 0;
-        for (unsigned base = 0; base < S.num_scan_blocks; base += blockDim.x) {
-            unsigned i = base + threadIdx.x;
-            unsigned v = i < S.num_scan_blocks ? S.scan_sums[i] : 0u;
-            unsigned total;
-            unsigned ex = block_exclusive_scan(v, &total);
-            if (i < S.num_scan_blocks) S.scan_sums[i] = carry + ex;
-            carry += total;
-        }
-    }
-}
-
-// Phase 3: add each tile's prefix.
-__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_add(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// Phase 2: each tile adds up the totals of its scene's earlier tiles, then
+// scans its cells through shared memory (coalesced loads and stores).
+__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_down(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    __shared__ unsigned tile[SPH_SCAN_TILE];
+    constexpr unsigned per = SPH_SCAN_TILE / SPH_SCAN_THREADS;
     for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
         const BlockWork bw = map.work[vb];
         const SceneDesc &S = scenes[bw.scene];
         if (scene_idle(S)) continue;
-        const unsigned add = S.scan_sums[bw.first / SPH_SCAN_TILE];
-        if (add == 0) continue;
-        for (unsigned c = bw.first + threadIdx.x; c < bw.first + SPH_SCAN_TILE && c < S.num_cells; c += blockDim.x)
-            S.celloffset[c] += add;
+        const unsigned t = bw.first / SPH_SCAN_TILE;
+        unsigned part = 0;
+        for (unsigned j = threadIdx.x; j < t; j += blockDim.x) part += S.scan_sums[j];
+        unsigned base;
+        block_exclusive_scan(part, &base);
+        const unsigned end = min(bw.first + SPH_SCAN_TILE, S.num_cells);
+        for (unsigned k = threadIdx.x; k < SPH_SCAN_TILE; k += blockDim.x) {
+            const unsigned c = bw.first + k;
+            tile[k] = c < end ? S.gridcount[c] : 0u;
+        }
+        __syncthreads();
+        unsigned v[per], sum = 0;
+#pragma unroll
+        for (unsigned j = 0; j < per; ++j) {
+            v[j] = tile[threadIdx.x * per + j];
+            sum += v[j];
+        }
+        unsigned total;
+        unsigned run = base + block_exclusive_scan(sum, &total);
+#pragma unroll
+        for (unsigned j = 0; j < per; ++j) {
+            tile[threadIdx.x * per + j] = run;
+            run += v[j];
+        }
+        __syncthreads();
+        for (unsigned k = threadIdx.x; bw.first + k < end; k += blockDim.x) S.celloffset[bw.first + k] = tile[k];
+        __syncthreads();  // the next tile reuses `tile`
     }
 }
 
 // insert_particles_in_bin_array (common.cl:523-529) without atomics: each
-// particle goes to celloffset[cell] + its arrival slot.
+// particle goes to celloffset[cell] + its arrival slot, in arrival order,
+// of an unsorted copy of cellparticles: the first pnum words of the sorted
+// position buffer, which is free until the gather.
+__device__ __forceinline__ unsigned *unsorted_cells(const SceneDesc &S) { return reinterpret_cast<unsigned *>(S.spos); }
+
 __global__ void k_scatter(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
         const unsigned cell = S.gridcell[item];
         if (cell < S.num_cells) {
             const unsigned dst = S.celloffset[cell] + S.slot[item];
-            if (dst < S.pnum) S.cellparticles[dst] = item;
+            if (dst < S.pnum) unsorted_cells(S)[dst] = item;
         }
     }
     SPH_END_WORK
 }
 
-// Canonical order inside each cell: ascending particle index.  Cells of up
-// to SPH_SMALL_CELL particles are insertion-sorted by one thread; larger
-// cells are queued for k_sort_big_cells.
-__global__ void k_sort_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// Canonical order inside each cell: ascending particle index.  One thread
+// per slot of the unsorted copy: its particle's place in the cell is the
+// number of the cell's particles with a smaller index.  Cells of more than
+// SPH_SMALL_CELL particles are copied as they are and queued (by the thread
+// of their first slot) for k_sort_big_cells.
+__global__ void k_rank_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
-    if (item < S.num_cells) {
-        const unsigned cnt = S.gridcount[item];
-        const unsigned off = S.celloffset[item];
-        if (off > S.pnum || cnt > S.pnum - off) {
-            // inconsistent tables (only from host-written garbage): leave it
-        } else if (cnt > SPH_SMALL_CELL) {
-            unsigned k = atomicAdd(S.big_cells, 1u);
-            S.big_cells[1 + k] = item;
-        } else if (cnt > 1) {
-            unsigned *seg = S.cellparticles + off;
-            unsigned v[SPH_SMALL_CELL];
-            for (unsigned a = 0; a < cnt; ++a) {
-                unsigned x = seg[a];
-                unsigned b = a;
-                while (b > 0 && v[b - 1] > x) {
-                    v[b] = v[b - 1];
-                    --b;
+    if (item < active_count(S)) {
+        const unsigned *U = unsorted_cells(S);
+        const unsigned x = U[item];
+        const unsigned cell = x < S.pnum ? S.gridcell[x] : 0xffffffffu;
+        if (cell < S.num_cells) {
+            const unsigned off = S.celloffset[cell], cnt = S.gridcount[cell];
+            // inconsistent tables come only from host-written garbage: skip
+            if (off <= item && item - off < cnt && cnt <= S.pnum - off) {
+                if (cnt > SPH_SMALL_CELL) {
+                    S.cellparticles[item] = x;
+                    if (item == off) {
+                        const unsigned k = atomicAdd(S.big_cells, 1u);
+                        S.big_cells[1 + k] = cell;
+                    }
+                } else {
+                    unsigned r = 0;
+                    for (unsigned a2 = 0; a2 < cnt; ++a2) r += U[off + a2] < x;
+                    S.cellparticles[off + r] = x;
                 }
-                v[b] = x;
             }
-            for (unsigned a = 0; a < cnt; ++a) seg[a] = v[a];
         }
     }
     SPH_END_WORK
