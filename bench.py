@@ -79,6 +79,8 @@ PHASE_BYTES = {
     "svk stresses": (60, 0),
     "svk forces+step": (200, 8),         # 124 + 76
     "svk step (planes)": (76, 0),
+    "corotational density (planes)": (24, 8),
+    "svk density (planes)": (24, 8),
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
@@ -388,7 +390,9 @@ def bench_batched(args, torch, world):
         m = b.scenes[sid].scene.material
         by_mat[m][0] += b.scenes[sid].scene.n
         by_mat[m][1] += c
-    counts = {"fluid forces+step": tuple(by_mat["fluid"])}
+    # the density pass covers the fluid scenes (a plane-free solid's first
+    # pass sums its own density)
+    counts = {"fluid forces+step": tuple(by_mat["fluid"]), "density": tuple(by_mat["fluid"])}
     for ph in ("rotations", "stresses", "forces+step", "step (planes)"):
         counts["corotational " + ph] = tuple(by_mat["corot"])
     for ph in ("deformations", "stresses", "forces+step", "step (planes)"):
