@@ -492,7 +492,8 @@ def bench_served(args):
     from sph.serving import Server, poisson_requests, release, sequential_fifo
 
     def make(rng, i):
-        return scenes.mixed_scene(rng, i, n_range=(2000, 262144), prefix="q")
+        # built on the device at admission (sph_batch_add_lattice)
+        return scenes.mixed_scene(rng, i, n_range=(2000, 262144), prefix="q", jitter_hash=True)
     reqs = poisson_requests(rate=50.0, duration=args.served_seconds, make_scene=make, steps_range=(100, 2000),
                             seed=args.seed)
     srv = Server(budget_bytes=150e9, max_chunk=25, max_particles=8 << 20, keep_results=False)
@@ -509,8 +510,8 @@ def bench_served(args):
             "busy_throughput": st["busy_throughput"], "chunk_profile": _chunk_profile(st["chunk_log"]),
             "requests_with_bad_status": st["status_failed"],
             "offered_load": demand, "saturated": bool(demand > st["throughput"]),
-            "policy": "FIFO admission by 150 GB HBM budget and 8M resident particles; device-side substep "
-                      "quotas; chunks of up to 25 substeps",
+            "policy": "FIFO admission by 150 GB HBM budget and 8M resident particles; scenes built on the "
+                      "device at admission; device-side substep quotas; chunks of up to 25 substeps",
             "sequential_plain_model": {"throughput": seq["throughput"], "p50_s": seq["p50_s"],
                                        "p99_s": seq["p99_s"],
                                        "how": "FIFO queue of one-at-a-time drop-in solves (sph_update loops), "

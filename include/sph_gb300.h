@@ -249,6 +249,28 @@ size_t sph_scene_bytes(psdata *scene, const char *file_list);
 /* Uploads a scene (its current host values) and, for solids, runs the
  * setup of scripts/sph/systems.py:185-192.  Returns its id (>= 0) or -1. */
 int sph_batch_add(sph_batch *batch, psdata *scene, const char *file_list);
+/* A jittered lattice scene built on the device.  Particle p sits at
+ * lattice point (p % nx, p / nx % ny, p / (nx ny)) * spacing + origin, each
+ * coordinate plus jitter * (2u - 1) with u = splitmix64(seed * 2^32 + 3p +
+ * axis) / 2^64 (its top 53 bits), computed in IEEE double and rounded to
+ * float; sph/scenes.py's lattice(hash_seed=...) gives the same floats on
+ * the host.  The first clamp_layers * nx * ny particles get body_number 1
+ * (where the field exists); identity_rotation sets every rotation to I. */
+typedef struct {
+    unsigned int nx, ny, nz;
+    unsigned int clamp_layers;
+    unsigned int identity_rotation;
+    double spacing, jitter;
+    double origin[3];
+    unsigned long long seed;
+} sph_lattice;
+/* sph_batch_add for a lattice scene built on the device: `scene` is a
+ * freshly built host store (build_psdata) of at least nx ny nz particles.
+ * Its fields of at most 4096 bytes (the conf's scalars and small arrays,
+ * n, body_dynamic) are copied; the larger fields start at zero, as in a
+ * freshly built store, except position, n (and body_number, rotation),
+ * which `gen` writes.  The large host fields are never read or uploaded. */
+int sph_batch_add_lattice(sph_batch *batch, psdata *scene, const char *file_list, const sph_lattice *gen);
 /* Releases a scene's device memory (stream-ordered). */
 int sph_batch_remove(sph_batch *batch, int id);
 /* Advances every scene of the batch by num_steps substeps. */

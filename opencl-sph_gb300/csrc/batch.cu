@@ -2,10 +2,14 @@
 // device, advanced together by segment-aware launches captured in one
 // CUDA graph per substep (see the sph_batch_* declarations in sph_gb300.h).
 //
-// Memory is stream-ordered (cudaMallocAsync/cudaFreeAsync on the batch's
-// stream), so adding or retiring a scene never synchronises the device and
-// work already queued keeps running: this is what lets the serving loop
-// admit requests while others are on the GPU.
+// Memory is stream-ordered (allocations from the batch's own pool and
+// cudaFreeAsync on the batch's stream), so adding or retiring a scene never
+// synchronises the device and work already queued keeps running: this is
+// what lets the serving loop admit requests while others are on the GPU.
+// The pool keeps what retired scenes freed for the next admissions (its
+// release threshold is unbounded): the default pool would hand it back to
+// the driver at every synchronisation and map it again for the next scene,
+// which cost about 6 ms per admission.
 #include <string.h>
 
 #include <algorithm>
@@ -47,9 +51,12 @@ struct GroupLaunch {
 
 }  // namespace
 
+
 struct sph_batch {
+    cudaMemPool_t pool = nullptr;  // every device allocation of the batch
     cudaStream_t stream = nullptr;
     cudaStream_t side[2] = {nullptr, nullptr};
+
     cudaEvent_t fork = nullptr, join[2] = {nullptr, nullptr};
     std::vector<BatchScene *> slots;
     bool dirty = true;
@@ -76,6 +83,11 @@ struct sph_batch {
     size_t seg_host_cap[2] = {0, 0};
     long long tickets = 0;  // reads enqueued so far
 };
+
+// A stream-ordered allocation from the batch's pool.
+static bool balloc(sph_batch *b, void **p, size_t bytes, cudaStream_t stream, const char *what) {
+    return ok(cudaMallocFromPoolAsync(p, bytes, b->pool, stream), what);
+}
 
 namespace {
 
@@ -116,7 +128,7 @@ bool solid_setup(sph_batch *b, BatchScene *sc) {
     size_t o_c = t.add(m.cells.data(), m.cells.size() * sizeof(BlockWork));
     size_t o_s = t.add(m.scan.data(), m.scan.size() * sizeof(BlockWork));
     char *d = nullptr;
-    if (!ok(cudaMallocAsync(&d, t.host.size(), b->stream), "cudaMallocAsync(setup)")) return false;
+    if (!balloc(b, (void **)&d, t.host.size(), b->stream, "scene setup tables")) return false;
     if (!ok(cudaMemcpyAsync(d, t.host.data(), t.host.size(), cudaMemcpyHostToDevice, b->stream), "setup upload"))
         return false;
     Launch L{};
@@ -183,7 +195,7 @@ bool rebuild(sph_batch *b) {
         o_gp[m] = t.add(g[m].particles.data(), g[m].particles.size() * sizeof(BlockWork));
         o_gpp[m] = t.add(g[m].pair_particles.data(), g[m].pair_particles.size() * sizeof(BlockWork));
     }
-    if (!ok(cudaMallocAsync(&b->tables, t.host.size(), b->stream), "cudaMallocAsync(batch tables)")) return false;
+    if (!balloc(b, (void **)&b->tables, t.host.size(), b->stream, "batch tables")) return false;
     b->table_bytes = t.host.size();
     if (!ok(cudaMemcpyAsync(b->tables, t.host.data(), t.host.size(), cudaMemcpyHostToDevice, b->stream),
             "batch tables upload") ||
@@ -275,7 +287,17 @@ BatchScene *scene_of(sph_batch *b, int id, const char *what) {
 
 extern "C" sph_batch *sph_batch_create(void) {
     sph_batch *b = new sph_batch();
-    bool good = ok(sph_prepare_kernels(), "sph_batch_create") &&
+    int dev = 0;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    const unsigned long long keep = ~0ull;
+    bool good = ok(cudaGetDevice(&dev), "sph_batch_create");
+    props.location.id = dev;
+    good = good && ok(cudaMemPoolCreate(&b->pool, &props), "sph_batch_create (memory pool)") &&
+           ok(cudaMemPoolSetAttribute(b->pool, cudaMemPoolAttrReleaseThreshold, (void *)&keep),
+              "sph_batch_create (memory pool)");
+    good = good && ok(sph_prepare_kernels(), "sph_batch_create") &&
                 ok(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "sph_batch_create") &&
                 ok(cudaStreamCreateWithFlags(&b->side[0], cudaStreamNonBlocking), "sph_batch_create") &&
                 ok(cudaStreamCreateWithFlags(&b->side[1], cudaStreamNonBlocking), "sph_batch_create") &&
@@ -306,6 +328,7 @@ static void unpin_host(sph_batch *b, BatchScene *s) {
 
 extern "C" void sph_batch_free(sph_batch *b) {
     if (!b) return;
+    drain_reads(b, "sph_batch_free");
     if (b->stream) cudaStreamSynchronize(b->stream);
     release_graph(b);
     for (BatchScene *s : b->slots)
@@ -328,6 +351,7 @@ extern "C" void sph_batch_free(sph_batch *b) {
         if (e) cudaEventDestroy(e);
     for (cudaStream_t s : {b->stream, b->side[0], b->side[1], b->reads})
         if (s) cudaStreamDestroy(s);
+    if (b->pool) cudaMemPoolDestroy(b->pool);
     delete b;
 }
 
@@ -342,7 +366,9 @@ extern "C" size_t sph_scene_bytes(psdata *scene, const char *file_list) {
     return Arena::align(psdata_data_size(*scene)) + sph_scratch_bytes(d);
 }
 
-extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list) {
+// sph_batch_add and sph_batch_add_lattice: the scene's device memory from
+// the host store (all of it, or with `gen` its small fields and a lattice).
+static int add_scene(sph_batch *b, psdata *scene, const char *file_list, const sph_lattice *gen) {
     if (!b || !scene) {
         sph_set_error("sph_batch_add: null batch or scene");
         return -1;
@@ -365,15 +391,38 @@ extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list)
     sc->blob_size = psdata_data_size(*scene);
     size_t o_scratch = Arena::align(sc->blob_size);
     sc->bytes = o_scratch + sph_scratch_bytes(probe);
-    if (!ok(cudaMallocAsync(&sc->mem, sc->bytes, b->stream), "cudaMallocAsync(scene)")) {
+    if (!balloc(b, (void **)&sc->mem, sc->bytes, b->stream, "scene memory")) {
         delete sc;
         return -1;
     }
     sph_resolve_scene(*scene, sc->mem, programs, &sc->desc, &err);
     sph_place_scratch(&sc->desc, sc->mem + o_scratch);
-    bool good = ok(cudaMemcpyAsync(sc->mem, scene->data, sc->blob_size, cudaMemcpyHostToDevice, b->stream),
-                   "sph_batch_add upload") &&
-                ok(cudaMemsetAsync(sc->desc.status, 0, 4, b->stream), "sph_batch_add") &&
+    bool good = true;
+    if (gen) {
+        const unsigned long long count = (unsigned long long)gen->nx * gen->ny * gen->nz;
+        if (count == 0 || count > sc->desc.pnum || !sc->desc.position || !sc->desc.n) {
+            sph_set_error("sph_batch_add_lattice: %llu lattice points for a store of %u particles", count,
+                          sc->desc.pnum);
+            good = false;
+        }
+        good = good && ok(cudaMemsetAsync(sc->mem, 0, sc->blob_size, b->stream), "sph_batch_add_lattice");
+        for (unsigned f = 0; good && f < scene->num_fields; ++f)
+            if (scene->data_sizes[f] && scene->data_sizes[f] <= 4096)
+                good = ok(cudaMemcpyAsync(sc->mem + scene->data_offsets[f],
+                                          static_cast<const char *>(scene->data) + scene->data_offsets[f],
+                                          scene->data_sizes[f], cudaMemcpyHostToDevice, b->stream),
+                          "sph_batch_add_lattice");
+        if (good) {
+            LatticeGen g{gen->nx, gen->ny, gen->nz, gen->clamp_layers, gen->identity_rotation, gen->spacing,
+                         gen->jitter, {gen->origin[0], gen->origin[1], gen->origin[2]}, gen->seed};
+            sph_launch_lattice(sc->desc, g, b->stream);
+            good = sph_check_launch("sph_batch_add_lattice") == cudaSuccess;
+        }
+    } else {
+        good = ok(cudaMemcpyAsync(sc->mem, scene->data, sc->blob_size, cudaMemcpyHostToDevice, b->stream),
+                  "sph_batch_add upload");
+    }
+    good = good && ok(cudaMemsetAsync(sc->desc.status, 0, 4, b->stream), "sph_batch_add") &&
                 (!sc->desc.rigid_state ||
                  ok(cudaMemsetAsync(sc->desc.rigid_state, 0, 8ull * sc->desc.body_capacity * SPH_RIGID_STRIDE,
                                     b->stream),
@@ -402,6 +451,18 @@ extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list)
     b->bytes += sc->bytes;
     b->dirty = true;
     return id;
+}
+
+extern "C" int sph_batch_add(sph_batch *b, psdata *scene, const char *file_list) {
+    return add_scene(b, scene, file_list, nullptr);
+}
+
+extern "C" int sph_batch_add_lattice(sph_batch *b, psdata *scene, const char *file_list, const sph_lattice *gen) {
+    if (!gen) {
+        sph_set_error("sph_batch_add_lattice: no lattice");
+        return -1;
+    }
+    return add_scene(b, scene, file_list, gen);
 }
 
 extern "C" int sph_batch_remove(sph_batch *b, int id) {
@@ -555,7 +616,7 @@ extern "C" int sph_batch_read_field_many(sph_batch *b, const int *ids, unsigned 
             b->copy_segs = nullptr;
             b->copy_cap = 0;
             const unsigned cap = (unsigned)segs.size() * 2;
-            if (!ok(cudaMallocAsync((void **)&b->copy_segs, cap * sizeof(CopySeg), b->stream), what)) return -1;
+            if (!balloc(b, (void **)&b->copy_segs, cap * sizeof(CopySeg), b->stream, what)) return -1;
             b->copy_cap = cap;
         }
         if (!ok(cudaMemcpyAsync(b->copy_segs, segs.data(), segs.size() * sizeof(CopySeg), cudaMemcpyHostToDevice,
@@ -570,13 +631,13 @@ extern "C" int sph_batch_read_field_many(sph_batch *b, const int *ids, unsigned 
 
 // Grows a stream-ordered buffer (on `stream`, after what it ordered).
 template <class T>
-static bool grow(T **p, size_t *cap, size_t want, cudaStream_t stream, const char *what) {
+static bool grow(sph_batch *b, T **p, size_t *cap, size_t want, cudaStream_t stream, const char *what) {
     if (want <= *cap) return true;
     if (*p) cudaFreeAsync(*p, stream);
     *p = nullptr;
     *cap = 0;
     const size_t c = want + want / 2;
-    if (!ok(cudaMallocAsync((void **)p, c * sizeof(T), stream), what)) return false;
+    if (!balloc(b, (void **)p, c * sizeof(T), stream, what)) return false;
     *cap = c;
     return true;
 }
@@ -625,8 +686,8 @@ extern "C" long long sph_batch_read_field_many_async(sph_batch *b, const int *id
     // the host stores (an event never recorded counts as complete)
     if (!ok(cudaStreamWaitEvent(b->stream, b->read_done[t], 0), what)) return -1;
     size_t seg_cap = b->snap_seg_cap[t];
-    if (!grow(&b->snap[t], &b->snap_cap[t], total ? total : 16, b->stream, what) ||
-        !grow(&b->snap_segs[t], &seg_cap, segs.size(), b->stream, what))
+    if (!grow(b, &b->snap[t], &b->snap_cap[t], total ? total : 16, b->stream, what) ||
+        !grow(b, &b->snap_segs[t], &seg_cap, segs.size(), b->stream, what))
         return -1;
     b->snap_seg_cap[t] = (unsigned)seg_cap;
     for (unsigned k = 0; k < count; ++k) segs[k].dst = b->snap[t] + at[k];

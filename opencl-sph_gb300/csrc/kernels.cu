@@ -333,3 +333,37 @@ void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long
         k_copy_segments<<<dim3(gx, gy), 256, 0, stream>>>(segs, first);
     }
 }
+
+// splitmix64 (Steele, Lea and Flood, 2014; the finaliser of Vigna's
+// xorshift generators): a 64-bit counter-based mix.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+    unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_lattice(SceneDesc S, LatticeGen g, unsigned count) {
+    for (unsigned p = blockIdx.x * blockDim.x + threadIdx.x; p < count; p += gridDim.x * blockDim.x) {
+        const unsigned q[3] = {p % g.nx, p / g.nx % g.ny, p / (g.nx * g.ny)};
+        for (int a = 0; a < 3; ++a) {
+            const unsigned long long z = splitmix64(g.seed * 0x100000000ull + 3ull * p + (unsigned long long)a);
+            const double u = (double)(z >> 11) * 0x1.0p-53;
+            const double off = __dmul_rn(g.jitter, __dsub_rn(__dmul_rn(2.0, u), 1.0));
+            const double x = __dadd_rn(__dadd_rn(__dmul_rn((double)q[a], g.spacing), g.origin[a]), off);
+            S.position[3 * (size_t)p + a] = __double2float_rn(x);
+        }
+        if (S.body_number)
+            const_cast<unsigned *>(S.body_number)[p] = p < g.clamp_layers * g.nx * g.ny ? 1u : 0u;
+        if (g.identity_rotation && S.rotation)
+            for (int c = 0; c < 9; ++c) S.rotation[9 * (size_t)p + c] = (c % 4 == 0) ? 1.f : 0.f;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *const_cast<unsigned *>(S.n) = count;
+}
+
+void sph_launch_lattice(const SceneDesc &d, const LatticeGen &g, cudaStream_t stream) {
+    const unsigned count = g.nx * g.ny * g.nz;
+    unsigned grid = (count + 255) / 256;
+    grid = grid < 1 ? 1 : grid > 4096 ? 4096 : grid;
+    k_lattice<<<grid, 256, 0, stream>>>(d, g, count);
+}

@@ -96,6 +96,19 @@ void sph_launch_rigid_reset(const Launch &L);
 void sph_launch_count_down(const Launch &L);
 void sph_launch_set_steps(unsigned *steps_left, unsigned steps, cudaStream_t stream);
 
+// A jittered lattice written into a scene on the device (the device form
+// of the lattice scene builders): particle p sits at lattice point
+// (p % nx, p / nx % ny, p / (nx ny)) * spacing + origin, each coordinate
+// plus jitter * (2u - 1), u = splitmix64(seed * 2^32 + 3p + axis) / 2^64
+// (53 bits), in IEEE double, rounded to float.  The first clamp_layers
+// nx ny particles get body_number 1; identity_rotation sets rotation = I.
+struct LatticeGen {
+    unsigned nx, ny, nz, clamp_layers, identity_rotation;
+    double spacing, jitter, origin[3];
+    unsigned long long seed;
+};
+void sph_launch_lattice(const SceneDesc &d, const LatticeGen &g, cudaStream_t stream);
+
 // One byte range to copy (device to device or to mapped host memory).
 struct CopySeg {
     const char *src;

@@ -47,6 +47,19 @@ class Batch(object):
         return ps
 
     @staticmethod
+    def lattice_store(scene):
+        """The host store of a device-built lattice scene: the conf's values
+        and the small initial fields only (the particle arrays are made on
+        the device)."""
+        ps = init_data_cpu(scene.spec)
+        v = bnd.store_views(ps)
+        for k, val in scene.init.items():
+            arr = np.asarray(val)
+            if arr.nbytes <= 4096:
+                v[k][...] = arr if arr.size == 1 else arr.reshape(v[k].shape)
+        return ps
+
+    @staticmethod
     def scene_bytes(scene, ps=None):
         own = ps is None
         ps = ps or Batch.host_store(scene)
@@ -59,6 +72,23 @@ class Batch(object):
         """Uploads `scene` (its initial values, or the given host store)."""
         ps = ps or self.host_store(scene)
         sid = bnd.sph_batch_add(self.handle, ctypes.byref(ps), scene.kernel_files)
+        if sid < 0:
+            free_data_cpu(ps)
+            raise bnd.SphError(bnd.last_error())
+        self.scenes[sid] = Scene(scene, ps, sid)
+        return sid
+
+    def add_lattice(self, scene, ps=None):
+        """Adds a lattice scene built on the device (scene.gen, from a
+        builder called with jitter_hash=True): no particle array is made or
+        uploaded on the host.  The result equals add(scene)."""
+        if not scene.gen:
+            raise ValueError("%s has no device lattice (build it with jitter_hash=True)" % scene.name)
+        g = scene.gen
+        lat = bnd.sph_lattice(g["nx"], g["ny"], g["nz"], g["clamp_layers"], g["identity_rotation"], g["spacing"],
+                              g["jitter"], (ctypes.c_double * 3)(*g["origin"]), g["seed"])
+        ps = ps or self.lattice_store(scene)
+        sid = bnd.sph_batch_add_lattice(self.handle, ctypes.byref(ps), scene.kernel_files, ctypes.byref(lat))
         if sid < 0:
             free_data_cpu(ps)
             raise bnd.SphError(bnd.last_error())

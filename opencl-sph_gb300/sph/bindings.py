@@ -94,6 +94,17 @@ class psdata_cuda(Structure):
     ]
 
 
+class sph_lattice(Structure):
+    """sph_lattice of sph_gb300.h: a lattice scene built on the device."""
+    _fields_ = [
+        ("nx", c_uint), ("ny", c_uint), ("nz", c_uint),
+        ("clamp_layers", c_uint), ("identity_rotation", c_uint),
+        ("spacing", c_double), ("jitter", c_double),
+        ("origin", c_double * 3),
+        ("seed", c_ulonglong),
+    ]
+
+
 psdata_opencl = psdata_cuda
 String = c_char_p
 _names = POINTER(c_char_p)
@@ -214,6 +225,7 @@ _SIGS = {
     "sph_batch_synchronize": ([c_void_p], c_int),
     "sph_batch_read_field": ([c_void_p, c_int, String, POINTER(psdata)], c_int),
     "sph_batch_read_field_async": ([c_void_p, c_int, String, POINTER(psdata)], c_int),
+    "sph_batch_add_lattice": ([c_void_p, POINTER(psdata), String, POINTER(sph_lattice)], c_int),
     "sph_batch_pin_host": ([c_void_p, c_int, POINTER(psdata)], c_int),
     "sph_batch_unpin_host": ([c_void_p, c_int], c_int),
     "sph_batch_read_field_many": ([c_void_p, POINTER(c_int), c_uint, String, POINTER(POINTER(psdata))], c_int),

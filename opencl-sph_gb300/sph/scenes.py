@@ -33,15 +33,19 @@ def _fmt(v):
 
 
 class Scene(object):
-    """A store specification plus initial values."""
+    """A store specification plus initial values.  `gen`, for a lattice
+    scene jittered by the counter-based generator, holds the lattice
+    parameters with which sph_batch_add_lattice builds the same particle
+    fields on the device."""
 
-    def __init__(self, name, material, kernel_files, entries, init, n):
+    def __init__(self, name, material, kernel_files, entries, init, n, gen=None):
         self.name = name
         self.material = material          # 'fluid' | 'corot' | 'svk'
         self.kernel_files = kernel_files
         self.entries = entries            # (name, dims, type, value or None)
         self.init = init                  # field -> array (set after build)
         self.n = n
+        self.gen = gen
 
     @property
     def spec(self):
@@ -74,16 +78,45 @@ class Scene(object):
         return ps
 
 
-def lattice(nx, ny, nz, spacing, origin=(0.0, 0.0, 0.0), jitter=0.0, rng=None):
+def splitmix64(x):
+    """splitmix64 (Steele, Lea and Flood, 2014) of a uint64 array."""
+    x = np.asarray(x, dtype=np.uint64)
+    z = x + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def hash_jitter(count, seed, jitter):
+    """(count, 3) offsets jitter * (2u - 1), u the top 53 bits of
+    splitmix64(seed * 2^32 + 3p + axis) over 2^53, in IEEE double: the
+    device lattice builder (sph_batch_add_lattice) computes the same."""
+    ctr = np.uint64(seed) * np.uint64(1 << 32) + np.arange(3 * count, dtype=np.uint64)
+    u = (splitmix64(ctr) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    return (float(jitter) * (2.0 * u - 1.0)).reshape(count, 3)
+
+
+def lattice(nx, ny, nz, spacing, origin=(0.0, 0.0, 0.0), jitter=0.0, rng=None, hash_seed=None):
     """x-fastest (nx*ny*nz, 3) lattice at `spacing` from `origin`, each
-    coordinate jittered uniformly in [-jitter, jitter]."""
+    coordinate jittered uniformly in [-jitter, jitter]: from `rng`, or with
+    `hash_seed` from the counter-based generator of hash_jitter (the
+    device builder's)."""
     i, j, k = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
     p = np.stack([i.T.ravel(), j.T.ravel(), k.T.ravel()], axis=1).astype(np.float64) * spacing
     p += np.asarray(origin, dtype=np.float64)
-    if jitter:
+    if hash_seed is not None:
+        if jitter:
+            p += hash_jitter(p.shape[0], hash_seed, jitter)
+    elif jitter:
         rng = rng if rng is not None else np.random.default_rng(0)
         p += rng.uniform(-jitter, jitter, size=p.shape)
     return p.astype(np.float32)
+
+
+def _gen(nx, ny, nz, spacing, origin, jitter, seed, clamp_layers=0, identity_rotation=0):
+    return {"nx": int(nx), "ny": int(ny), "nz": int(nz), "spacing": float(spacing),
+            "origin": tuple(float(o) for o in origin), "jitter": float(jitter), "seed": int(seed),
+            "clamp_layers": int(clamp_layers), "identity_rotation": int(identity_rotation)}
 
 
 def _common_entries(pnum, mass, dt, h, gravity, gridbounds, nplanes=0, body_count=1):
@@ -112,11 +145,15 @@ def _common_entries(pnum, mass, dt, h, gravity, gridbounds, nplanes=0, body_coun
 
 def wcsph_block(nx=20, ny=20, nz=20, spacing=0.01, h=0.02, box=(0.0, 0.4), jitter=1e-4, seed=0,
                 restdens=1000.0, stiffness=3.0, viscosity=0.2, gravity=(0.0, -9.8, 0.0), dt=1e-4,
-                mass=None, walls=True, pnum=None, name=None):
+                mass=None, walls=True, pnum=None, name=None, jitter_hash=False):
     """WCSPH fluid lattice in the low corner of the cube box^3 (the dam
-    break).  `walls` adds the reflective-box extension at the box faces."""
+    break).  `walls` adds the reflective-box extension at the box faces.
+    `jitter_hash`: the counter-based jitter, so that the device builder
+    (Batch.add_lattice) can make the scene without the host arrays."""
     rng = np.random.default_rng(seed)
-    pos = lattice(nx, ny, nz, spacing, origin=(box[0] + spacing / 2,) * 3, jitter=jitter, rng=rng)
+    origin = (box[0] + spacing / 2,) * 3
+    pos = lattice(nx, ny, nz, spacing, origin=origin, jitter=jitter, rng=rng,
+                  hash_seed=seed if jitter_hash else None)
     n = pos.shape[0]
     pnum = pnum or n
     if mass is None:
@@ -127,7 +164,8 @@ def wcsph_block(nx=20, ny=20, nz=20, spacing=0.01, h=0.02, box=(0.0, 0.4), jitte
                 ("viscosity", "1", "float", viscosity)]
     if walls:
         entries.append(("wallbounds", "6", "float", gb))
-    return Scene(name or "wcsph-%d" % n, "fluid", FLUID_KERNELS, entries, {"position": pos, "n": n}, n)
+    gen = _gen(nx, ny, nz, spacing, origin, jitter, seed) if jitter_hash else None
+    return Scene(name or "wcsph-%d" % n, "fluid", FLUID_KERNELS, entries, {"position": pos, "n": n}, n, gen)
 
 
 def ball(radius, spacing, center):
@@ -202,11 +240,12 @@ def large_scene(seed=0):
 
 def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", youngs_modulus=1e5,
                   poisson=0.3, density=1000.0, viscosity=6e-5, gravity=(0.0, -9.8, 0.0), dt=5e-5,
-                  clamp_layers=2, jitter=0.0, seed=0, margin=None, name=None):
+                  clamp_layers=2, jitter=0.0, seed=0, margin=None, name=None, jitter_hash=False):
     """Elastic lattice whose first `clamp_layers` layers along z belong to
-    body 1, a fixed (non-dynamic) body: the clamped beam."""
+    body 1, a fixed (non-dynamic) body: the clamped beam.  `jitter_hash` as
+    for wcsph_block."""
     rng = np.random.default_rng(seed)
-    pos = lattice(nx, ny, nz, spacing, jitter=jitter, rng=rng)
+    pos = lattice(nx, ny, nz, spacing, jitter=jitter, rng=rng, hash_seed=seed if jitter_hash else None)
     n = pos.shape[0]
     ext = np.array([nx, ny, nz]) * spacing
     m = margin if margin is not None else 4 * h
@@ -242,7 +281,8 @@ def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", y
     body[: clamp_layers * layer] = 1
     rot = np.tile(np.eye(3, dtype=np.float32), (n, 1, 1))
     init = {"position": pos, "n": n, "body_number": body, "rotation": rot, "body_dynamic": np.zeros(1, np.uint32)}
-    return Scene(name or "%s-%d" % (material, n), material, kernels, entries, init, n)
+    gen = _gen(nx, ny, nz, spacing, (0.0, 0.0, 0.0), jitter, seed, clamp_layers, 1) if jitter_hash else None
+    return Scene(name or "%s-%d" % (material, n), material, kernels, entries, init, n, gen)
 
 
 def _dims_for(n_target, aspect=(1.0, 1.0, 1.0)):
@@ -256,7 +296,7 @@ MATERIALS = ("fluid", "corot", "svk")
 
 
 def mix_member(material, n_target, seed=0, youngs_modulus=1e5, poisson=0.3, spacing=0.01, h=0.02, dt_fluid=1e-4,
-               dt_solid=5e-5, jitter=1e-4, name=None):
+               dt_solid=5e-5, jitter=1e-4, name=None, jitter_hash=False):
     """A scene of the batched/served mix with about n_target particles.  A
     fluid block is 1 x 1/2 x 1 and sits in a box twice its width (room to
     collapse); a solid is a 1 x 1 x 2 beam clamped at one end."""
@@ -265,10 +305,11 @@ def mix_member(material, n_target, seed=0, youngs_modulus=1e5, poisson=0.3, spac
         ext = max(nx, nz) * spacing
         box_hi = 2.0 * ext + 4 * h
         return wcsph_block(nx, ny, nz, spacing=spacing, h=h, box=(0.0, box_hi), jitter=jitter, seed=seed,
-                           dt=dt_fluid, name=name)
+                           dt=dt_fluid, name=name, jitter_hash=jitter_hash)
     nx, ny, nz = _dims_for(n_target, (1.0, 1.0, 2.0))
     return solid_lattice(nx, ny, nz, spacing=spacing, h=h, material=material, youngs_modulus=youngs_modulus,
-                         poisson=poisson, dt=dt_solid, clamp_layers=1, jitter=jitter, seed=seed, name=name)
+                         poisson=poisson, dt=dt_solid, clamp_layers=1, jitter=jitter, seed=seed, name=name,
+                         jitter_hash=jitter_hash)
 
 
 def mixed_scene(rng, index, n_range=(1000, 65536), mix=(0.6, 0.25, 0.15), e_range=(1e4, 1e6),

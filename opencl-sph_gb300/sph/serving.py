@@ -66,10 +66,12 @@ class Server(object):
         self.tune = tune
 
     def prepare(self, requests):
-        """Builds each request's host store ahead of its arrival."""
+        """Builds each request's host store ahead of its arrival: the full
+        store, or for a device-built lattice scene (scene.gen) only its
+        conf values, the particles being made on the device at admission."""
         for r in requests:
             if r.host is None:
-                r.host = Batch.host_store(r.scene)
+                r.host = Batch.lattice_store(r.scene) if r.scene.gen else Batch.host_store(r.scene)
                 r.bytes = Batch.scene_bytes(r.scene, r.host)
 
     def _fits(self, batch, resident, r, active):
@@ -105,7 +107,7 @@ class Server(object):
             now = clock()
             while pending and pending[0].arrival <= now and self._fits(batch, resident, pending[0], active):
                 r = pending.popleft()
-                sid = batch.add(r.scene, ps=r.host)
+                sid = batch.add_lattice(r.scene, ps=r.host) if r.scene.gen else batch.add(r.scene, ps=r.host)
                 r.host = None  # owned by the batch now
                 batch.set_steps(sid, r.remaining)
                 r.admitted = clock()

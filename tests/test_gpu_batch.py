@@ -270,6 +270,39 @@ def test_solids_with_and_without_planes_in_one_batch():
     b.close()
 
 
+@pytest.mark.parametrize("material", ["fluid", "corot", "svk"])
+def test_device_lattice_equals_host_built_scene(material):
+    """A lattice scene built on the device (sph_batch_add_lattice) holds the
+    same store as the host-built scene uploaded whole, and runs the same."""
+    sc = scenes.mix_member(material, 3000, seed=123457, jitter_hash=True, name="dev-" + material)
+    a, b = Batch(), Batch()
+    ia, ib = a.add_lattice(sc), b.add(sc)
+    va, vb = a.read(ia), b.read(ib)
+    for f in va:
+        assert np.array_equal(va[f], vb[f]), f
+    a.step(10)
+    b.step(10)
+    va, vb = a.read(ia), b.read(ib)
+    assert np.array_equal(va["position"], vb["position"]) and np.array_equal(va["velocity"], vb["velocity"])
+    a.close()
+    b.close()
+
+
+def test_served_device_built_scenes_equal_alone():
+    def make(rng, i):
+        mat = scenes.MATERIALS[i % 3]
+        return scenes.mix_member(mat, int(rng.integers(800, 3000)), seed=i + 17, jitter_hash=True, name="d%d" % i)
+    reqs = poisson_requests(rate=200.0, duration=0.05, make_scene=make, steps_range=(3, 15), seed=9)
+    assert len(reqs) >= 5
+    stats = Server(budget_bytes=60e6, max_chunk=4).run(reqs, realtime=False)
+    assert stats["requests"] == len(reqs)
+    for r in reqs:
+        pos, vel = alone(r.scene, r.steps)
+        assert np.array_equal(r.result["position"], pos), r.scene.name
+        assert np.array_equal(r.result["velocity"], vel), r.scene.name
+    release(reqs)
+
+
 def test_ragged_and_empty_scenes_in_a_batch():
     """Scenes with fewer active particles than their capacity, and with none,
     run beside full ones: the ragged scene equals itself alone, the empty
