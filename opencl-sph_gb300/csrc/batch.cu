@@ -787,7 +787,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
         log.mark("bin_count");
         sph_launch_bin_count(A);
         log.mark("scan");
-        sph_launch_scan(A);
+        sph_launch_scan(A, true);
         log.mark("insert");
         sph_launch_insert(A);
         log.mark("gather");

@@ -38,15 +38,16 @@ void sph_launch_find_bins(const Launch &L) {
 }
 
 void sph_launch_zero_cells(const Launch &L) {
-    k_zero_cells<<<grid_for(L.cells, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.cells);
+    k_zero_cells<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
 }
 
 void sph_launch_count(const Launch &L) {
     k_count_only<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
 }
 
-void sph_launch_scan(const Launch &L) {
-    k_scan_reduce<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
+void sph_launch_scan(const Launch &L, bool sums_ready) {
+    if (!sums_ready)
+        k_scan_reduce<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
     k_scan_down<<<grid_for(L.scan, L.grid_cap), SPH_SCAN_THREADS, 0, L.stream>>>(L.scenes, L.scan);
 }
 
@@ -65,7 +66,7 @@ void sph_launch_bin_count(const Launch &L) {
 
 void sph_launch_bins(const Launch &L) {
     sph_launch_bin_count(L);
-    sph_launch_scan(L);
+    sph_launch_scan(L, true);
     sph_launch_insert(L);
 }
 
@@ -209,7 +210,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     phase("bin_count");
     sph_launch_bin_count(L);
     phase("scan");
-    sph_launch_scan(L);
+    sph_launch_scan(L, true);
     phase("insert");
     sph_launch_insert(L);
     phase("gather");

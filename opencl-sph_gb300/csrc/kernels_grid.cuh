@@ -49,18 +49,31 @@ __global__ void k_bin_count(const SceneDesc *__restrict__ scenes, BlockMap map, 
             if (lane == leader) base = atomicAdd(S.gridcount + cell, (unsigned)__popc(peers));
             base = __shfl_sync(peers, base, leader);
             S.slot[item] = base + __popc(peers & ((1u << lane) - 1u));
+            // the scan tile's total (k_scan_down reads these)
+            const unsigned tile = cell / SPH_SCAN_TILE;
+            const unsigned tpeers = __match_any_sync(lanes, tile);
+            if (lane == (unsigned)(__ffs(tpeers) - 1)) atomicAdd(S.scan_sums + tile, (unsigned)__popc(tpeers));
         }
     }
     SPH_END_WORK
 }
 
-// zero_gridcount (common.cl:392-400) for every scene of the launch, plus
-// the crowded-cell queue counter.
-__global__ void k_zero_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    SPH_FOR_WORK(map)
-    if (item < S.num_cells) S.gridcount[item] = 0u;
-    if (item == 0) S.big_cells[0] = 0u;
-    SPH_END_WORK
+// zero_gridcount (common.cl:392-400) for every scene of the launch, one
+// block per scan tile of SPH_SCAN_TILE cells: the counts, the tile's total
+// (which k_bin_count accumulates) and, once per scene, the crowded-cell
+// queue counter.
+__global__ void __launch_bounds__(SPH_SCAN_THREADS) k_zero_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    for (unsigned vb = blockIdx.x; vb < map.num; vb += gridDim.x) {
+        const BlockWork bw = map.work[vb];
+        const SceneDesc &S = scenes[bw.scene];
+        if (scene_idle(S)) continue;
+        const unsigned end = min(bw.first + SPH_SCAN_TILE, S.num_cells);
+        for (unsigned c = bw.first + threadIdx.x; c < end; c += blockDim.x) S.gridcount[c] = 0u;
+        if (threadIdx.x == 0) {
+            S.scan_sums[bw.first / SPH_SCAN_TILE] = 0u;
+            if (bw.first == 0) S.big_cells[0] = 0u;
+        }
+    }
 }
 
 // count_particles_in_bins alone, for a driver that calls the reference's

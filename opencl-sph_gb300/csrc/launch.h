@@ -36,7 +36,9 @@ enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2 };
 void sph_launch_find_bins(const Launch &L);
 void sph_launch_zero_cells(const Launch &L);
 void sph_launch_count(const Launch &L);
-void sph_launch_scan(const Launch &L);
+// sums_ready: k_bin_count has added up the tiles' totals (a fused binning);
+// otherwise a pass over the counts does (prefix_sum called by name)
+void sph_launch_scan(const Launch &L, bool sums_ready = false);
 void sph_launch_insert(const Launch &L);  // scatter + per-cell ordering
 // zero_gridcount + find_particle_bins + count_particles_in_bins in one
 // pass, recording each particle's arrival slot
