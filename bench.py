@@ -88,13 +88,13 @@ PHASE_BYTES = {
 # (profiles/fluid_pair_passes_wcsph-1m.md, profiles/fluid_pair_passes_batched-256.md,
 # profiles/solid_scan_passes_batched-256.md, profiles/solid_force_passes_batched-256.md).
 MEASURED_TRAFFIC = {
-    ("wcsph-1m", "forces_fluids+step"): 110.37e6,               # k_forces_fluids_masked
-    ("batched-256", "density"): 245.84e6,                       # k_density<false> (writes the candidate masks too)
-    ("batched-256", "fluid forces+step"): 344.56e6,             # k_forces_fluids_masked
-    ("batched-256", "corotational rotations"): 238.50e6,        # k_rotations_and_strains (with the stress law)
-    ("batched-256", "corotational forces+step"): 241.55e6,      # k_forces_solids<1, 1> (with the step)
-    ("batched-256", "svk deformations"): 105.82e6,              # k_deformations (with the stress law)
-    ("batched-256", "svk forces+step"): 162.44e6,               # k_forces_solids<0, 1> (with the step)
+    ("wcsph-1m", "forces_fluids+step"): 118.61e6,               # k_forces_fluids_masked
+    ("batched-256", "density"): 264.06e6,                       # k_density<false> (masks, pressure, 1/density too)
+    ("batched-256", "fluid forces+step"): 367.19e6,             # k_forces_fluids_masked
+    ("batched-256", "corotational rotations"): 238.39e6,        # k_rotations_and_strains (with the stress law)
+    ("batched-256", "corotational forces+step"): 241.54e6,      # k_forces_solids<1, 1> (with the step)
+    ("batched-256", "svk deformations"): 105.71e6,              # k_deformations (with the stress law)
+    ("batched-256", "svk forces+step"): 162.05e6,               # k_forces_solids<0, 1> (with the step)
 }
 
 
