@@ -7,9 +7,8 @@
 // synchronises the device and work already queued keeps running: this is
 // what lets the serving loop admit requests while others are on the GPU.
 // The pool keeps what retired scenes freed for the next admissions (its
-// release threshold is unbounded): the default pool would hand it back to
-// the driver at every synchronisation and map it again for the next scene,
-// which cost about 6 ms per admission.
+// release threshold is unbounded): the default pool releases its memory at
+// every synchronisation and would map it again for the next scene.
 #include <string.h>
 
 #include <algorithm>

@@ -1,8 +1,8 @@
 """ctypes front end of the CPU oracle (liboracle.so, sph_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: the tests, __graft_entry__.smoke() and the
-CPU-baseline legs of bench.py use this module as the checker.  The product
-(opencl-sph_gb300/) never imports it.
+CPU-baseline legs of bench.py use this module to check results and time
+the CPU path.  The product (opencl-sph_gb300/) never imports it.
 
 An :class:`OracleScene` owns NumPy copies of a store's fields (taken from
 the arrays a ``ParticleSystem.get_fields`` returns, i.e. with the store's

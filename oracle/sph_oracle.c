@@ -1,7 +1,8 @@
 /*
  * sph_oracle.c -- instantiates the CPU oracle (sph_oracle_impl.h) in FP32
- * and FP64.  Test infrastructure only: loaded by the tests, by smoke() as
- * the checker and by bench.py's CPU-baseline leg, never by the product.
+ * and FP64.  Test infrastructure only: loaded by the tests, by smoke() to
+ * check its results and by bench.py's CPU-baseline leg, never by the
+ * product.
  *
  * Build: make -C oracle  (gcc -O2 -ffp-contract=off -fopenmp, no fast-math,
  * so every float operation is individually rounded as in the source).
