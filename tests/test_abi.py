@@ -69,3 +69,14 @@ def test_errors_are_recorded_not_aborted():
         raised = "not a live device store" in str(e)
     assert raised
     assert bnd.sph_version().startswith(b"sph_gb300")
+
+
+def test_missing_library_fails_loudly():
+    """Without the compiled library the package does not import: there is
+    no CPU fallback behind the interface."""
+    import sys
+    code = "import sys; sys.path.insert(0, %r); import sph" % os.path.join(ROOT, "opencl-sph_gb300")
+    env = dict(os.environ, SPH_GB300_LIB=os.path.join(ROOT, "no-such-dir", "libsph_gb300.so"))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
+    assert r.returncode != 0
+    assert "libsph_gb300.so not found" in r.stderr
