@@ -180,6 +180,7 @@ __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3
 struct FluidI {
     float3 ipos, ivel;
     float inv_rhoi, pi, h, rho0, stiff, visc, kv;
+    float vk, pk;  // visc kv and -kv / 2, the pair term's constant factors
     DistBounds B;
 };
 
@@ -196,6 +197,8 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
     const float h3 = I.h * I.h * I.h;
     I.kv = 45.0f / (SPH_PI_F * h3 * h3);  // 45 / (pi h^6)
     I.pi = fluid_pressure(rhoi, I.rho0, I.stiff);
+    I.vk = __fmul_rn(I.visc, I.kv);
+    I.pk = __fmul_rn(-0.5f, I.kv);
     return I;
 }
 
@@ -213,9 +216,8 @@ __device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3
     const float dist = __fmul_rn(r2, rinv);
     const float din = __fsub_rn(I.h, dist);
     const float inv_didj = __fmul_rn(I.inv_rhoi, inv_rhoj);
-    const float vterm = __fmul_rn(__fmul_rn(I.visc, din), I.kv);
-    const float pterm = __fmul_rn(
-        __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(-__fadd_rn(I.pi, pj), 0.5f), rinv), din), din), I.kv);
+    const float vterm = __fmul_rn(din, I.vk);
+    const float pterm = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fadd_rn(I.pi, pj), I.pk), rinv), din), din);
     const float3 rv = sub3(jvel, I.ivel);
     f.add(make_float3(__fmul_rn(__fmaf_rn(d.x, pterm, __fmul_rn(rv.x, vterm)), inv_didj),
                       __fmul_rn(__fmaf_rn(d.y, pterm, __fmul_rn(rv.y, vterm)), inv_didj),
