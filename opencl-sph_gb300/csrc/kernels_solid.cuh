@@ -216,7 +216,9 @@ struct SolidConsts {
 __device__ __forceinline__ SolidConsts solid_consts(const SceneDesc &S) {
     SolidConsts c;
     c.h = *S.h;
-    c.h2 = c.h * c.h;
+    // rounded on its own, as the density pass rounds it: inlined, h * h
+    // could otherwise fuse with a later h2 - r2 into one FMA in some kernels
+    c.h2 = __fmul_rn(c.h, c.h);
     DistBounds b = dist_bounds(c.h);
     c.le = b.le;
     c.lt = b.lt;
@@ -601,19 +603,20 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 
 // Pass 1 of the plane-free solid passes over particle k's stencil rows,
 // from the cell-sorted copies.  Each row is taken in chunks of 32
-// candidates, one mask word each: a tight loop over the chunk adds the
-// density term (j = i included, in the density pass's order), records the
-// mask bits and the bits of the chunk's current neighbours (|p| <= h);
-// particle k's own bit is cleared afterwards.  Then sum(p, q, w) runs for
-// the neighbours in candidate order, w = (h^2 - |p|^2)^3.  The sums see
-// the neighbours in the order a plain scan would, while the scan loop stays
-// free of their work, which otherwise every lane would issue whenever any
-// lane of its warp met a neighbour.  Only a row's first 64 candidates have
-// mask bits; `overflow` records a longer row.
+// candidates, one mask word each: a tight loop over the chunk records the
+// mask bits (|p| <= h or |q| <= h, k itself excluded) and the bits of the
+// chunk's current neighbours (|p| <= h, k itself included).  Then a walk
+// over those neighbours, in candidate order, adds each one's density term
+// (the density pass's sum, in its order) and for j != i runs sum(p, q, w),
+// w = (h^2 - |p|^2)^3.  The scan loop thus stays free of the sums' work,
+// which otherwise every lane would issue whenever any lane of its warp met
+// a neighbour, and every sum sees the neighbours in the order a plain scan
+// would.  Only a row's first 64 candidates have mask bits; `overflow`
+// records a longer row.
 //
 // The density terms are summed whether or not the caller stores them: a
-// flag tested inside the loop lets the compiler emit one copy of the loop
-// per value, and copies may contract the sums' products differently, which
+// flag tested inside the loops lets the compiler emit one copy of them per
+// value, and copies may contract the sums' products differently, which
 // would break the equality of the named and fused passes.
 template <class Sum>
 __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, const StencilRows &rows,
@@ -634,29 +637,24 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
             for (unsigned t = 0; t < cn; ++t) {
                 const unsigned kk = cb + t;
                 const float r2 = norm2(sub3(xyz(spos[kk]), ipos));
-                if (r2 <= C.le) {
-                    const float d = fmaxf(C.h2 - r2, 0.f);
-                    rho.add(d * d * d);
-                    count += r2 <= C.lt;
-                }
                 const float q2 = norm2(sub3(xyz(spos0[kk]), ipos0));
                 const unsigned bit = 1u << t;
                 if (r2 <= C.le) near |= bit;
                 if (r2 <= C.le || q2 <= C.le) bits |= bit;
             }
-            if (k - cb < cn) {  // k itself is in this chunk
-                const unsigned self = ~(1u << (k - cb));
-                bits &= self;
-                near &= self;
-            }
+            if (k - cb < cn) bits &= ~(1u << (k - cb));  // k itself has no mask bit
             // mask words 2r and 2r + 1 (store_row_mask's layout)
             if (c0 < 64) S.nbmask[(size_t)(2 * r + (c0 >> 5)) * S.pnum + k] = bits;
             while (near) {
                 const unsigned kk = cb + (unsigned)(__ffs(near) - 1);
                 near &= near - 1u;
                 const float3 p = sub3(xyz(spos[kk]), ipos);
-                const float d = fmaxf(C.h2 - norm2(p), 0.f);
-                sum(p, sub3(xyz(spos0[kk]), ipos0), d * d * d);
+                const float r2 = norm2(p);
+                const float d = fmaxf(C.h2 - r2, 0.f);
+                const float w = d * d * d;
+                rho.add(w);
+                count += r2 <= C.lt;
+                if (kk != k) sum(p, sub3(xyz(spos0[kk]), ipos0), w);
             }
         }
         overflow |= len > 64;
@@ -691,11 +689,15 @@ __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restr
         scan_solid_rows(S, k, rows, ipos, ipos0, C, rho, count, total, overflow,
                         [&](float3 p, float3 q, float w) { add_outer(p * w, q, apq); });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        // the sorted density copy (scratch) is written either way: a value
+        // the named pass would discard lets the compiler emit a second copy
+        // of this kernel without the density sums, whose other sums may
+        // then round differently
+        const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
+        S.sdens[k] = value;
         if (with_density) {
-            const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
             S.density[i] = value;
             S.num_neighbours[i] = count;
-            S.sdens[k] = value;
         }
         float R[9];
         if (__float_as_uint(q4.w) > 0) {
@@ -771,11 +773,15 @@ __global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap ma
                             aqq[5] = __fmaf_rn(wq.y, q.z, aqq[5]);
                         });
         S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
+        // the sorted density copy (scratch) is written either way: a value
+        // the named pass would discard lets the compiler emit a second copy
+        // of this kernel without the density sums, whose other sums may
+        // then round differently
+        const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
+        S.sdens[k] = value;
         if (with_density) {
-            const float value = poly6_density(rho.s, C.h2, C.h, C.mass);
             S.density[i] = value;
             S.num_neighbours[i] = count;
-            S.sdens[k] = value;
         }
         float inv[6];
         sym_inverse(aqq, inv);
