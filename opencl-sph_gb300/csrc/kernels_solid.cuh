@@ -179,17 +179,23 @@ __device__ void sym_inverse(const float m[6], float out[6]) {
     p_d_pt(eig, P, out);
 }
 
+// a0 b0 + a1 b1 + a2 b2 with every rounding written out: the products and
+// sums below run in several kernels (the named and the fused passes), and
+// each copy must round alike whatever the compiler would contract.
+__device__ __forceinline__ float dot3_rn(float a0, float b0, float a1, float b1, float a2, float b2) {
+    return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, __fmul_rn(a0, b0)));
+}
 __device__ __forceinline__ float3 mat_vec(const float m[9], float3 v) {
-    return make_float3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
-                       m[6] * v.x + m[7] * v.y + m[8] * v.z);
+    return make_float3(dot3_rn(m[0], v.x, m[1], v.y, m[2], v.z), dot3_rn(m[3], v.x, m[4], v.y, m[5], v.z),
+                       dot3_rn(m[6], v.x, m[7], v.y, m[8], v.z));
 }
 __device__ __forceinline__ float3 mat_t_vec(const float m[9], float3 v) {
-    return make_float3(m[0] * v.x + m[3] * v.y + m[6] * v.z, m[1] * v.x + m[4] * v.y + m[7] * v.z,
-                       m[2] * v.x + m[5] * v.y + m[8] * v.z);
+    return make_float3(dot3_rn(m[0], v.x, m[3], v.y, m[6], v.z), dot3_rn(m[1], v.x, m[4], v.y, m[7], v.z),
+                       dot3_rn(m[2], v.x, m[5], v.y, m[8], v.z));
 }
 __device__ __forceinline__ float3 sym_vec(const float s[6], float3 v) {
-    return make_float3(s[0] * v.x + s[3] * v.y + s[4] * v.z, s[3] * v.x + s[1] * v.y + s[5] * v.z,
-                       s[4] * v.x + s[5] * v.y + s[2] * v.z);
+    return make_float3(dot3_rn(s[0], v.x, s[3], v.y, s[4], v.z), dot3_rn(s[3], v.x, s[1], v.y, s[5], v.z),
+                       dot3_rn(s[4], v.x, s[5], v.y, s[2], v.z));
 }
 // m += a b^T, one fused multiply-add per entry, written out so that every
 // copy of a sum rounds alike whatever the compiler would contract.
@@ -205,8 +211,8 @@ __device__ __forceinline__ float3 spiky_grad(float3 d, float h, float kv, float 
     float r2 = norm2(d);
     if (!(r2 <= le) || r2 == 0.f) return make_float3(0.f, 0.f, 0.f);
     float rinv = rsqrtf(r2);
-    float din = h - r2 * rinv;
-    float s = -kv * din * din * rinv;
+    const float din = __fsub_rn(h, __fmul_rn(r2, rinv));
+    const float s = -kv * din * din * rinv;
     return d * s;
 }
 
@@ -328,9 +334,6 @@ __global__ void k_rotations_and_strains_planes(const SceneDesc *__restrict__ sce
 // Stress laws (solid_corotation.cl:197-208; solid_svk.cl:45-80).  Every
 // rounding is written out: the laws run in the named stress pass and inside
 // the fused first solid pass, and both must give the same bits.
-__device__ __forceinline__ float dot3_rn(float a0, float b0, float a1, float b1, float a2, float b2) {
-    return __fmaf_rn(a2, b2, __fmaf_rn(a1, b1, __fmul_rn(a0, b0)));
-}
 
 struct Lame {
     float lam, mu2;  // lambda and 2 mu
@@ -887,10 +890,7 @@ __device__ __forceinline__ void side_from_sorted(const SceneDesc &S, unsigned kk
         }
 }
 
-__device__ __forceinline__ float3 mat3_vec(const float m[9], float3 v) {
-    return make_float3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
-                       m[6] * v.x + m[7] * v.y + m[8] * v.z);
-}
+__device__ __forceinline__ float3 mat3_vec(const float m[9], float3 v) { return mat_vec(m, v); }
 
 // Particle i's side of the pair term: its stress, R sigma and (corotational
 // body particles pair with) its stress again.
