@@ -188,8 +188,36 @@ void sph_clear_error(void);
 /* 1 (default, the reference's behaviour): a failing void call aborts.
  * 0: it records the error and returns. */
 void sph_set_abort_on_error(int abort_on_error);
-/* Waits for the store's stream; returns 0 or a non-zero CUDA error. */
+/* Waits for the store's stream and its reads (sph_read_fields_async);
+ * returns 0 or a non-zero CUDA error. */
 int sph_synchronize(psdata_cuda pso);
+/* Page-locks the host store `data` (the psdata the device store mirrors) so
+ * that copies to and from it run on the copy engines without a staging
+ * copy; the library ends the registration on sph_unpin_host or
+ * free_psdata_cuda, which must come before the blob is freed.  One host
+ * store per device store.  Returns 0 or -1. */
+int sph_pin_host(psdata data, psdata_cuda pso);
+int sph_unpin_host(psdata_cuda pso);
+/* sync_psdata_fields_host_to_device (particle_system_host.c:812-829)
+ * without the wait: the copies are enqueued on the store's stream, so the
+ * named fields of `data` must stay unchanged until the stream has passed
+ * them (a later blocking call or sph_synchronize).  An unknown name is an
+ * error (-1). */
+int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_fields, const char *const *names);
+/* sync_psdata_fields_device_to_host (particle_system_host.c:843-858)
+ * without the wait: the fields are copied to a device snapshot in stream
+ * order (after the substeps enqueued so far), and a side stream copies the
+ * snapshot into `data` (one cudaMemcpyAsync per field) while later
+ * substeps run.  Returns a ticket (>= 0), or -1.  `data` holds the
+ * snapshot after sph_wait_read(ticket); its named fields must not be used
+ * until then, and a later read writes them again, so enqueue it after the
+ * previous snapshot has been used.  Two reads are in flight at most: a
+ * third waits, on the device, for the first to finish.  Every blocking
+ * sync_* call first waits for the reads in flight. */
+long long sph_read_fields_async(psdata data, psdata_cuda pso, size_t num_fields, const char *const *names);
+int sph_wait_read(psdata_cuda pso, long long ticket);
+/* Waits for every read enqueued so far. */
+int sph_wait_reads(psdata_cuda pso);
 /* Runs `num_steps` substeps of the store's material recipe (the sequence a
  * reference driver issues through call_for_all_particles:
  * scripts/sph/systems.py:194-204 for corotational solids, :225-235 for SVK,

@@ -89,6 +89,16 @@ struct Store {
     char *rec_mem = nullptr;
     RecordPlan rec{};
     std::vector<std::string> rec_fields;
+    // sph_pin_host: the host blob, page-locked by this store
+    void *pinned = nullptr;
+    // sph_read_fields_async: reads take turns over two snapshot buffers;
+    // the stream `reads` copies a snapshot into the host store while later
+    // substeps run on `stream`
+    cudaStream_t reads = nullptr;
+    cudaEvent_t snap_done[2] = {nullptr, nullptr}, read_done[2] = {nullptr, nullptr};
+    char *snap[2] = {nullptr, nullptr};
+    size_t snap_cap[2] = {0, 0};
+    long long tickets = 0;  // reads enqueued so far
 };
 
 std::mutex g_stores_mu;
@@ -110,8 +120,23 @@ Store *store_of(const psdata_cuda &pso, const char *what) {
     return s;
 }
 
+// Waits for every asynchronous read of the store.
+bool drain_reads(Store *s, const char *what) {
+    return !s->reads || cuda_ok(cudaStreamSynchronize(s->reads), what);
+}
+
 void destroy(Store *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->reads) {
+        cudaStreamSynchronize(s->reads);
+        for (int t = 0; t < 2; ++t) {
+            if (s->snap[t]) cudaFree(s->snap[t]);
+            if (s->snap_done[t]) cudaEventDestroy(s->snap_done[t]);
+            if (s->read_done[t]) cudaEventDestroy(s->read_done[t]);
+        }
+        cudaStreamDestroy(s->reads);
+    }
+    if (s->pinned) cudaHostUnregister(s->pinned);
     if (s->rec_mem) cudaFree(s->rec_mem);
     if (s->step_graph) cudaGraphExecDestroy(s->step_graph);
     if (s->arena.base) cudaFree(s->arena.base);
@@ -414,6 +439,7 @@ extern "C" void free_psdata_cuda(psdata_cuda *pso) {
 // particle_system_host.c:837-841
 extern "C" void sync_psdata_device_to_host(psdata data, psdata_cuda pso) {
     with_store(pso, "sync_psdata_device_to_host", true, [&](Store *s) {
+        if (!drain_reads(s, "sync_psdata_device_to_host")) return false;
         size_t sz = psdata_data_size(data);
         if (sz > s->blob_size) {
             sph_set_error("store layout differs from the device copy");
@@ -429,6 +455,7 @@ extern "C" void sync_psdata_device_to_host(psdata data, psdata_cuda pso) {
 extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int full) {
     (void)full;
     with_store(pso, "sync_psdata_host_to_device", true, [&](Store *s) {
+        if (!drain_reads(s, "sync_psdata_host_to_device")) return false;
         size_t sz = psdata_data_size(data);
         if (sz > s->blob_size) {
             sph_set_error("store layout differs from the device copy");
@@ -446,6 +473,7 @@ extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int ful
 extern "C" void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso, size_t num_fields,
                                                   const char *const *names) {
     with_store(pso, "sync_psdata_fields_host_to_device", true, [&](Store *s) {
+        if (!drain_reads(s, "sync_psdata_fields_host_to_device")) return false;
         bool rigid = false;
         for (size_t i = 0; i < num_fields; ++i) {
             if (names[i] && !copy_field(s, data, names[i], true)) return false;
@@ -463,6 +491,7 @@ extern "C" void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso, 
 extern "C" void sync_psdata_fields_device_to_host(psdata data, psdata_cuda pso, size_t num_fields,
                                                   const char *const *names) {
     with_store(pso, "sync_psdata_fields_device_to_host", true, [&](Store *s) {
+        if (!drain_reads(s, "sync_psdata_fields_device_to_host")) return false;
         for (size_t i = 0; i < num_fields; ++i)
             if (names[i] && !copy_field(s, data, names[i], false)) return false;
         return true;
@@ -551,8 +580,134 @@ extern "C" int sph_synchronize(psdata_cuda pso) {
     Store *s = store_of(pso, "sph_synchronize");
     if (!s) return -1;
     cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e == cudaSuccess && s->reads) e = cudaStreamSynchronize(s->reads);
     if (e != cudaSuccess) sph_set_error("sph_synchronize: %s", cudaGetErrorString(e));
     return (int)e;
+}
+
+extern "C" int sph_pin_host(psdata data, psdata_cuda pso) {
+    const char *what = "sph_pin_host";
+    Store *s = store_of(pso, what);
+    if (!s) return -1;
+    if (psdata_data_size(data) != s->blob_size || !data.data) {
+        sph_set_error("%s: store layout differs from the device copy", what);
+        return -1;
+    }
+    if (s->pinned == data.data) return 0;
+    if (s->pinned) {
+        sph_set_error("%s: another host store is pinned for this device store (sph_unpin_host first)", what);
+        return -1;
+    }
+    if (!cuda_ok(cudaHostRegister(data.data, s->blob_size, cudaHostRegisterDefault), what)) return -1;
+    s->pinned = data.data;
+    return 0;
+}
+
+extern "C" int sph_unpin_host(psdata_cuda pso) {
+    const char *what = "sph_unpin_host";
+    Store *s = store_of(pso, what);
+    if (!s) return -1;
+    if (!s->pinned) return 0;
+    // copies into or out of the blob must end before it is unlocked
+    if (!cuda_ok(cudaStreamSynchronize(s->stream), what) || !drain_reads(s, what)) return -1;
+    void *p = s->pinned;
+    s->pinned = nullptr;
+    return cuda_ok(cudaHostUnregister(p), what) ? 0 : -1;
+}
+
+extern "C" int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_fields, const char *const *names) {
+    const char *what = "sph_write_fields_async";
+    Store *s = store_of(pso, what);
+    if (!s) return -1;
+    bool rigid = false;
+    for (size_t i = 0; i < num_fields; ++i) {
+        if (names[i] && !copy_field(s, data, names[i], true)) return -1;
+        rigid = rigid || (names[i] && touches_rigid_setup(names[i]));
+    }
+    if (rigid && s->desc.rigid_state) {
+        if (!refresh_rigid(s, data)) return -1;
+        sph_launch_rigid_reset(s->L);
+    }
+    return finish(s, what, false) ? 0 : -1;
+}
+
+extern "C" long long sph_read_fields_async(psdata data, psdata_cuda pso, size_t num_fields,
+                                           const char *const *names) {
+    const char *what = "sph_read_fields_async";
+    Store *s = store_of(pso, what);
+    if (!s) return -1;
+    if (psdata_data_size(data) != s->blob_size || !data.data) {
+        sph_set_error("%s: store layout differs from the device copy", what);
+        return -1;
+    }
+    if (!s->reads) {
+        bool good = cuda_ok(cudaStreamCreateWithFlags(&s->reads, cudaStreamNonBlocking), what);
+        for (int t = 0; good && t < 2; ++t)
+            good = cuda_ok(cudaEventCreateWithFlags(&s->snap_done[t], cudaEventDisableTiming), what) &&
+                   cuda_ok(cudaEventCreateWithFlags(&s->read_done[t], cudaEventDisableTiming), what);
+        if (!good) return -1;
+    }
+    struct Part {
+        size_t off, at, bytes;
+    };
+    std::vector<Part> parts;
+    size_t total = 0;
+    for (size_t i = 0; i < num_fields; ++i) {
+        const int f = names[i] ? get_field_psdata(data, names[i]) : -1;
+        if (f < 0) {
+            sph_set_error("%s: no field '%s'", what, names[i] ? names[i] : "");
+            return -1;
+        }
+        parts.push_back(Part{data.data_offsets[f], total, data.data_sizes[f]});
+        total += (data.data_sizes[f] + 15) / 16 * 16;
+    }
+    const int t = (int)(s->tickets & 1);
+    // turn t's snapshot is free once the read two tickets back has written
+    // the host store (an event never recorded counts as complete)
+    if (!cuda_ok(cudaStreamWaitEvent(s->stream, s->read_done[t], 0), what)) return -1;
+    if (total > s->snap_cap[t]) {
+        if (s->snap[t] && !cuda_ok(cudaStreamSynchronize(s->reads), what)) return -1;
+        if (s->snap[t]) cudaFree(s->snap[t]);
+        s->snap[t] = nullptr;
+        s->snap_cap[t] = 0;
+        if (!cuda_ok(cudaMalloc(&s->snap[t], total), what)) return -1;
+        s->snap_cap[t] = total;
+    }
+    // the snapshot, in stream order after the substeps enqueued so far
+    for (const Part &p : parts)
+        if (!cuda_ok(cudaMemcpyAsync(s->snap[t] + p.at, s->d_blob + p.off, p.bytes, cudaMemcpyDeviceToDevice,
+                                     s->stream),
+                     what))
+            return -1;
+    if (!cuda_ok(cudaEventRecord(s->snap_done[t], s->stream), what) ||
+        !cuda_ok(cudaStreamWaitEvent(s->reads, s->snap_done[t], 0), what))
+        return -1;
+    // the host store, written by the copy engines beside later substeps
+    char *host = static_cast<char *>(data.data);
+    for (const Part &p : parts)
+        if (!cuda_ok(cudaMemcpyAsync(host + p.off, s->snap[t] + p.at, p.bytes, cudaMemcpyDeviceToHost, s->reads),
+                     what))
+            return -1;
+    if (!cuda_ok(cudaEventRecord(s->read_done[t], s->reads), what)) return -1;
+    return s->tickets++;
+}
+
+extern "C" int sph_wait_read(psdata_cuda pso, long long ticket) {
+    Store *s = store_of(pso, "sph_wait_read");
+    if (!s) return -1;
+    if (ticket < 0 || ticket >= s->tickets) {
+        sph_set_error("sph_wait_read: no such read");
+        return -1;
+    }
+    // the turn's event covers this read or a later one of the same turn,
+    // which the stream ordered after it
+    return cuda_ok(cudaEventSynchronize(s->read_done[ticket & 1]), "sph_wait_read") ? 0 : -1;
+}
+
+extern "C" int sph_wait_reads(psdata_cuda pso) {
+    Store *s = store_of(pso, "sph_wait_reads");
+    if (!s) return -1;
+    return drain_reads(s, "sph_wait_reads") ? 0 : -1;
 }
 
 extern "C" int sph_update(psdata_cuda pso, unsigned num_steps) {

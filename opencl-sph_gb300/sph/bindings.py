@@ -200,6 +200,12 @@ _SIGS = {
     "set_body_rotation_device_opencl": ([psdata_cuda, c_uint, POINTER(c_float)], None),
     # additions
     "sph_synchronize": ([psdata_cuda], c_int),
+    "sph_pin_host": ([psdata, psdata_cuda], c_int),
+    "sph_unpin_host": ([psdata_cuda], c_int),
+    "sph_write_fields_async": ([psdata, psdata_cuda, c_size_t, _names], c_int),
+    "sph_read_fields_async": ([psdata, psdata_cuda, c_size_t, _names], ctypes.c_longlong),
+    "sph_wait_read": ([psdata_cuda, ctypes.c_longlong], c_int),
+    "sph_wait_reads": ([psdata_cuda], c_int),
     "sph_update": ([psdata_cuda, c_uint], c_int),
     "sph_record_start": ([psdata_cuda, c_size_t, _names, c_uint, c_uint], c_int),
     "sph_record_stop": ([psdata_cuda], c_int),

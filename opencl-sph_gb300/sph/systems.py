@@ -136,6 +136,42 @@ class ParticleSystem(object):
         if bnd.sph_synchronize(self.psdata_opencl) != 0:
             raise bnd.SphError(bnd.last_error())
 
+    # asynchronous transfers --------------------------------------------------
+    def pin(self):
+        """Page-locks the host store, so that the asynchronous transfers
+        below run on the copy engines (released by unpin or free)."""
+        if bnd.sph_pin_host(self.psdata, self.psdata_opencl) != 0:
+            raise bnd.SphError(bnd.last_error())
+        self._pinned = True
+
+    def unpin(self):
+        if bnd.sph_unpin_host(self.psdata_opencl) != 0:
+            raise bnd.SphError(bnd.last_error())
+        self._pinned = False
+
+    def write_fields_async(self, *args):
+        """sync_fields_host_to_device without the wait: the named fields of
+        the host store must stay unchanged until a later blocking call."""
+        if bnd.sph_write_fields_async(self.psdata, self.psdata_opencl, len(args), self._names(args)) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def read_fields_async(self, *args):
+        """Snapshots the named fields after the work enqueued so far and
+        copies them into the host store while later substeps run; returns a
+        ticket for wait_read, after which get_fields sees the snapshot."""
+        t = bnd.sph_read_fields_async(self.psdata, self.psdata_opencl, len(args), self._names(args))
+        if t < 0:
+            raise bnd.SphError(bnd.last_error())
+        return t
+
+    def wait_read(self, ticket):
+        if bnd.sph_wait_read(self.psdata_opencl, ticket) != 0:
+            raise bnd.SphError(bnd.last_error())
+
+    def wait_reads(self):
+        if bnd.sph_wait_reads(self.psdata_opencl) != 0:
+            raise bnd.SphError(bnd.last_error())
+
     def status(self):
         return bnd.sph_status(self.psdata_opencl)
 
@@ -197,11 +233,19 @@ class ParticleSystem(object):
             self.setup()
 
     def free(self):
+        self._release_pin()
         free_data(self.psdata, self.psdata_opencl)
         self.fields = {}
 
+    def _release_pin(self):
+        # free_data frees the host blob before the device store (the
+        # reference's order), so the page-locking ends here, before either
+        if getattr(self, "_pinned", False):
+            self.unpin()
+
     def close(self):
         """Frees the store (the reference's free() rebuilds it afterwards)."""
+        self._release_pin()
         free_data(self.psdata, self.psdata_opencl)
         self.fields = {}
         self.psdata = self.psdata_opencl = None

@@ -240,3 +240,54 @@ def test_device_recording_equals_host_syncs():
     a.update_fused(1)
     a.close()
     b.close()
+
+
+def test_async_store_transfers_match_blocking_syncs():
+    """The store's asynchronous transfers give what the blocking syncs give:
+    a read holds the fields as of its place in the stream although later
+    substeps run while it is written, an asynchronous upload acts like the
+    blocking one, and pipelined reads end on the final state."""
+    sc = scenes.wcsph_block(14, 10, 12, jitter=1e-4, seed=21)
+    a, b = sc.system(), sc.system()
+    a.pin()
+    a.pin()  # pinning twice is harmless
+    a.update_fused(3)
+    b.update_fused(3)
+    t = a.read_fields_async("position", "velocity")
+    a.update_fused(4)
+    a.wait_read(t)
+    b.sync_fields_device_to_host("position", "velocity")
+    pa, va = (np.array(x) for x in a.get_fields("position", "velocity"))
+    pb, vb = b.get_fields("position", "velocity")
+    assert np.array_equal(pa, pb) and np.array_equal(va, vb)
+    # an asynchronous upload of gravity, then pipelined reads
+    b.update_fused(4)
+    for ps in (a, b):
+        ps.get_fields("gravity")[0][:] = (0.5, -3.0, 0.25)
+    a.write_fields_async("gravity")
+    b.sync_fields_host_to_device("gravity")
+    prev = None
+    for _ in range(5):
+        a.update_fused(1)
+        tk = a.read_fields_async("position")
+        if prev is not None:
+            a.wait_read(prev)
+        prev = tk
+    a.wait_reads()
+    b.update_fused(5)
+    b.sync_fields_device_to_host("position")
+    assert np.array_equal(np.array(a.get_fields("position")[0]), np.array(b.get_fields("position")[0]))
+    # a blocking sync after reads in flight sees the newest state
+    a.update_fused(2)
+    b.update_fused(2)
+    a.read_fields_async("position")
+    a.sync_fields_device_to_host("velocity", "position")
+    b.sync_fields_device_to_host("velocity", "position")
+    assert np.array_equal(np.array(a.get_fields("position")[0]), np.array(b.get_fields("position")[0]))
+    with pytest.raises(Exception):
+        a.read_fields_async("no_such_field")
+    with pytest.raises(Exception):
+        a.wait_read(10 ** 9)
+    a.unpin()
+    a.close()
+    b.close()
