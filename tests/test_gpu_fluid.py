@@ -291,3 +291,43 @@ def test_async_store_transfers_match_blocking_syncs():
     a.unpin()
     a.close()
     b.close()
+
+
+def test_known_answers_single_particle_and_pair():
+    """Hand-checkable cases on the CUDA path: a lone particle's density is
+    its own weight m 315/(64 pi h^3) with one neighbour (itself) and no
+    force but gravity; two particles at distance r < h have equal densities
+    m (W(0) + W(r)), two neighbours each, and equal and opposite forces
+    along the line between them."""
+    one = scenes.wcsph_block(1, 1, 1, jitter=0.0, walls=False, gravity=(0.0, 0.0, 0.0))
+    ps = one.system()
+    ps.compute_particle_bins()
+    ps.call_for_all_particles("compute_density")
+    ps.call_for_all_particles("compute_forces_fluids")
+    ps.sync_device_to_host()
+    h = float(ps.get_fields("smoothingradius")[0].ravel()[0])
+    m = float(ps.get_fields("mass")[0].ravel()[0])
+    pi = float(np.float32(3.1415926535))
+    w0 = 315.0 / (64.0 * pi * h ** 3)
+    assert ps.get_fields("density")[0][0] == pytest.approx(m * w0, rel=1e-6)
+    assert int(ps.get_fields("num_neighbours")[0][0]) == 1
+    assert np.all(ps.get_fields("force")[0][0] == 0.0)
+    ps.close()
+
+    two = scenes.wcsph_block(2, 1, 1, spacing=0.013, jitter=0.0, walls=False, gravity=(0.0, 0.0, 0.0))
+    ps = two.system()
+    ps.compute_particle_bins()
+    ps.call_for_all_particles("compute_density")
+    ps.call_for_all_particles("compute_forces_fluids")
+    ps.sync_device_to_host()
+    m = float(ps.get_fields("mass")[0].ravel()[0])
+    x = ps.get_fields("position")[0][:2].astype(np.float64)
+    r = float(np.linalg.norm(x[1] - x[0]))
+    want = m * 315.0 / (64.0 * pi * h ** 9) * ((h * h) ** 3 + (h * h - r * r) ** 3)
+    rho = ps.get_fields("density")[0][:2]
+    assert rho[0] == rho[1] and rho[0] == pytest.approx(want, rel=1e-5)
+    assert list(ps.get_fields("num_neighbours")[0][:2]) == [2, 2]
+    f = ps.get_fields("force")[0][:2].astype(np.float64)
+    assert np.all(f[0] == -f[1]) and f[0][0] != 0.0
+    assert f[0][1] == 0.0 and f[0][2] == 0.0
+    ps.close()
