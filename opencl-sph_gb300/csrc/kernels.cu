@@ -52,8 +52,8 @@ void sph_launch_scan(const Launch &L, bool sums_ready) {
 }
 
 void sph_launch_insert(const Launch &L) {
-    k_scatter<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
-    k_rank_cells<<<grid_for(L.particles, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+    k_scatter<<<wide_grid(L.particles.num, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
+    k_rank_cells<<<wide_grid(L.particles.num, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
     // crowded cells are rare: a few blocks per scene walk its queue
     const unsigned gy = L.num_scenes < 65535u ? (L.num_scenes ? L.num_scenes : 1u) : 65535u;
     k_sort_big_cells<<<dim3(L.num_scenes > 1 ? 4 : 32, gy), 1024, 0, L.stream>>>(L.scenes, L.num_scenes);

@@ -13,32 +13,87 @@
 
 #include "kernels_common.cuh"
 
+// The scatter and the per-cell ranking are chains of dependent loads (work
+// entry -> scene -> gridcell -> celloffset -> the cell's entries), so each
+// of their blocks takes SPH_WIDE consecutive work entries per pass and runs
+// their chains side by side: the loads of all entries are issued before any
+// result is used, and a launch needs a quarter of the blocks.
+#define SPH_WIDE 4
+
+struct WideItem {
+    const SceneDesc *S;  // null: no entry, or the scene idles
+    unsigned item;
+    bool valid;          // item < the scene's active count
+};
+
+__device__ __forceinline__ void wide_items(const SceneDesc *__restrict__ scenes, const BlockMap &map, unsigned v0,
+                                           WideItem (&w)[SPH_WIDE]) {
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j) {
+        w[j].S = nullptr;
+        w[j].item = 0u;
+        w[j].valid = false;
+        const unsigned v = v0 + j;
+        if (v < map.num) {
+            const BlockWork bw = map.work[v];
+            const SceneDesc *S = scenes + bw.scene;
+            if (!scene_idle(*S)) {
+                w[j].S = S;
+                w[j].item = bw.first + threadIdx.x;
+                w[j].valid = w[j].item < active_count(*S);
+            }
+        }
+    }
+}
+
+#define SPH_FOR_WIDE(map)                                                                       \
+    for (unsigned v0_ = blockIdx.x * SPH_WIDE; v0_ < (map).num; v0_ += gridDim.x * SPH_WIDE) { \
+        WideItem W[SPH_WIDE];                                                                   \
+        wide_items(scenes, map, v0_, W);
+#define SPH_END_WIDE }
+
+// Blocks for a wide launch over `map`, at most `cap`.
+__host__ __device__ inline unsigned wide_grid(unsigned num, unsigned cap) {
+    const unsigned g = (num + SPH_WIDE - 1) / SPH_WIDE;
+    const unsigned c = g < cap ? g : cap;
+    return c ? c : 1u;
+}
+
+// find_particle_bins' cell coordinate (common.cl:372-391): clamp((uint)((p
+// - b0)/(b1 - b0)*R), 0, R-1) with each float operation individually
+// rounded and a saturating conversion; *outside is set for a particle
+// outside gridbounds.
+__device__ __forceinline__ unsigned cell_of(const SceneDesc &S, float3 p, bool *outside) {
+    const float *gb = S.gridbounds;
+    const float q[3] = {p.x, p.y, p.z};
+    unsigned c[3];
+    bool out = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float lo = gb[2 * a], hi = gb[2 * a + 1];
+        const float r = (float)S.gridres[a];
+        const float v = __fmul_rn(__fdiv_rn(__fsub_rn(q[a], lo), __fsub_rn(hi, lo)), r);
+        unsigned u = __float2uint_rz(v);  // saturating: negative and NaN -> 0
+        if (u > S.gridres[a] - 1) u = S.gridres[a] - 1;
+        out |= !(v >= 0.f && v < r);
+        c[a] = u;
+    }
+    *outside = out;
+    return c[2] * S.gridres[0] * S.gridres[1] + c[1] * S.gridres[0] + c[0];
+}
+
 // find_particle_bins (common.cl:372-391) fused with count_particles_in_bins
-// (:401-408).  The cell coordinate is clamp((uint)((p-b0)/(b1-b0)*R), 0,
-// R-1) with each float operation individually rounded and a saturating
-// conversion.  Lanes of a warp that hit the same cell combine into one
-// atomicAdd; each particle keeps its arrival slot within the cell.
+// (:401-408).  Lanes of a warp that hit the same cell combine into one
+// atomicAdd; each particle keeps its arrival slot within the cell.  (One
+// work entry per block: the wide form measured slower here.)
 __global__ void k_bin_count(const SceneDesc *__restrict__ scenes, BlockMap map, int do_count) {
     SPH_FOR_WORK(map)
     const unsigned n = active_count(S);
     const bool valid = item < n;
     const unsigned lanes = __ballot_sync(SPH_FULL_MASK, valid);
     if (valid) {
-        const float *gb = S.gridbounds;
-        float3 p = ld3(S.position, item);
-        float q[3] = {p.x, p.y, p.z};
-        unsigned c[3];
-        bool outside = false;
-        for (int a = 0; a < 3; ++a) {
-            float lo = gb[2 * a], hi = gb[2 * a + 1];
-            float r = (float)S.gridres[a];
-            float v = __fmul_rn(__fdiv_rn(__fsub_rn(q[a], lo), __fsub_rn(hi, lo)), r);
-            unsigned u = __float2uint_rz(v);  // saturating: negative and NaN -> 0
-            if (u > S.gridres[a] - 1) u = S.gridres[a] - 1;
-            outside |= !(v >= 0.f && v < r);
-            c[a] = u;
-        }
-        const unsigned cell = c[2] * S.gridres[0] * S.gridres[1] + c[1] * S.gridres[0] + c[0];
+        bool outside;
+        const unsigned cell = cell_of(S, ld3(S.position, item), &outside);
         S.gridcell[item] = cell;
         if (outside) atomicOr(S.status, (unsigned)STATUS_OUTSIDE_GRID);
         if (do_count) {
@@ -190,15 +245,28 @@ __global__ void __launch_bounds__(SPH_SCAN_THREADS) k_scan_down(const SceneDesc 
 __device__ __forceinline__ unsigned *unsorted_cells(const SceneDesc &S) { return reinterpret_cast<unsigned *>(S.spos); }
 
 __global__ void k_scatter(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    SPH_FOR_WORK(map)
-    if (item < active_count(S)) {
-        const unsigned cell = S.gridcell[item];
-        if (cell < S.num_cells) {
-            const unsigned dst = S.celloffset[cell] + S.slot[item];
-            if (dst < S.pnum) unsorted_cells(S)[dst] = item;
+    SPH_FOR_WIDE(map)
+    unsigned cell[SPH_WIDE], slot[SPH_WIDE];
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j)
+        if (W[j].valid) {
+            cell[j] = W[j].S->gridcell[W[j].item];
+            slot[j] = W[j].S->slot[W[j].item];
         }
+    unsigned off[SPH_WIDE];
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j) {
+        off[j] = 0xffffffffu;
+        if (W[j].valid && cell[j] < W[j].S->num_cells) off[j] = W[j].S->celloffset[cell[j]];
     }
-    SPH_END_WORK
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j)
+        if (off[j] != 0xffffffffu) {
+            const SceneDesc &S = *W[j].S;
+            const unsigned dst = off[j] + slot[j];
+            if (dst < S.pnum) unsorted_cells(S)[dst] = W[j].item;
+        }
+    SPH_END_WIDE
 }
 
 // Canonical order inside each cell: ascending particle index.  One thread
@@ -207,30 +275,44 @@ __global__ void k_scatter(const SceneDesc *__restrict__ scenes, BlockMap map) {
 // SPH_SMALL_CELL particles are copied as they are and queued (by the thread
 // of their first slot) for k_sort_big_cells.
 __global__ void k_rank_cells(const SceneDesc *__restrict__ scenes, BlockMap map) {
-    SPH_FOR_WORK(map)
-    if (item < active_count(S)) {
-        const unsigned *U = unsorted_cells(S);
-        const unsigned x = U[item];
-        const unsigned cell = x < S.pnum ? S.gridcell[x] : 0xffffffffu;
-        if (cell < S.num_cells) {
-            const unsigned off = S.celloffset[cell], cnt = S.gridcount[cell];
-            // inconsistent tables come only from host-written garbage: skip
-            if (off <= item && item - off < cnt && cnt <= S.pnum - off) {
-                if (cnt > SPH_SMALL_CELL) {
-                    S.cellparticles[item] = x;
-                    if (item == off) {
-                        const unsigned k = atomicAdd(S.big_cells, 1u);
-                        S.big_cells[1 + k] = cell;
-                    }
-                } else {
-                    unsigned r = 0;
-                    for (unsigned a2 = 0; a2 < cnt; ++a2) r += U[off + a2] < x;
-                    S.cellparticles[off + r] = x;
+    SPH_FOR_WIDE(map)
+    unsigned x[SPH_WIDE], cell[SPH_WIDE];
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j) x[j] = W[j].valid ? unsorted_cells(*W[j].S)[W[j].item] : 0xffffffffu;
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j)
+        cell[j] = W[j].valid && x[j] < W[j].S->pnum ? W[j].S->gridcell[x[j]] : 0xffffffffu;
+    unsigned off[SPH_WIDE], cnt[SPH_WIDE];
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j) {
+        off[j] = 0u;
+        cnt[j] = 0u;
+        if (W[j].valid && cell[j] < W[j].S->num_cells) {
+            off[j] = W[j].S->celloffset[cell[j]];
+            cnt[j] = W[j].S->gridcount[cell[j]];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < SPH_WIDE; ++j) {
+        const unsigned item = W[j].item;
+        // inconsistent tables come only from host-written garbage: skip
+        if (cnt[j] && off[j] <= item && item - off[j] < cnt[j] && cnt[j] <= W[j].S->pnum - off[j]) {
+            const SceneDesc &S = *W[j].S;
+            if (cnt[j] > SPH_SMALL_CELL) {
+                S.cellparticles[item] = x[j];
+                if (item == off[j]) {
+                    const unsigned k = atomicAdd(S.big_cells, 1u);
+                    S.big_cells[1 + k] = cell[j];
                 }
+            } else {
+                const unsigned *U = unsorted_cells(S) + off[j];
+                unsigned r = 0;
+                for (unsigned a2 = 0; a2 < cnt[j]; ++a2) r += U[a2] < x[j];
+                S.cellparticles[off[j] + r] = x[j];
             }
         }
     }
-    SPH_END_WORK
+    SPH_END_WIDE
 }
 
 // Fallback for crowded cells (e.g. particles clamped into an edge cell):
