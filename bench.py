@@ -97,6 +97,21 @@ MEASURED_TRAFFIC = {
     ("batched-256", "svk forces+step"): 162.05e6,               # k_forces_solids<0, 1> (with the step)
 }
 
+# Warp instructions per launch of the same kernels (ncu
+# smsp__inst_executed.sum, same captures as the traffic above): with the
+# live phase time they give the issue rate, against 4 warp instructions per
+# SM per clock.
+MEASURED_INST = {
+    ("wcsph-1m", "density"): 190.31e6,                          # k_density<false>
+    ("wcsph-1m", "forces_fluids+step"): 191.99e6,               # k_forces_fluids_masked
+    ("batched-256", "density"): 493.39e6,
+    ("batched-256", "fluid forces+step"): 494.24e6,
+    ("batched-256", "corotational rotations"): 498.80e6,
+    ("batched-256", "corotational forces+step"): 285.16e6,
+    ("batched-256", "svk deformations"): 384.29e6,
+    ("batched-256", "svk forces+step"): 282.13e6,
+}
+
 
 def workload(name, seed):
     from sph import scenes
@@ -209,10 +224,32 @@ def _solid_setup(ps):
     ps.call_for_all_particles("compute_original_density")
 
 
-def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None, workload=None):
+def _issue_roofline(phases, workload, clocks):
+    """The instruction-issue limit of each captured phase kernel: its warp
+    instructions per launch over its live time, against 4 warp instructions
+    per SM per clock at the SM clock sampled under load."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz")
+    if not mhz:
+        return None
+    peak = 4.0 * sms * mhz * 1e6 / 1e12
+    per = {}
+    for ph, ms in phases.items():
+        inst = MEASURED_INST.get((workload, ph))
+        if inst and ms:
+            a = inst / (ms * 1e-3) / 1e12
+            per[ph] = {"achieved": a, "frac": a / peak, "warp_instructions_per_launch": inst}
+    return {"unit": "T warp-instructions/s", "peak": peak, "sm_mhz": mhz, "sms": sms, "phases": per,
+            "source": "instruction counts from ncu (profiles/*_passes_*.md), times live"}
+
+
+def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None, workload=None, clocks=None):
     """Roofline of the phase that takes longest: its algorithmic bytes (for
     the particles and cells it processes) over its measured time; traffic is
-    the measured DRAM bytes of that phase's kernel where captured."""
+    the measured DRAM bytes of that phase's kernel where captured.  `issue`
+    sets the pair kernels against the instruction-issue limit that binds
+    them."""
     dom = max(phases, key=phases.get)
     bp, bc = PHASE_BYTES.get(dom, (0, 0))
     pn, pc = (counts or {}).get(dom, (n, cells))
@@ -221,7 +258,8 @@ def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None, workload=Non
     return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
             "traffic": MEASURED_TRAFFIC.get((workload, dom)),
-            "algorithmic_bytes_per_launch": alg, "phase_ms": phases}
+            "algorithmic_bytes_per_launch": alg, "phase_ms": phases,
+            "issue": _issue_roofline(phases, workload, clocks)}
 
 
 def bench_plain(args, scene, torch, world):
@@ -685,7 +723,7 @@ def run_ours(args, rank, world, local_rank):
             extra["plain_1m"] = {"workload": "wcsph-1m: " + d1m, "value": p1["n"] * args.steps / p1["total_s"],
                                  "ms_per_step": p1["total_s"] * 1e3 / args.steps,
                                  "roofline": _phase_roofline(p1["phases"], p1["n"], p1["cells"], peak, peak_kind,
-                                                             workload="wcsph-1m"),
+                                                             workload="wcsph-1m", clocks=p1["clocks"]),
                                  "e2e": p1["e2e"]}
     else:
         scene, desc = workload(args.workload, args.seed + rank)
@@ -728,7 +766,7 @@ def run_ours(args, rank, world, local_rank):
         "e2e": r["e2e"],
         "gpu_launches": r["kernels_per_step"] * args.steps,
         "roofline": _phase_roofline(r["phases"], n, r["cells"], peak, peak_kind, r.get("counts"),
-                                    workload=args.workload),
+                                    workload=args.workload, clocks=r["clocks"]),
     }
     line.update(extra)
     return line
