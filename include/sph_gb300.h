@@ -201,8 +201,8 @@ int sph_unpin_host(psdata_cuda pso);
 /* sync_psdata_fields_host_to_device (particle_system_host.c:812-829)
  * without the wait: the copies are enqueued on the store's stream, so the
  * named fields of `data` must stay unchanged until the stream has passed
- * them (a later blocking call or sph_synchronize).  An unknown name is an
- * error (-1). */
+ * them (a later blocking call or sph_synchronize).  An unknown name is
+ * logged and skipped, as in the blocking sync.  Returns 0 or -1. */
 int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_fields, const char *const *names);
 /* sync_psdata_fields_device_to_host (particle_system_host.c:843-858)
  * without the wait: the fields are copied to a device snapshot in stream

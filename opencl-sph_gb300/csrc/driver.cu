@@ -619,6 +619,10 @@ extern "C" int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_f
     const char *what = "sph_write_fields_async";
     Store *s = store_of(pso, what);
     if (!s) return -1;
+    if (num_fields && !names) {
+        sph_set_error("%s: no field names", what);
+        return -1;
+    }
     bool rigid = false;
     for (size_t i = 0; i < num_fields; ++i) {
         if (names[i] && !copy_field(s, data, names[i], true)) return -1;
@@ -638,6 +642,10 @@ extern "C" long long sph_read_fields_async(psdata data, psdata_cuda pso, size_t 
     if (!s) return -1;
     if (psdata_data_size(data) != s->blob_size || !data.data) {
         sph_set_error("%s: store layout differs from the device copy", what);
+        return -1;
+    }
+    if (num_fields && !names) {
+        sph_set_error("%s: no field names", what);
         return -1;
     }
     if (!s->reads) {
