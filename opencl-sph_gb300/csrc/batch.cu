@@ -80,6 +80,7 @@ struct sph_batch {
     unsigned snap_seg_cap[2] = {0, 0};
     CopySeg *seg_host[2] = {nullptr, nullptr};  // pinned: the upload must not wait for the stream
     size_t seg_host_cap[2] = {0, 0};
+    unsigned seg_count[2] = {0, 0};             // segments in turn t's device table (0: none)
     long long tickets = 0;  // reads enqueued so far
 };
 
@@ -690,22 +691,33 @@ extern "C" long long sph_batch_read_field_many_async(sph_batch *b, const int *id
         return -1;
     b->snap_seg_cap[t] = (unsigned)seg_cap;
     for (unsigned k = 0; k < count; ++k) segs[k].dst = b->snap[t] + at[k];
-    // turn t's pinned table was last uploaded before the snapshot two
-    // tickets back
-    if (!ok(cudaEventSynchronize(b->snap_done[t]), what)) return -1;
-    if (segs.size() > b->seg_host_cap[t]) {
-        if (b->seg_host[t]) cudaFreeHost(b->seg_host[t]);
-        b->seg_host[t] = nullptr;
-        b->seg_host_cap[t] = 0;
-        const size_t c = segs.size() * 2;
-        if (!ok(cudaMallocHost((void **)&b->seg_host[t], c * sizeof(CopySeg)), what)) return -1;
-        b->seg_host_cap[t] = c;
+    // a frame loop reads the same field of the same scenes every time: the
+    // turn's device table is then current and is not uploaded again (the
+    // pinned copy holds what was uploaded, and `grow` kept the table)
+    const bool same = b->seg_count[t] == count && b->snap_segs[t] && b->seg_host[t] &&
+                      std::equal(segs.begin(), segs.end(), b->seg_host[t], [](const CopySeg &x, const CopySeg &y) {
+                          return x.src == y.src && x.dst == y.dst && x.bytes == y.bytes;
+                      });
+    if (!same) {
+        // turn t's pinned table was last uploaded before the snapshot two
+        // tickets back
+        if (!ok(cudaEventSynchronize(b->snap_done[t]), what)) return -1;
+        b->seg_count[t] = 0;
+        if (segs.size() > b->seg_host_cap[t]) {
+            if (b->seg_host[t]) cudaFreeHost(b->seg_host[t]);
+            b->seg_host[t] = nullptr;
+            b->seg_host_cap[t] = 0;
+            const size_t c = segs.size() * 2;
+            if (!ok(cudaMallocHost((void **)&b->seg_host[t], c * sizeof(CopySeg)), what)) return -1;
+            b->seg_host_cap[t] = c;
+        }
+        std::copy(segs.begin(), segs.end(), b->seg_host[t]);
+        if (!ok(cudaMemcpyAsync(b->snap_segs[t], b->seg_host[t], segs.size() * sizeof(CopySeg),
+                                cudaMemcpyHostToDevice, b->stream),
+                what))
+            return -1;
+        b->seg_count[t] = count;
     }
-    std::copy(segs.begin(), segs.end(), b->seg_host[t]);
-    if (!ok(cudaMemcpyAsync(b->snap_segs[t], b->seg_host[t], segs.size() * sizeof(CopySeg), cudaMemcpyHostToDevice,
-                            b->stream),
-            what))
-        return -1;
     // the snapshot, in stream order after the substeps enqueued so far
     sph_launch_copy_segments(b->snap_segs[t], count, max_bytes, b->stream);
     if (!ok(cudaEventRecord(b->snap_done[t], b->stream), what) ||
