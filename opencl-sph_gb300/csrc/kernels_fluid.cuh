@@ -77,15 +77,17 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             __syncwarp();
         }
         const unsigned len = e - b;
-        unsigned long long bits = 0;
-        auto visit = [&](float3 jpos, unsigned t) {
+        // the row's mask in two words, each filled by its own loop below
+        // (a 32-bit shift per neighbour, no test of the candidate's place)
+        unsigned lo = 0, hi = 0;
+        auto visit = [&](float3 jpos, unsigned *word, unsigned bit) {
             const float r2 = norm2(sub3(jpos, ipos));
             if (r2 <= B.le) {
                 const float d = fmaxf(h2 - r2, 0.f);
                 rho.add(d * d * d);
                 // a fused plane-free substep counts in the force pass
                 if (!MASK || PLANES) count += r2 <= B.lt;
-                if (MASK && t < 64) bits |= 1ull << t;
+                if (MASK && word) *word |= 1u << bit;
             }
             if (PLANES && P.imask) {
                 const unsigned jm = plane_jmask(P, jpos, h);
@@ -104,14 +106,23 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
                 }
             }
         };
+        // candidates [0, 32) set bits of `lo`, [32, 64) of `hi`; a row
+        // longer than 64 (the later passes scan it) records none past 64
+        const unsigned n1 = len < 32u ? len : 32u, n2 = len < 64u ? len : 64u;
         if (staged) {
             const float4 *src = wstage + (b - ub);
 #pragma unroll 4
-            for (unsigned t = 0; t < len; ++t) visit(xyz(src[t]), t);
+            for (unsigned t = 0; t < n1; ++t) visit(xyz(src[t]), &lo, t);
+#pragma unroll 4
+            for (unsigned t = n1; t < n2; ++t) visit(xyz(src[t]), &hi, t - 32u);
+            for (unsigned t = n2; t < len; ++t) visit(xyz(src[t]), nullptr, 0u);
         } else {
-            for (unsigned t = 0; t < len; ++t) visit(xyz(spos[b + t]), t);
+            for (unsigned t = 0; t < n1; ++t) visit(xyz(spos[b + t]), &lo, t);
+            for (unsigned t = n1; t < n2; ++t) visit(xyz(spos[b + t]), &hi, t - 32u);
+            for (unsigned t = n2; t < len; ++t) visit(xyz(spos[b + t]), nullptr, 0u);
         }
         if (MASK && active) {
+            const unsigned long long bits = ((unsigned long long)hi << 32) | lo;
             store_row_mask(S, k, r, len, bits);
             overflow |= len > 64;
             total += len;
