@@ -240,11 +240,15 @@ __device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, 
     for (int r = 0; r < 9; ++r) {
         unsigned b, e;
         rows.row(S, r, &b, &e);
-        unsigned long long m = load_row_mask(S, k, r, e - b);
-        while (m) {
-            const unsigned t = (unsigned)(__ffsll((long long)m) - 1);
-            m &= m - 1ull;
-            f(b + t);
+        const unsigned long long mask = load_row_mask(S, k, r, e - b);
+        // the row's two mask words in turn, with 32-bit bit scans
+#pragma unroll 1
+        for (unsigned w = 0, m = (unsigned)mask; w < 2; ++w, m = (unsigned)(mask >> 32), b += 32) {
+            while (m) {
+                const unsigned t = (unsigned)(__ffs(m) - 1);
+                m &= m - 1u;
+                f(b + t);
+            }
         }
     }
 }

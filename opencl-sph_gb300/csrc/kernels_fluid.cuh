@@ -304,19 +304,23 @@ __global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restri
             for (int r = 0; r < 9; ++r) {
                 unsigned b, e;
                 rows.row(S, r, &b, &e);
-                unsigned long long m = load_row_mask(S, k, r, e - b);
-                while (m) {
-                    const unsigned t1 = (unsigned)(__ffsll((long long)m) - 1);
-                    m &= m - 1ull;
-                    const float4 p1 = spos[b + t1], v1 = svel[b + t1];
-                    if (m) {
-                        const unsigned t2 = (unsigned)(__ffsll((long long)m) - 1);
-                        m &= m - 1ull;
-                        const float4 p2 = spos[b + t2], v2 = svel[b + t2];
-                        count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
-                        count += fluid_pair(I, xyz(p2), xyz(v2), p2.w, v2.w, f) <= I.B.lt;
-                    } else {
-                        count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                const unsigned long long mask = load_row_mask(S, k, r, e - b);
+                // the row's two mask words in turn, with 32-bit bit scans
+#pragma unroll 1
+                for (unsigned w = 0, m = (unsigned)mask; w < 2; ++w, m = (unsigned)(mask >> 32), b += 32) {
+                    while (m) {
+                        const unsigned t1 = (unsigned)(__ffs(m) - 1);
+                        m &= m - 1u;
+                        const float4 p1 = spos[b + t1], v1 = svel[b + t1];
+                        if (m) {
+                            const unsigned t2 = (unsigned)(__ffs(m) - 1);
+                            m &= m - 1u;
+                            const float4 p2 = spos[b + t2], v2 = svel[b + t2];
+                            count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                            count += fluid_pair(I, xyz(p2), xyz(v2), p2.w, v2.w, f) <= I.B.lt;
+                        } else {
+                            count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                        }
                     }
                 }
             }
