@@ -217,12 +217,15 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
 // from the neighbour's pressure pj and reciprocal density inv_rhoj.  Every
 // rounding is pinned, so the scan and the mask walk produce the same sum.
 // Distinct particles at exactly zero distance (and i itself) contribute
-// nothing.  Returns r^2 (the neighbour count's test).
+// nothing.  Returns r^2 (the neighbour count's test).  IN_RANGE: the caller
+// walks the density pass's masks, whose candidates passed r^2 <= le with
+// the same positions and arithmetic, so that test is not repeated.
+template <bool IN_RANGE = false>
 __device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3 jvel, float pj, float inv_rhoj,
                                             Kahan3 &f) {
     const float3 d = sub3(jpos, I.ipos);
     const float r2 = norm2(d);
-    if (!(r2 <= I.B.le) || r2 == 0.f) return r2;
+    if ((!IN_RANGE && !(r2 <= I.B.le)) || r2 == 0.f) return r2;
     const float rinv = rsqrtf(r2);
     const float dist = __fmul_rn(r2, rinv);
     const float din = __fsub_rn(I.h, dist);
@@ -316,10 +319,10 @@ __global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restri
                             const unsigned t2 = (unsigned)(__ffs(m) - 1);
                             m &= m - 1u;
                             const float4 p2 = spos[b + t2], v2 = svel[b + t2];
-                            count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
-                            count += fluid_pair(I, xyz(p2), xyz(v2), p2.w, v2.w, f) <= I.B.lt;
+                            count += fluid_pair<true>(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                            count += fluid_pair<true>(I, xyz(p2), xyz(v2), p2.w, v2.w, f) <= I.B.lt;
                         } else {
-                            count += fluid_pair(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                            count += fluid_pair<true>(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
                         }
                     }
                 }

@@ -909,13 +909,15 @@ struct SolidI {
 //   SVK fe = f_ij - f_ji = v (sigma_i + sigma_j) gW, or 2 v sigma_i gW.
 // The volume factor comes from per-particle reciprocals and the Laplacian's
 // distance from rsqrt, so a pair costs no division or square root.
-template <bool COROT>
+// IN_RANGE: the caller walks the first pass's masks, whose candidates
+// passed this range test with the same positions and arithmetic.
+template <bool COROT, bool IN_RANGE = false>
 __device__ __forceinline__ void solid_pair(const SolidConsts &C, const SolidI &II, const SolidSide &J,
                                            Kahan3 &fe_s, Kahan3 &fv_s) {
     const SolidSide &I = II.side;
     const float3 x = sub3(I.pos0, J.pos0);
     const float r2 = norm2(sub3(J.pos, I.pos));
-    if (!(norm2(x) <= C.le || r2 <= C.le)) return;
+    if (!IN_RANGE && !(norm2(x) <= C.le || r2 <= C.le)) return;
     const float vivj = __fmul_rn(__fmul_rn(__fmul_rn(C.mass, C.mass), I.inv_rho0), J.inv_rho0);
     const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
     float3 fe;
@@ -964,8 +966,14 @@ __global__ void __maxnreg__(80) k_forces_solids(const SceneDesc *__restrict__ sc
             else side_from_fields<COROT>(S, min(S.cellparticles[kk], S.pnum - 1), xyz(S.spos[kk]), C.mass, J);
             solid_pair<COROT>(C, I, J, fe_s, fv_s);
         };
+        // the masks hold neither k itself nor a candidate out of range
+        auto visit_masked = [&](unsigned kk) {
+            SolidSide J;
+            side_from_sorted<COROT>(S, kk, false, J);
+            solid_pair<COROT, true>(C, I, J, fe_s, fv_s);
+        };
         if (MASKED && S.ncand[k] != SPH_NCAND_SCAN)
-            for_each_masked(S, k, StencilRows(S, S.gridcell[i]), visit);
+            for_each_masked(S, k, StencilRows(S, S.gridcell[i]), visit_masked);
         else
             for_each_neighbour(S, S.gridcell[i], visit);
         const float visc = *S.viscosity;
