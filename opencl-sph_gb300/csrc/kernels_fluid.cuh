@@ -298,6 +298,7 @@ __global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restri
         Kahan3 f;
         unsigned count = 0;  // num_neighbours, which the density pass left to this one
         if (S.ncand[k] != SPH_NCAND_SCAN) {
+            count = 1;  // k itself (r^2 = 0), whose mask bit the walk clears
             const float4 *__restrict__ spos = S.spos;
             const float4 *__restrict__ svel = S.svel;
             // two neighbours per iteration: both loads are in flight
@@ -307,7 +308,10 @@ __global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restri
             for (int r = 0; r < 9; ++r) {
                 unsigned b, e;
                 rows.row(S, r, &b, &e);
-                const unsigned long long mask = load_row_mask(S, k, r, e - b);
+                unsigned long long mask = load_row_mask(S, k, r, e - b);
+                // k itself (row 4, its own cell's) adds no force and is
+                // counted above
+                if (r == 4 && k - b < 64u) mask &= ~(1ull << (k - b));
                 // the row's two mask words in turn, with 32-bit bit scans
 #pragma unroll 1
                 for (unsigned w = 0, m = (unsigned)mask; w < 2; ++w, m = (unsigned)(mask >> 32), b += 32) {

@@ -716,8 +716,8 @@ __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restr
             }
             const float scale = C.mass / S.density0[i];
             float D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-            auto pass2 = [&](unsigned kk) {
-                if (kk == k) return;
+            // the masks hold no bit for k itself
+            auto pass2_masked = [&](unsigned kk) {
                 const float3 q = sub3(xyz(spos0[kk]), ipos0);
                 const float3 g = spiky_grad(-q, C.h, C.kv, C.le);
                 if (g.x != 0.f || g.y != 0.f || g.z != 0.f) {
@@ -725,8 +725,11 @@ __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restr
                     add_outer(u * scale, g, D);
                 }
             };
+            auto pass2 = [&](unsigned kk) {
+                if (kk != k) pass2_masked(kk);
+            };
             if (overflow) for_each_neighbour(S, S.gridcell[i], pass2);
-            else for_each_masked(S, k, rows, pass2);
+            else for_each_masked(S, k, rows, pass2_masked);
             float *st = S.strain + 6 * (size_t)i;
             st[0] = D[0];
             st[1] = D[4];
