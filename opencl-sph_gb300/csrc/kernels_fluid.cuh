@@ -304,11 +304,26 @@ __global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restri
             // two neighbours per iteration: both loads are in flight
             // before the first pair's arithmetic (same order)
             const StencilRows rows(S, cell);
+            // the next row's bounds and low mask word are loaded while this
+            // row is walked
+            unsigned nb, ne;
+            rows.row(S, 0, &nb, &ne);
+            unsigned nlo = S.nbmask[k];
 #pragma unroll 1
             for (int r = 0; r < 9; ++r) {
-                unsigned b, e;
-                rows.row(S, r, &b, &e);
-                unsigned long long mask = load_row_mask(S, k, r, e - b);
+                unsigned b = nb;
+                const unsigned len = ne - nb;
+                unsigned lo = nlo & (len >= 32u ? 0xffffffffu : (1u << len) - 1u);
+                if (r < 8) {
+                    rows.row(S, r + 1, &nb, &ne);
+                    nlo = S.nbmask[(size_t)(2 * (r + 1)) * S.pnum + k];
+                }
+                unsigned hi = 0;
+                if (len > 32u) {
+                    hi = S.nbmask[(size_t)(2 * r + 1) * S.pnum + k];
+                    hi &= len >= 64u ? 0xffffffffu : (1u << (len - 32u)) - 1u;
+                }
+                unsigned long long mask = ((unsigned long long)hi << 32) | lo;
                 // k itself (row 4, its own cell's) adds no force and is
                 // counted above
                 if (r == 4 && k - b < 64u) mask &= ~(1ull << (k - b));
