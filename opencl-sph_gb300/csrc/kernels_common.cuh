@@ -234,13 +234,39 @@ __device__ __forceinline__ unsigned long long load_row_mask(const SceneDesc &S, 
 }
 
 // Calls f(kk) for the candidates of particle k's recorded masks, in order.
-template <class F>
+// PREFETCH: the next row's bounds and low mask word are loaded while a row
+// is walked (it pays in the corotational pass 2; the solid force passes,
+// at their register cap, run slower with it).
+template <bool PREFETCH = false, class F>
 __device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {
+    unsigned nb = 0, ne = 0, nlo = 0;
+    if (PREFETCH) {
+        rows.row(S, 0, &nb, &ne);
+        nlo = S.nbmask[k];
+    }
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         unsigned b, e;
-        rows.row(S, r, &b, &e);
-        const unsigned long long mask = load_row_mask(S, k, r, e - b);
+        unsigned long long mask;
+        if (PREFETCH) {
+            b = nb;
+            e = ne;
+            const unsigned len = e - b;
+            const unsigned lo = nlo & (len >= 32u ? 0xffffffffu : (1u << len) - 1u);
+            if (r < 8) {
+                rows.row(S, r + 1, &nb, &ne);
+                nlo = S.nbmask[(size_t)(2 * (r + 1)) * S.pnum + k];
+            }
+            unsigned hi = 0;
+            if (len > 32u) {
+                hi = S.nbmask[(size_t)(2 * r + 1) * S.pnum + k];
+                hi &= len >= 64u ? 0xffffffffu : (1u << (len - 32u)) - 1u;
+            }
+            mask = ((unsigned long long)hi << 32) | lo;
+        } else {
+            rows.row(S, r, &b, &e);
+            mask = load_row_mask(S, k, r, e - b);
+        }
         // the row's two mask words in turn, with 32-bit bit scans
 #pragma unroll 1
         for (unsigned w = 0, m = (unsigned)mask; w < 2; ++w, m = (unsigned)(mask >> 32), b += 32) {

@@ -729,7 +729,7 @@ __global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restr
                 if (kk != k) pass2_masked(kk);
             };
             if (overflow) for_each_neighbour(S, S.gridcell[i], pass2);
-            else for_each_masked(S, k, rows, pass2_masked);
+            else for_each_masked<true>(S, k, rows, pass2_masked);
             float *st = S.strain + 6 * (size_t)i;
             st[0] = D[0];
             st[1] = D[4];
