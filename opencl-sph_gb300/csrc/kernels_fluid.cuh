@@ -286,9 +286,9 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
 // scan the stencil.  It also counts num_neighbours (the candidates closer
 // than h, j = i included), which the fused density pass of a plane-free
 // scene leaves to it.
-// At most 56 registers (70 unbounded): nine blocks per SM instead of seven
-// (0.222 -> 0.2085 ms at 1M particles; 64 gave 0.213).
-__global__ void __maxnreg__(56) k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
+// At most 64 registers: with the current walk 64 beats 56 (0.1886 ->
+// 0.1859 ms at 1M particles), where the earlier walk ran best at 56.
+__global__ void __maxnreg__(64) k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
         const unsigned k = item;
