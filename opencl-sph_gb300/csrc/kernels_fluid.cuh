@@ -33,7 +33,9 @@
 // candidates; a row of more than 64 marks the particle for a scan
 // (ncand[k] = SPH_NCAND_SCAN).  The stores of one row are one coalesced
 // store per warp.
-#define SPH_STAGE 256
+// 128 float4s per warp hold a warp's row union (about 48 candidates in a
+// lattice); 256 measured the same and took twice the shared memory.
+#define SPH_STAGE 128
 
 __host__ __device__ constexpr size_t density_smem_bytes(unsigned block) {
     return sizeof(float4) * SPH_STAGE * (block / 32);
