@@ -233,7 +233,9 @@ bool rebuild(sph_batch *b) {
     if (!ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "batch capture")) return false;
     sph_launch_bins(A);
     sph_launch_gather(A, true, false, true);
-    sph_launch_density(A, false, true, true);  // masks for the fluid scenes only
+    // masks for the fluid scenes only; the plane-free solid scenes' blocks
+    // are not launched at all
+    sph_launch_density_fused(A, b->group[MAT_FLUID].present ? &b->group[MAT_FLUID].L : nullptr);
     cudaEventRecord(b->fork, b->stream);
     for (int m = 0; m < 3; ++m) {
         GroupLaunch &G = b->group[m];
@@ -804,7 +806,7 @@ extern "C" int sph_batch_profile(sph_batch *b, unsigned reps, float *phase_ms, c
         log.mark("gather");
         sph_launch_gather(A, true, false, true);
         log.mark("density");
-        sph_launch_density(A, false, true, true);
+        sph_launch_density_fused(A, b->group[MAT_FLUID].present ? &b->group[MAT_FLUID].L : nullptr);
         for (int m = 0; m < 3; ++m) {
             if (!b->group[m].present) continue;
             Launch G = b->group[m].L;

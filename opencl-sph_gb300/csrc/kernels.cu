@@ -85,6 +85,16 @@ void sph_launch_density(const Launch &L, bool original, bool mask, bool skip_sol
                                                              mask ? 1 : 0, 0);
 }
 
+void sph_launch_density_fused(const Launch &L, const Launch *fluids) {
+    const size_t smem = density_smem_bytes(L.pair_block);
+    if (fluids && fluids->pair_particles.num)
+        k_density<false><<<grid_for(fluids->pair_particles, L.grid_cap), L.pair_block, smem, L.stream>>>(
+            L.scenes, fluids->pair_particles, 0, 1, 1);
+    if (!L.no_symmetry_planes)
+        k_density<true><<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, smem, L.stream>>>(
+            L.scenes, L.pair_particles, 0, 1, 0);
+}
+
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
     if (masked)
         k_forces_fluids_masked<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(

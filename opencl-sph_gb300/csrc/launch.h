@@ -51,6 +51,11 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid = false)
 // skip_solids: a fused substep, where a plane-free solid's first solid pass
 // sums its density
 void sph_launch_density(const Launch &L, bool original, bool mask = false, bool skip_solids = false);
+// The fused batched density: the plane-free instantiation over `fluids`'
+// pair map only (plane-free solids sum their density in their first solid
+// pass), the plane instantiation over every scene of L when some has
+// planes.  `fluids` is null when the batch has no fluid scene.
+void sph_launch_density_fused(const Launch &L, const Launch *fluids);
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked = false);
 // planes_only: skip plane-free scenes (a fused substep's solid force pass
 // stepped them)
