@@ -89,7 +89,7 @@ PHASE_BYTES = {
 # profiles/solid_scan_passes_batched-256.md, profiles/solid_force_passes_batched-256.md).
 MEASURED_TRAFFIC = {
     ("wcsph-1m", "forces_fluids+step"): 116.76e6,               # k_forces_fluids_masked
-    ("batched-256", "density"): 264.37e6,                       # k_density<false> (masks, pressure, 1/density too)
+    ("batched-256", "density"): 263.80e6,                       # k_density<false> (masks, pressure, 1/density too)
     ("batched-256", "fluid forces+step"): 365.99e6,             # k_forces_fluids_masked
     ("batched-256", "corotational rotations"): 243.08e6,        # k_rotations_and_strains (with the stress law)
     ("batched-256", "corotational forces+step"): 242.06e6,      # k_forces_solids<1, 1> (with the step)
@@ -104,7 +104,7 @@ MEASURED_TRAFFIC = {
 MEASURED_INST = {
     ("wcsph-1m", "density"): 183.25e6,                          # k_density<false>
     ("wcsph-1m", "forces_fluids+step"): 173.16e6,               # k_forces_fluids_masked
-    ("batched-256", "density"): 475.32e6,
+    ("batched-256", "density"): 472.37e6,
     ("batched-256", "fluid forces+step"): 448.54e6,
     ("batched-256", "corotational rotations"): 480.37e6,
     ("batched-256", "corotational forces+step"): 260.60e6,
