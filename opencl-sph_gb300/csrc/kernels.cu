@@ -56,7 +56,11 @@ void sph_launch_insert(const Launch &L) {
     k_rank_cells<<<wide_grid(L.particles.num, L.grid_cap), L.block, 0, L.stream>>>(L.scenes, L.particles);
     // crowded cells are rare: a few blocks per scene walk its queue
     const unsigned gy = L.num_scenes < 65535u ? (L.num_scenes ? L.num_scenes : 1u) : 65535u;
-    k_sort_big_cells<<<dim3(L.num_scenes > 1 ? 4 : 32, gy), 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
+    // (a batch: 4 blocks of 256 per scene, most of which find no queue)
+    if (L.num_scenes > 1)
+        k_sort_big_cells<<<dim3(4, gy), 256, 0, L.stream>>>(L.scenes, L.num_scenes);
+    else
+        k_sort_big_cells<<<dim3(32, gy), 1024, 0, L.stream>>>(L.scenes, L.num_scenes);
 }
 
 void sph_launch_bin_count(const Launch &L) {
