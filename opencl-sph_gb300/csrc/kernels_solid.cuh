@@ -670,9 +670,9 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
 // with |p| <= h and records the masks, R = polar(Apq), pass 2 sums D over
 // the masked candidates with |q| <= h.  Body particles keep their rotation and strain
 // (their masks are still recorded).  Also writes the sorted rotation copy.
-// At most 80 registers (96 unbounded; 32 bytes spill to L1): six blocks per
-// SM instead of five (0.707 -> 0.670 ms on batched-256).
-__global__ void __maxnreg__(80) k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map,
+// At most 72 registers (96 unbounded; ~60 bytes spill to L1): seven
+// 128-thread blocks per SM; 80 gave six (0.640 -> 0.597 ms on batched-256).
+__global__ void __maxnreg__(72) k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map,
                                                         int with_density, int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
