@@ -84,9 +84,7 @@ PHASE_BYTES = {
 }
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-# the dominant phase's kernel, from one ncu capture of the same workload
-# (profiles/fluid_pair_passes_wcsph-1m.md, profiles/fluid_pair_passes_batched-256.md,
-# profiles/solid_scan_passes_batched-256.md, profiles/solid_force_passes_batched-256.md).
+# the dominant phase's kernel, from one ncu capture of the same workload.
 MEASURED_TRAFFIC = {
     ("wcsph-1m", "forces_fluids+step"): 116.76e6,               # k_forces_fluids_masked
     ("batched-256", "density"): 263.80e6,                       # k_density<false> (masks, pressure, 1/density too)
@@ -116,15 +114,7 @@ MEASURED_INST = {
 def workload(name, seed):
     from sph import scenes
     if name == "wcsph-1m":
-        # 1,048,576 particles (the configuration's count; a 128^3 lattice
-        # would hold 2,097,152) as a 128 x 64 x 128 slab, 64 layers high.
-        # The reference's fluid force omits the neighbour mass
-        # (fluids.cl:43-56), so stiffness and viscosity act per unit particle
-        # mass: at 1/8 of the dam break's particle mass they are scaled by
-        # 1/8 to keep its sound speed and viscous time (unscaled, the slab
-        # blows up within ten substeps).
-        return scenes.wcsph_block(128, 64, 128, spacing=0.005, h=0.01, box=(0.0, 1.0), jitter=5e-5, seed=seed,
-                                  dt=2e-5, walls=True, stiffness=0.375, viscosity=0.025, name="wcsph-1m"), \
+        return scenes.wcsph_slab_1m(seed), \
             ("1,048,576-particle WCSPH slab, 128x64x128 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s, "
              "stiffness 0.375, viscosity 0.025 (the dam break's 3 and 0.2 scaled by the 1/8 particle mass)")
     if name == "dam-8k":
@@ -247,7 +237,7 @@ def _issue_roofline(phases, workload, clocks):
             a = inst / (ms * 1e-3) / 1e12
             per[ph] = {"achieved": a, "frac": a / peak, "warp_instructions_per_launch": inst}
     return {"unit": "T warp-instructions/s", "peak": peak, "sm_mhz": mhz, "sms": sms, "phases": per,
-            "source": "instruction counts from ncu (profiles/*_passes_*.md), times live"}
+            "source": "instruction counts from ncu captures of the same kernels, times live"}
 
 
 def _phase_roofline(phases, n, cells, peak, peak_kind, counts=None, workload=None, clocks=None):

@@ -364,26 +364,35 @@ unsigned int sph_batch_status(sph_batch *batch, int id);
 
 /* ---- NEW: neighbour grid without allocation -------------------------------
  * No counterpart in the reference.  compute_particle_bins for callers that
- * cannot allocate device memory (inside a CUDA graph capture, in an engine
- * that owns all device memory through its own pool, or in a real-time loop
- * that cannot afford cudaMalloc's implicit synchronisation).  The caller
- * passes device buffers: positions (AoS float[3] x n), gridbounds (6
- * floats), and the outputs gridcell[n], gridcount[rx*ry*rz],
- * celloffset[rx*ry*rz], cellparticles[n], with the meanings and layout of
- * the store fields of the same names.  The scratch is a fixed file-scope
- * device array (about 12.3 MB, held by every GPU that loads the library),
- * so n <= SPH_NOALLOC_MAX_PARTICLES and rx*ry*rz <= SPH_NOALLOC_MAX_CELLS;
+ * cannot allocate device memory: engines and plugin hosts whose own pool
+ * owns all device memory and forbids other allocations in their frame
+ * loop, and real-time loops that cannot afford the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  The caller passes device
+ * buffers: positions (AoS float[3] x n), gridbounds (6 floats), and the
+ * outputs gridcell[n], gridcount[rx*ry*rz], celloffset[rx*ry*rz],
+ * cellparticles[n], with the meanings and layout of the store fields of the
+ * same names.  `status`, when not NULL, is a device word into which the
+ * call ORs its status bits (those of sph_status: bit 1 = a particle lay
+ * outside gridbounds and was clamped into an edge cell); NULL drops them.
+ * The scratch is a fixed file-scope device array (about 12.3 MB, held by
+ * every GPU that loads the library until the process exits), so
+ * n <= SPH_NOALLOC_MAX_PARTICLES and rx*ry*rz <= SPH_NOALLOC_MAX_CELLS;
  * larger sizes return -1 with an error message.  The call allocates
  * nothing, enqueues on `stream` (a cudaStream_t, NULL for the default
- * stream) and returns 0.  Calls share the array: calls that overlap on the
- * GPU race, so order them on one stream.  The first call on a device looks
- * up the array's address; make it before any stream capture. */
+ * stream) and returns 0.  Calls share the array and each starts by
+ * clearing what must start at zero: calls that overlap on the GPU race, so
+ * order them on one stream.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.  The address is looked up again on every call whose stream is
+ * not capturing, so a context made anew (after cudaDeviceReset) is served;
+ * one context per device is assumed. */
 #define SPH_NOALLOC_MAX_PARTICLES (1u << 20)
 #define SPH_NOALLOC_MAX_CELLS (1u << 22)
 int sph_compute_particle_bins_noalloc(const float *position, unsigned int n, const float *gridbounds,
                                       unsigned int rx, unsigned int ry, unsigned int rz,
                                       unsigned int *gridcell, unsigned int *gridcount,
-                                      unsigned int *celloffset, unsigned int *cellparticles, void *stream);
+                                      unsigned int *celloffset, unsigned int *cellparticles,
+                                      unsigned int *status, void *stream);
 
 /* Library and device description (static string). */
 const char *sph_version(void);

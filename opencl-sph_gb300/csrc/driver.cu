@@ -167,6 +167,32 @@ bool refresh_rigid(Store *s, const psdata &data) {
     return true;
 }
 
+// The grid resolution and the particle capacity size the device tables and
+// block maps when the store is created, so an upload may not change them:
+// the reference re-reads gridres on every launch (USE_FIELD), but its
+// gridcount and celloffset fields keep the size the store was built with,
+// and a larger gridres would index past them.  Checked before any copy.
+bool shape_unchanged(const Store *s, const psdata &data, const char *what) {
+    const int fr = get_field_psdata(data, "gridres"), fp = get_field_psdata(data, "pnum");
+    if (fr < 0 || fp < 0) return true;
+    const unsigned *res = (const unsigned *)((const char *)data.data + data.data_offsets[fr]);
+    const unsigned pnum = *(const unsigned *)((const char *)data.data + data.data_offsets[fp]);
+    if (res[0] == s->desc.gridres[0] && res[1] == s->desc.gridres[1] && res[2] == s->desc.gridres[2] &&
+        pnum == s->desc.pnum)
+        return true;
+    sph_set_error("%s: gridres %ux%ux%u / pnum %u differ from the %ux%ux%u / %u the device store was created "
+                  "with; the cell tables and block maps are sized at creation (create a new store instead)",
+                  what, res[0], res[1], res[2], pnum, s->desc.gridres[0], s->desc.gridres[1], s->desc.gridres[2],
+                  s->desc.pnum);
+    return false;
+}
+
+bool names_shape(const char *const *names, size_t num) {
+    for (size_t i = 0; i < num; ++i)
+        if (names[i] && (!strcmp(names[i], "gridres") || !strcmp(names[i], "pnum"))) return true;
+    return false;
+}
+
 // Fields the rigid bodies are set up from.
 bool touches_rigid_setup(const char *name) {
     static const char *kNames[] = {"position", "velocity", "body_number", "body_dynamic", "body_count", "n"};
@@ -461,6 +487,7 @@ extern "C" void sync_psdata_host_to_device(psdata data, psdata_cuda pso, int ful
             sph_set_error("store layout differs from the device copy");
             return false;
         }
+        if (!shape_unchanged(s, data, "sync_psdata_host_to_device")) return false;
         if (!cuda_ok(cudaMemcpyAsync(s->d_blob, data.data, sz, cudaMemcpyHostToDevice, s->stream), "sync") ||
             !refresh_rigid(s, data))
             return false;
@@ -474,6 +501,8 @@ extern "C" void sync_psdata_fields_host_to_device(psdata data, psdata_cuda pso, 
                                                   const char *const *names) {
     with_store(pso, "sync_psdata_fields_host_to_device", true, [&](Store *s) {
         if (!drain_reads(s, "sync_psdata_fields_host_to_device")) return false;
+        if (names_shape(names, num_fields) && !shape_unchanged(s, data, "sync_psdata_fields_host_to_device"))
+            return false;
         bool rigid = false;
         for (size_t i = 0; i < num_fields; ++i) {
             if (names[i] && !copy_field(s, data, names[i], true)) return false;
@@ -623,6 +652,7 @@ extern "C" int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_f
         sph_set_error("%s: no field names", what);
         return -1;
     }
+    if (names_shape(names, num_fields) && !shape_unchanged(s, data, what)) return -1;
     bool rigid = false;
     for (size_t i = 0; i < num_fields; ++i) {
         if (names[i] && !copy_field(s, data, names[i], true)) return -1;

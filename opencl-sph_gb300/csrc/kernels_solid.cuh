@@ -1056,7 +1056,12 @@ __global__ void k_store_body_vec(const SceneDesc *__restrict__ scenes, int which
 // ---- scene init (common.cl:533-604) ------------------------------------------
 
 // populate_position_cuboid: a size.x x size.y x size.z lattice spanning
-// corner1..corner2; sets n as the reference does.
+// corner1..corner2; sets n as the reference does.  Each coordinate is
+// (i / (size - 1)) (c2 - c1) + c1 with every operation rounded on its own
+// (no contraction), so positions equal the reference's bit for bit.
+__device__ __forceinline__ float cuboid_coord(unsigned i, unsigned size, float c1, float c2) {
+    return __fadd_rn(__fmul_rn(__fdiv_rn((float)i, (float)(size - 1)), __fsub_rn(c2, c1)), c1);
+}
 __global__ void k_populate_cuboid(const SceneDesc *__restrict__ scenes, float3 c1, float3 c2, uint3 size) {
     const SceneDesc &S = scenes[0];
     const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1068,14 +1073,20 @@ __global__ void k_populate_cuboid(const SceneDesc *__restrict__ scenes, float3 c
     unsigned *n = const_cast<unsigned *>(S.n);
     if (p == S.pnum - 1) *n = S.pnum;
     else if (i == size.x - 1 && j == size.y - 1 && k == size.z - 1) *n = size.x * size.y * size.z;
-    float3 q = make_float3(((float)i / (float)(size.x - 1)) * (c2.x - c1.x) + c1.x,
-                           ((float)j / (float)(size.y - 1)) * (c2.y - c1.y) + c1.y,
-                           ((float)k / (float)(size.z - 1)) * (c2.z - c1.z) + c1.z);
-    st3(S.position, p, q);
+    st3(S.position, p, make_float3(cuboid_coord(i, size.x, c1.x, c2.x), cuboid_coord(j, size.y, c1.y, c2.y),
+                                   cuboid_coord(k, size.z, c1.z, c2.z)));
 }
 
-// rotate_particles: positions rotated by Rx(ax) Ry(ay) Rz(az) with the
-// source's sign conventions.
+// rotate_particles: positions rotated by Rx(ax) (Ry(ay) Rz(az)) with the
+// source's sign conventions.  The matrix products and the matrix-vector
+// product are rounded term by term in the source's order (no contraction);
+// only cosf/sinf may differ from the host libm's in the last bit.
+__device__ __forceinline__ void mat_mul_rn(const float a[9], const float b[9], float out[9]) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            out[3 * r + c] = __fadd_rn(__fadd_rn(__fmul_rn(a[3 * r], b[c]), __fmul_rn(a[3 * r + 1], b[3 + c])),
+                                       __fmul_rn(a[3 * r + 2], b[6 + c]));
+}
 __global__ void k_rotate_particles(const SceneDesc *__restrict__ scenes, BlockMap map, float ax, float ay, float az) {
     SPH_FOR_WORK(map)
     if (item < active_count(S)) {
@@ -1084,11 +1095,14 @@ __global__ void k_rotate_particles(const SceneDesc *__restrict__ scenes, BlockMa
         const float ry[9] = {cy, 0, -sy, 0, 1, 0, sy, 0, cy};
         const float rz[9] = {cz, -sz, 0, sz, cz, 0, 0, 0, 1};
         float ryz[9], r[9];
-        for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) ryz[3 * a + c] = ry[3 * a] * rz[c] + ry[3 * a + 1] * rz[3 + c] + ry[3 * a + 2] * rz[6 + c];
-        for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) r[3 * a + c] = rx[3 * a] * ryz[c] + rx[3 * a + 1] * ryz[3 + c] + rx[3 * a + 2] * ryz[6 + c];
-        st3(S.position, item, mat_vec(r, ld3(S.position, item)));
+        mat_mul_rn(ry, rz, ryz);
+        mat_mul_rn(rx, ryz, r);
+        const float3 p = ld3(S.position, item);
+        float3 q;
+        q.x = __fadd_rn(__fadd_rn(__fmul_rn(r[0], p.x), __fmul_rn(r[1], p.y)), __fmul_rn(r[2], p.z));
+        q.y = __fadd_rn(__fadd_rn(__fmul_rn(r[3], p.x), __fmul_rn(r[4], p.y)), __fmul_rn(r[5], p.z));
+        q.z = __fadd_rn(__fadd_rn(__fmul_rn(r[6], p.x), __fmul_rn(r[7], p.y)), __fmul_rn(r[8], p.z));
+        st3(S.position, item, q);
     }
     SPH_END_WORK
 }

@@ -5,8 +5,6 @@
 // slots, scan partial sums, the crowded-cell queue and the buffer the
 // crowded-cell sort works in, all carved from one cudaMalloc.  Some callers
 // cannot make that allocation:
-//   - code running while a CUDA graph is being captured, where cudaMalloc
-//     is not allowed;
 //   - engines and plugin hosts that own all device memory through their
 //     own pool and forbid other allocations in their frame loop;
 //   - real-time loops where the implicit device synchronisation of
@@ -21,8 +19,10 @@
 // start of each call.  Calls that overlap on the GPU (on different streams,
 // or from different host threads) race on the array: order them on one
 // stream.  The first call on each device looks up the array's device
-// address (cudaGetSymbolAddress); make that first call before any stream
-// capture.
+// address (cudaGetSymbolAddress) with that device current; make that first
+// call before any stream capture.  Later calls look the address up again
+// whenever their stream is not capturing, so a context that was torn down
+// and made again (cudaDeviceReset) gets the array's new address.
 #include <mutex>
 
 #include "launch.h"
@@ -82,13 +82,18 @@ __global__ void k_noalloc_setup(unsigned char *base, SceneDesc d, unsigned n) {
     for (unsigned b = t; b < ns; b += stride) sm[b] = BlockWork{0u, b * SPH_SCAN_TILE};
 }
 
+// ORs the call's status bits (SphStatus) into the caller's word.
+__global__ void k_noalloc_status(const unsigned char *base, unsigned *out) {
+    *out |= *reinterpret_cast<const unsigned *>(base + kStatus);
+}
+
 }  // namespace
 
 extern "C" int sph_compute_particle_bins_noalloc(const float *position, unsigned int n, const float *gridbounds,
                                                   unsigned int rx, unsigned int ry, unsigned int rz,
                                                   unsigned int *gridcell, unsigned int *gridcount,
                                                   unsigned int *celloffset, unsigned int *cellparticles,
-                                                  void *stream) {
+                                                  unsigned int *status, void *stream) {
     const unsigned long long cells = (unsigned long long)rx * ry * rz;
     if (n > kMaxParticles) {
         sph_set_error("sph_compute_particle_bins_noalloc: %u particles exceed the fixed scratch's limit of %zu",
@@ -111,10 +116,20 @@ extern "C" int sph_compute_particle_bins_noalloc(const float *position, unsigned
         sph_set_error("sph_compute_particle_bins_noalloc: no current device (%s)", cudaGetErrorString(e));
         return -1;
     }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the address is looked up again outside a stream capture (a context
+    // made anew after cudaDeviceReset loads the array elsewhere); a
+    // capturing stream uses the address its device had last
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(s, &cap);
+    if (e != cudaSuccess) {
+        sph_set_error("sph_compute_particle_bins_noalloc: stream: %s", cudaGetErrorString(e));
+        return -1;
+    }
     unsigned char *base;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_base[dev]) {
+        if (!g_base[dev] || cap == cudaStreamCaptureStatusNone) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess) {
@@ -145,7 +160,6 @@ extern "C" int sph_compute_particle_bins_noalloc(const float *position, unsigned
     d.num_scan_blocks = (unsigned)((cells + SPH_SCAN_TILE - 1) / SPH_SCAN_TILE);
     d.big_cells = reinterpret_cast<unsigned *>(base + kBig);
     d.status = reinterpret_cast<unsigned *>(base + kStatus);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     k_noalloc_setup<<<64, 256, 0, s>>>(base, d, n);
 
     Launch L{};
@@ -160,6 +174,7 @@ extern "C" int sph_compute_particle_bins_noalloc(const float *position, unsigned
     L.grid_cap = 1u << 30;
     L.stream = s;
     sph_launch_bins(L);
+    if (status) k_noalloc_status<<<1, 1, 0, s>>>(base, status);
     e = sph_check_launch("sph_compute_particle_bins_noalloc");
     return e == cudaSuccess ? 0 : -1;
 }

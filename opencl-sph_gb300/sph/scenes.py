@@ -168,6 +168,19 @@ def wcsph_block(nx=20, ny=20, nz=20, spacing=0.01, h=0.02, box=(0.0, 0.4), jitte
     return Scene(name or "wcsph-%d" % n, "fluid", FLUID_KERNELS, entries, {"position": pos, "n": n}, n, gen)
 
 
+def wcsph_slab_1m(seed=0):
+    """The 1,048,576-particle WCSPH slab: 128 x 64 x 128 at 0.005 m (the
+    configuration's count; a 128^3 lattice would hold 2,097,152), h = 0.01
+    m, +-5e-5 m jitter, on the floor of a [0,1]^3 box with reflective
+    walls, dt = 2e-5 s.  The reference's fluid force omits the neighbour
+    mass (fluids.cl:43-56), so stiffness and viscosity act per unit
+    particle mass: at 1/8 of the dam break's particle mass its 3 and 0.2
+    are scaled to 0.375 and 0.025 (unscaled, the slab blows up within ten
+    substeps)."""
+    return wcsph_block(128, 64, 128, spacing=0.005, h=0.01, box=(0.0, 1.0), jitter=5e-5, seed=seed, dt=2e-5,
+                       walls=True, stiffness=0.375, viscosity=0.025, name="wcsph-1m")
+
+
 def ball(radius, spacing, center):
     """Lattice points within `radius` of `center` (x-fastest order)."""
     k = int(math.floor(radius / spacing))

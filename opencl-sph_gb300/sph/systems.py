@@ -270,52 +270,6 @@ class StrainSolid(ParticleSystem):
     config = os.path.join(_CONF_DIR, "strainsolid.conf")
     init_values = None
 
-    # device-resident recording ------------------------------------------------
-    def record_start(self, fields, every=1, frames=1024):
-        """Records `fields` on the device every `every` substeps of
-        update_fused into a ring of `frames` frames (no host copy until
-        record_read)."""
-        names = (ctypes.c_char_p * len(fields))(*[f.encode() for f in fields])
-        if bnd.sph_record_start(self.psdata_opencl, len(fields), names, int(every), int(frames)) != 0:
-            raise bnd.SphError(bnd.last_error())
-        self._rec = list(fields)
-        self._rec_frames_n = int(frames)
-
-    def record_stop(self):
-        if bnd.sph_record_stop(self.psdata_opencl) != 0:
-            raise bnd.SphError(bnd.last_error())
-        self._rec = None
-
-    def record_count(self):
-        """Frames recorded so far (the ring keeps the last `frames`)."""
-        return int(bnd.sph_record_count(self.psdata_opencl))
-
-    def record_read(self, first=None, count=None):
-        """The recorded frames [first, first + count) as field -> array of
-        shape (count,) + the field's view shape; by default every frame the
-        ring holds."""
-        total = self.record_count()
-        held = min(total, self._rec_frames()) if total else 0
-        if first is None:
-            first = total - held
-        if count is None:
-            count = total - first
-        fb = int(bnd.sph_record_frame_bytes(self.psdata_opencl))
-        buf = np.empty(count * fb, dtype=np.uint8)
-        if count and bnd.sph_record_read(self.psdata_opencl, buf.ctypes.data, int(first), int(count)) != 0:
-            raise bnd.SphError(bnd.last_error())
-        frames = buf.reshape(count, fb)
-        out, off = {}, 0
-        for name in self._rec:
-            view = self.get_fields(name)[0]
-            nb = view.nbytes
-            out[name] = frames[:, off:off + nb].copy().view(view.dtype).reshape((count,) + view.shape)
-            off += nb
-        return out
-
-    def _rec_frames(self):
-        return self._rec_frames_n
-
     def init(self, **kwargs):
         super(StrainSolid, self).init(**kwargs)
         if self.init_values is None:

@@ -115,11 +115,9 @@ _DRIVER = r'''
 #define PSO_PASS num_fields, names, names_offsets, dimensions, num_dimensions, dimensions_offsets, \
     entry_sizes, data, data_sizes, data_offsets
 
-/* Returns 0, or -1 for an unknown kernel, or -(100 + k) when field k of
- * the program is missing from the store (the reference's program build
- * fails in that case). */
-extern "C" int @NS@_call(const char *kernel_name, unsigned global_size, int nthreads, PSO_PARAMS,
-                         unsigned body, const @REAL@ *vec3arg) {
+/* Looks the program's fields up in the store: 0, or -(100 + k) when field
+ * k is missing (the reference's program build fails in that case). */
+static int @NS@_resolve(unsigned num_fields, char *names, unsigned *names_offsets) {
     using namespace @NS@;
     for (unsigned k = 0; k < sizeof(FIELDS) / sizeof(FIELDS[0]); ++k) {
         *FIDX[k] = -1;
@@ -127,6 +125,48 @@ extern "C" int @NS@_call(const char *kernel_name, unsigned global_size, int nthr
             if (strcmp(names + names_offsets[f], FIELDS[k]) == 0) { *FIDX[k] = (int)f; break; }
         if (*FIDX[k] < 0) return -(100 + (int)k);
     }
+    return 0;
+}
+
+/* populate_position_cuboid (common.cl:533-555) over its 3-D range, one
+ * work item at a time; returns 0 or the field lookup's error. */
+extern "C" int @NS@_populate_cuboid(PSO_PARAMS, const @REAL@ *c1, const @REAL@ *c2, const unsigned *size) {
+    using namespace @NS@;
+    int rc = @NS@_resolve(num_fields, names, names_offsets);
+    if (rc) return rc;
+    vec3<@REAL@> a = {c1[0], c1[1], c1[2]}, b = {c2[0], c2[1], c2[2]};
+    uint3 sz = {size[0], size[1], size[2]};
+    g_work_dim = 3;
+    for (unsigned k = 0; k < size[2]; ++k)
+        for (unsigned j = 0; j < size[1]; ++j)
+            for (unsigned i = 0; i < size[0]; ++i) {
+                g_global_id = i;
+                g_global_id_yz[0] = j;
+                g_global_id_yz[1] = k;
+                populate_position_cuboid(PSO_PASS, a, b, sz);
+            }
+    g_work_dim = 1;
+    return 0;
+}
+
+/* rotate_particles (common.cl:556-604) over `global_size` work items. */
+extern "C" int @NS@_rotate(PSO_PARAMS, unsigned global_size, @REAL@ ax, @REAL@ ay, @REAL@ az) {
+    using namespace @NS@;
+    int rc = @NS@_resolve(num_fields, names, names_offsets);
+    if (rc) return rc;
+    for (unsigned i = 0; i < global_size; ++i) {
+        g_global_id = i;
+        rotate_particles(PSO_PASS, ax, ay, az);
+    }
+    return 0;
+}
+
+/* Returns 0, or -1 for an unknown kernel, or the field lookup's error. */
+extern "C" int @NS@_call(const char *kernel_name, unsigned global_size, int nthreads, PSO_PARAMS,
+                         unsigned body, const @REAL@ *vec3arg) {
+    using namespace @NS@;
+    int rc = @NS@_resolve(num_fields, names, names_offsets);
+    if (rc) return rc;
     if (nthreads < 1) nthreads = 1;
     auto run_all = [&](kfn fn, unsigned count) {
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)

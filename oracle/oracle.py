@@ -186,6 +186,19 @@ class OracleScene(object):
         ptr = v.ctypes.data_as(POINTER(c_float if self.prec == "f32" else c_double))
         getattr(lib(), "oracle_set_body_rotation" + self._sfx)(ctypes.byref(self.state), body, ptr)
 
+    def populate_position_cuboid(self, corner1, corner2, size):
+        """populate_position_cuboid (common.cl:533-555): a lattice spanning
+        corner1..corner2 with size[a] points per axis, at most pnum of them."""
+        T = c_float if self.prec == "f32" else c_double
+        getattr(lib(), "oracle_populate_position_cuboid" + self._sfx)(
+            ctypes.byref(self.state), c_uint(self.pnum), (T * 3)(*corner1), (T * 3)(*corner2),
+            (c_uint * 3)(*[int(x) for x in size]))
+
+    def rotate_particles(self, ax, ay, az):
+        """rotate_particles (common.cl:556-604)."""
+        T = c_float if self.prec == "f32" else c_double
+        getattr(lib(), "oracle_rotate_particles" + self._sfx)(ctypes.byref(self.state), T(ax), T(ay), T(az))
+
     def reset_rigid(self):
         """Rigid bodies are set up again from the particles on their next
         substep (what a host upload of positions does on the device)."""

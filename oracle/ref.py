@@ -136,6 +136,29 @@ class RefStore(object):
         if rc != 0:
             raise RuntimeError("reference kernel %s/%s returned %d" % (program, kernel, rc))
 
+    def _pso(self):
+        ps = self.ps
+        return (ps.num_fields, ps.names, ps.names_offsets, ps.dimensions, ps.num_dimensions, ps.dimensions_offsets,
+                ps.entry_sizes, c_void_p(ps.data), ps.data_sizes, ps.data_offsets)
+
+    def populate_cuboid(self, program, prec, corner1, corner2, size):
+        """populate_position_cuboid (common.cl:533-555) over its 3-D range."""
+        fn = getattr(kernels_lib(), "ref_%s_%s_populate_cuboid" % (program, prec))
+        real = c_float if prec == "f32" else c_double
+        fn.restype = c_int
+        rc = fn(*self._pso(), (real * 3)(*corner1), (real * 3)(*corner2), (c_uint * 3)(*size))
+        if rc != 0:
+            raise RuntimeError("reference populate_position_cuboid returned %d" % rc)
+
+    def rotate(self, program, prec, angles, global_size):
+        """rotate_particles (common.cl:556-604) over `global_size` items."""
+        fn = getattr(kernels_lib(), "ref_%s_%s_rotate" % (program, prec))
+        real = c_float if prec == "f32" else c_double
+        fn.restype = c_int
+        rc = fn(*self._pso(), c_uint(global_size), real(angles[0]), real(angles[1]), real(angles[2]))
+        if rc != 0:
+            raise RuntimeError("reference rotate_particles returned %d" % rc)
+
     def free(self):
         if self.ps.num_fields:
             if self._own:

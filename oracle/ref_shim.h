@@ -91,13 +91,17 @@ inline double cos(double a) { return ::cos(a); }
 inline float sin(float a) { return sinf(a); }
 inline double sin(double a) { return ::sin(a); }
 
-/* work-item functions: the host loop sets the global id before each call */
+/* work-item functions: the host loop sets the global id before each call
+ * (a 3-D launch, as populate_position_cuboid needs, also sets the y and z
+ * ids and the work dimension) */
 static thread_local size_t g_global_id;
-inline size_t get_global_id(uint) { return g_global_id; }
+static thread_local size_t g_global_id_yz[2];
+static thread_local uint g_work_dim = 1;
+inline size_t get_global_id(uint d) { return d == 0 ? g_global_id : (d < 3 ? g_global_id_yz[d - 1] : 0); }
 inline size_t get_local_id(uint) { return 0; }
 inline size_t get_local_size(uint) { return 1; }
 inline size_t get_group_id(uint) { return 0; }
-inline uint get_work_dim() { return 1; }
+inline uint get_work_dim() { return g_work_dim; }
 enum { CLK_LOCAL_MEM_FENCE = 1, CLK_GLOBAL_MEM_FENCE = 2 };
 inline void barrier(int) {}
 inline uint atomic_inc(uint *p) { return (*p)++; }

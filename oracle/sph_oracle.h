@@ -118,6 +118,11 @@ typedef struct { SPH_ORACLE_STATE_FIELDS(double) } sph_oracle_state_f64;
                                        unsigned int body, const REAL *pos);   \
     void oracle_set_body_rotation##SFX(sph_oracle_state##SFX *s,               \
                                        unsigned int body, const REAL *euler); \
+    void oracle_populate_position_cuboid##SFX(sph_oracle_state##SFX *s,        \
+                                              unsigned int pnum, const REAL *c1, \
+                                              const REAL *c2, const unsigned int *size); \
+    void oracle_rotate_particles##SFX(sph_oracle_state##SFX *s, REAL ax,       \
+                                      REAL ay, REAL az);                       \
     void oracle_get_r##SFX(const REAL *apq, REAL *r, int guard);             \
     void oracle_jacobi_invert##SFX(const REAL *m6, REAL *out6, int guard);
 

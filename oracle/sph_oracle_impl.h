@@ -929,6 +929,42 @@ void OF(oracle_set_body_rotation)(OST *s, unsigned body, const REAL *euler) {
     s->body_euler_rotation[3 * body + 2] = euler[2];
 }
 
+/* populate_position_cuboid, common.cl:533-555: work item (i, j, k) of a
+ * size[0] x size[1] x size[2] range writes particle p = i + size[0] j +
+ * size[0] size[1] k at (i / (size[0] - 1)) (c2 - c1) + c1 per axis, unless
+ * p >= pnum; the item p = pnum - 1 sets n = pnum, else the last item of the
+ * range sets n = its size.  Items run in order; no two write one particle. */
+void OF(oracle_populate_position_cuboid)(OST *s, unsigned pnum, const REAL *c1, const REAL *c2,
+                                         const unsigned *size) {
+    for (unsigned k = 0; k < size[2]; ++k)
+        for (unsigned j = 0; j < size[1]; ++j)
+            for (unsigned i = 0; i < size[0]; ++i) {
+                unsigned p = i + size[0] * j + size[0] * size[1] * k;
+                if (p >= pnum) continue;
+                if (p == pnum - 1) s->n = pnum;
+                else if (i == size[0] - 1 && j == size[1] - 1 && k == size[2] - 1) s->n = size[0] * size[1] * size[2];
+                REAL q[3];
+                const unsigned idx[3] = {i, j, k};
+                for (int a = 0; a < 3; ++a)
+                    q[a] = ((REAL)idx[a] / (REAL)(size[a] - 1)) * (c2[a] - c1[a]) + c1[a];
+                OF(v3_store)(OF(v3)(q[0], q[1], q[2]), s->position, p);
+            }
+}
+
+/* rotate_particles, common.cl:556-604: x <- Rx(ax) (Ry(ay) Rz(az)) x for
+ * the first n particles, with the source's sign conventions (Ry has -sin
+ * above the diagonal). */
+void OF(oracle_rotate_particles)(OST *s, REAL ax, REAL ay, REAL az) {
+    REAL cx = R_COS(ax), sx = R_SIN(ax), cy = R_COS(ay), sy = R_SIN(ay), cz = R_COS(az), sz = R_SIN(az);
+    REAL rx[9] = {1, 0, 0, 0, cx, -sx, 0, sx, cx};
+    REAL ry[9] = {cy, 0, -sy, 0, 1, 0, sy, 0, cy};
+    REAL rz[9] = {cz, -sz, 0, sz, cz, 0, 0, 0, 1};
+    REAL ryz[9], r[9];
+    OF(mul_mm)(ry, rz, ryz);
+    OF(mul_mm)(rx, ryz, r);
+    for (size_t i = 0; i < s->n; ++i) OF(v3_store)(OF(mul_mv)(r, OF(v3_load)(s->position, i)), s->position, i);
+}
+
 #undef O_FOR_NEIGHBOURS
 #undef O_PLANE_POINT
 #undef O_PLANE_NORMAL

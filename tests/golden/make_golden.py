@@ -13,6 +13,11 @@ Writes:
   kernels_*.npz     small seeded scenes run through the reference's own
                     kernels (kernels/*.cl compiled as C++ into oracle/_ref)
                     in FP32 and FP64: each kernel's inputs and outputs.
+  kernels_scene_builders.npz
+                    populate_position_cuboid and rotate_particles
+                    (common.cl:533-604) on a few ranges and angle sets.
+
+    python tests/golden/make_golden.py scene_builders   # only that file
 
 The tests compare the product's builder, the C oracle and the GPU path
 against these files; nothing at test time reads the reference checkout.
@@ -178,9 +183,46 @@ def bodies_and_constraints(rs, program, prec, n, rec):
         _snapshot(rs, prec + "/apply_plane_constraints/", rec, OUTPUTS["apply_plane_constraints"])
 
 
+# (corner1, corner2, size) ranges of populate_position_cuboid: one that
+# fills pnum exactly, one larger than pnum (n = pnum), one smaller (n = its
+# size), and a flat one with negative extents
+CUBOIDS = [((0.0, 0.0, 0.0), (0.1, 0.05, 0.07), (5, 4, 6)),
+           ((-0.2, 0.1, 0.3), (0.4, 0.35, 0.9), (7, 5, 6)),
+           ((0.01, 0.02, 0.03), (0.3, 0.2, 0.1), (3, 4, 5)),
+           ((0.5, -0.5, 0.25), (-0.5, 0.5, 0.25), (11, 9, 2))]
+ANGLES = [(0.3, -0.2, 0.1), (1.2, 0.7, -2.5), (0.0, 0.0, 3.14159265)]
+
+
+def scene_builders():
+    """populate_position_cuboid over CUBOIDS, then rotate_particles by each
+    of ANGLES in turn, on a 120-particle store; FP32 and FP64."""
+    sc = scenes.wcsph_block(6, 5, 4, jitter=0.0, seed=0, walls=False)
+    rec = {"spec": np.array(sc.spec)}
+    for prec in ("f32", "f64"):
+        spec = sc.spec if prec == "f32" else sc.spec.replace("| float", "| double")
+        for c, (c1, c2, size) in enumerate(CUBOIDS):
+            rs = ref.RefStore(spec)
+            rs.view("n")[...] = 0
+            rs.populate_cuboid("fluid", prec, c1, c2, size)
+            rec["%s/cuboid%d/position" % (prec, c)] = np.array(rs.view("position"))
+            rec["%s/cuboid%d/n" % (prec, c)] = np.array(rs.view("n"))
+            for a, ang in enumerate(ANGLES):
+                rs.rotate("fluid", prec, ang, int(rs.view("n")[0]))
+                rec["%s/cuboid%d/rotate%d/position" % (prec, c, a)] = np.array(rs.view("position"))
+            rs.free()
+    rec["cuboids"] = np.array([list(c1) + list(c2) + list(sz) for c1, c2, sz in CUBOIDS], dtype=np.float64)
+    rec["angles"] = np.array(ANGLES, dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "kernels_scene_builders.npz"), **rec)
+    print("kernels_scene_builders.npz")
+
+
 def main():
     if not (ref.available("kernels") and ref.available("psdata")):
         raise SystemExit("oracle/_ref is not built: run python oracle/make_ref.py first")
+    if sys.argv[1:] == ["scene_builders"]:
+        scene_builders()
+        return
+    scene_builders()
     layouts()
     fl = scenes.wcsph_block(7, 6, 5, jitter=2e-3, seed=1, walls=False)
     rng = np.random.default_rng(2)

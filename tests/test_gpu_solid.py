@@ -5,8 +5,10 @@ Kernels are compared one at a time on identical inputs (the oracle's
 fields are uploaded first), then whole trajectories.  Tolerances, relative
 to the largest magnitude of the compared field (measured errors on a
 GB300 are 2-5x below them):
-  - rotation R (GPU polar decomposition in FP64, oracle in FP32),
-    deformation, stress, forces: 2e-5;
+  - rotation R (GPU: Newton's polar iteration in FP32 finished by one
+    FP64 step; oracle: the reference's FP32 Jacobi getR), deformation,
+    stress, forces: 2e-5 (R against an exact FP64 polar factor is pinned
+    separately, at 2e-7);
   - strain (a small difference of nearly equal neighbour sums): 5e-5;
   - positions after N substeps: relative L2 error 1e-5.
 Neighbour counts stay bit-exact.

@@ -194,3 +194,26 @@ def test_zero_distance_guard():
         orc.call("compute_forces_fluids")
         assert np.isfinite(orc.a["force"][: sc.n]).all() == finite
     free_data_cpu(ps)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_oracle_reproduces_reference_scene_builders(prec):
+    """populate_position_cuboid and rotate_particles (common.cl:533-604)
+    against the reference's own kernels: positions and n bit for bit."""
+    g = dict(np.load(os.path.join(GOLD, "kernels_scene_builders.npz")))
+    spec = str(g["spec"])
+    if prec == "f64":
+        spec = spec.replace("| float", "| double")
+    for c, row in enumerate(g["cuboids"]):
+        ps = init_data_cpu(spec)
+        v = bnd.store_views(ps)
+        orc = OracleScene({k: np.array(a) for k, a in v.items()}, prec)
+        free_data_cpu(ps)
+        orc.state.n = 0
+        orc.populate_position_cuboid(row[0:3], row[3:6], row[6:9].astype(int))
+        pre = "%s/cuboid%d/" % (prec, c)
+        assert orc.n == int(g[pre + "n"][0])
+        assert np.array_equal(orc.a["position"], g[pre + "position"])
+        for a, ang in enumerate(g["angles"]):
+            orc.rotate_particles(*ang)
+            assert np.array_equal(orc.a["position"], g[pre + "rotate%d/position" % a]), (c, a)

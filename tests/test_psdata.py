@@ -85,19 +85,16 @@ def test_config_sections_and_missing_file():
     assert bnd.load_config("/nonexistent/file.conf") == 1
 
 
-def test_build_psdata_from_file():
+def test_build_psdata_from_file(tmp_path):
     ps = bnd.psdata()
     # a spec file whose last byte is overwritten by the terminator, as the
     # reference's build_psdata does
-    path = os.path.join(os.path.dirname(GOLDEN), "..", "..", "_work_spec_tmp.txt")
+    path = str(tmp_path / "spec.txt")
     with open(path, "w") as f:
         f.write(LAYOUTS["fp32-grid-truncation"]["spec"] + "\n")
-    try:
-        bnd.build_psdata(ctypes.byref(ps), path)
-        assert list(bnd.store_views(ps)["gridres"]) == [39, 39, 39]  # 4 / (double)0.1f truncates to 39
-        bnd.free_psdata(ctypes.byref(ps))
-    finally:
-        os.remove(path)
+    bnd.build_psdata(ctypes.byref(ps), path)
+    assert list(bnd.store_views(ps)["gridres"]) == [39, 39, 39]  # 4 / (double)0.1f truncates to 39
+    bnd.free_psdata(ctypes.byref(ps))
 
 
 def test_missing_grid_fields_is_an_error():
