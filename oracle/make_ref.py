@@ -24,12 +24,15 @@ Recipe, run in the container that holds the reference checkout
    run serially with particle 0 last so every particle reads the old pose.
 2. Host store.  src/build_psdata.c, particle_system.c, config.c, note.c and
    stringly.c are compiled against a one-line stub ``CL/opencl.h`` into
-   libref_psdata.so, giving the reference's own psdata layouts.
+   libref_psdata.so, giving the reference's own psdata layouts.  The
+   sources (and the headers they include) are copied, unedited, into
+   oracle/_ref/host/src/ first, so that a machine that receives oracle/_ref/
+   without the reference checkout builds the same library.
 
 Outputs go to oracle/_ref/ only (git-ignored).  When the reference checkout
-is absent (a machine that only received this repository), the generated
-kernel sources already in oracle/_ref/ are compiled and the host store is
-skipped.  Nothing in the product imports this module.
+is absent (a machine that only received this repository and oracle/_ref/),
+the generated kernel sources and the copied host sources already in
+oracle/_ref/ are compiled.  Nothing in the product imports this module.
 """
 import os
 import re
@@ -235,6 +238,12 @@ def generate():
     os.makedirs(os.path.join(host, "CL"), exist_ok=True)
     with open(os.path.join(host, "CL", "opencl.h"), "w") as fh:
         fh.write("typedef void *cl_mem; typedef void *cl_kernel; typedef void *cl_program;\n")
+    # the host builder's sources and headers, as they are
+    src_copy = os.path.join(host, "src")
+    if os.path.isdir(src_copy):
+        shutil.rmtree(src_copy)
+    shutil.copytree(os.path.join(REF, "src"), src_copy,
+                    ignore=shutil.ignore_patterns("mex", "*.o", "*.so"))
     return paths
 
 
@@ -250,7 +259,9 @@ def compile_all(jobs=8):
     _run(["g++", "-shared", "-fopenmp", "-o", lib] + objs + ["-lm"])
     built = [lib]
     src_dir = os.path.join(REF, "src")
-    if os.path.isdir(src_dir):
+    if not os.path.isdir(src_dir):
+        src_dir = os.path.join(OUT, "host", "src")
+    if all(os.path.exists(os.path.join(src_dir, f)) for f in HOST_SOURCES):
         inc = os.path.join(OUT, "host")
         srcs = [os.path.join(src_dir, s) for s in HOST_SOURCES]
         plib = os.path.join(OUT, "libref_psdata.so")
