@@ -343,6 +343,18 @@ int sph_batch_read_field_many(sph_batch *batch, const int *ids, unsigned int cou
 long long sph_batch_read_field_many_async(sph_batch *batch, const int *ids, unsigned int count, const char *field,
                                           psdata *const *outs);
 int sph_batch_wait_read(sph_batch *batch, long long ticket);
+/* The write direction (the per-substep inputs a host controller sets, such
+ * as each scene's time step or gravity): the named field of each host
+ * store ins[k] is copied into scene ids[k], in stream order before the
+ * substeps enqueued after this call.  The bytes are taken from the stores
+ * during the call (into a page-locked staging buffer), so the stores may
+ * change as soon as it returns; one host-to-device copy and one scatter
+ * kernel carry every scene's bytes.  gridres and pnum cannot be written
+ * (they size the scene's tables), nor, in a scene with rigid bodies, the
+ * fields the bodies are set up from (position, velocity, n, body tables).
+ * Returns a non-negative count of writes so far, or -1. */
+int sph_batch_write_field_many_async(sph_batch *batch, const int *ids, unsigned int count, const char *field,
+                                     psdata *const *ins);
 /* Waits for every read enqueued so far. */
 int sph_batch_wait_reads(sph_batch *batch);
 /* Runs `reps` substeps of the batch as individual launches with CUDA events

@@ -82,6 +82,16 @@ struct sph_batch {
     size_t seg_host_cap[2] = {0, 0};
     unsigned seg_count[2] = {0, 0};             // segments in turn t's device table (0: none)
     long long tickets = 0;  // reads enqueued so far
+    // sph_batch_write_field_many_async: writes take turns over two pinned
+    // staging buffers (segment table, then the fields' bytes), each copied
+    // to a device buffer of its turn and scattered into the scenes by one
+    // copy kernel; write_done[t] marks the staging buffer's copy finished
+    char *wstage_host[2] = {nullptr, nullptr};
+    size_t wstage_host_cap[2] = {0, 0};
+    char *wstage_dev[2] = {nullptr, nullptr};
+    size_t wstage_dev_cap[2] = {0, 0};
+    cudaEvent_t write_done[2] = {nullptr, nullptr};
+    long long wtickets = 0;  // writes enqueued so far
 };
 
 // A stream-ordered allocation from the batch's pool.
@@ -345,11 +355,15 @@ extern "C" void sph_batch_free(sph_batch *b) {
         if (b->snap[t]) cudaFreeAsync(b->snap[t], b->stream);
         if (b->snap_segs[t]) cudaFreeAsync(b->snap_segs[t], b->stream);
     }
-    if (b->stream) cudaStreamSynchronize(b->stream);
     for (int t = 0; t < 2; ++t)
+        if (b->wstage_dev[t]) cudaFreeAsync(b->wstage_dev[t], b->stream);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (int t = 0; t < 2; ++t) {
         if (b->seg_host[t]) cudaFreeHost(b->seg_host[t]);
+        if (b->wstage_host[t]) cudaFreeHost(b->wstage_host[t]);
+    }
     for (cudaEvent_t e : {b->fork, b->join[0], b->join[1], b->snap_done[0], b->snap_done[1], b->read_done[0],
-                          b->read_done[1]})
+                          b->read_done[1], b->write_done[0], b->write_done[1]})
         if (e) cudaEventDestroy(e);
     for (cudaStream_t s : {b->stream, b->side[0], b->side[1], b->reads})
         if (s) cudaStreamDestroy(s);
@@ -733,6 +747,90 @@ extern "C" long long sph_batch_read_field_many_async(sph_batch *b, const int *id
             return -1;
     if (!ok(cudaEventRecord(b->read_done[t], b->reads), what) || sph_check_launch(what) != cudaSuccess) return -1;
     return b->tickets++;
+}
+
+// Fields a write may not touch: the shape the scene's tables were sized
+// for, and (in a scene with rigid bodies) what the bodies are set up from.
+static bool write_allowed(const BatchScene *sc, const char *field, const char *what, int id) {
+    static const char *kShape[] = {"pnum", "gridres"};
+    static const char *kRigid[] = {"position", "velocity", "body_number", "body_dynamic", "body_count", "n"};
+    for (const char *k : kShape)
+        if (!strcmp(field, k)) {
+            sph_set_error("%s: '%s' sizes scene %d's device tables and cannot be written", what, field, id);
+            return false;
+        }
+    if (!sc->rigid.empty())
+        for (const char *k : kRigid)
+            if (!strcmp(field, k)) {
+                sph_set_error("%s: scene %d has rigid bodies, which are set up from '%s'; add it anew instead",
+                              what, id, field);
+                return false;
+            }
+    return true;
+}
+
+extern "C" int sph_batch_write_field_many_async(sph_batch *b, const int *ids, unsigned int count, const char *field,
+                                                psdata *const *ins) {
+    const char *what = "sph_batch_write_field_many_async";
+    if (!b || !count || !ids || !ins || !field) {
+        sph_set_error("%s: no batch, ids, stores or field", what);
+        return -1;
+    }
+    if (!b->write_done[0]) {
+        for (int t = 0; t < 2; ++t)
+            if (!ok(cudaEventCreateWithFlags(&b->write_done[t], cudaEventDisableTiming), what)) return -1;
+    }
+    // layout of a turn's staging buffer: the segment table, then each
+    // scene's bytes at a 16-byte aligned offset
+    std::vector<CopySeg> segs(count);
+    std::vector<const char *> src(count);
+    std::vector<size_t> at(count);
+    const size_t table = (count * sizeof(CopySeg) + 255) / 256 * 256;
+    size_t total = table;
+    unsigned long long max_bytes = 0;
+    for (unsigned k = 0; k < count; ++k) {
+        BatchScene *sc = scene_of(b, ids[k], what);
+        if (!sc) return -1;
+        const psdata *in = ins[k];
+        const int f = in ? get_field_psdata(*in, field) : -1;
+        if (f < 0 || psdata_data_size(*in) != sc->blob_size) {
+            sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field);
+            return -1;
+        }
+        if (!write_allowed(sc, field, what, ids[k])) return -1;
+        const size_t off = in->data_offsets[f], sz = in->data_sizes[f];
+        segs[k] = CopySeg{nullptr, sc->mem + off, (unsigned long long)sz};
+        src[k] = static_cast<const char *>(in->data) + off;
+        at[k] = total;
+        total += (sz + 15) / 16 * 16;
+        if (sz > max_bytes) max_bytes = sz;
+    }
+    const int t = (int)(b->wtickets & 1);
+    // turn t's staging buffer is free once its copy two writes back is done
+    if (!ok(cudaEventSynchronize(b->write_done[t]), what)) return -1;
+    if (total > b->wstage_host_cap[t]) {
+        if (b->wstage_host[t]) cudaFreeHost(b->wstage_host[t]);
+        b->wstage_host[t] = nullptr;
+        b->wstage_host_cap[t] = 0;
+        const size_t c = total + total / 2;
+        if (!ok(cudaMallocHost((void **)&b->wstage_host[t], c), what)) return -1;
+        b->wstage_host_cap[t] = c;
+    }
+    if (!grow(b, &b->wstage_dev[t], &b->wstage_dev_cap[t], total, b->stream, what)) return -1;
+    char *dev = b->wstage_dev[t];
+    for (unsigned k = 0; k < count; ++k) {
+        segs[k].src = dev + at[k];
+        memcpy(b->wstage_host[t] + at[k], src[k], (size_t)segs[k].bytes);
+    }
+    memcpy(b->wstage_host[t], segs.data(), count * sizeof(CopySeg));
+    // one host-to-device copy of the table and the bytes, in stream order
+    // before the substeps enqueued after this call, then the scatter
+    if (!ok(cudaMemcpyAsync(dev, b->wstage_host[t], total, cudaMemcpyHostToDevice, b->stream), what) ||
+        !ok(cudaEventRecord(b->write_done[t], b->stream), what))
+        return -1;
+    sph_launch_copy_segments(reinterpret_cast<const CopySeg *>(dev), count, max_bytes, b->stream);
+    if (sph_check_launch(what) != cudaSuccess) return -1;
+    return (int)(b->wtickets++ & 0x7fffffff);
 }
 
 extern "C" int sph_batch_wait_read(sph_batch *b, long long ticket) {

@@ -164,6 +164,15 @@ class Batch(object):
             raise bnd.SphError(bnd.last_error())
         return t
 
+    def write_fields_async(self, sids, name):
+        """Enqueues a write of one field of several scenes from their host
+        stores (one host-to-device copy and one scatter kernel), in stream
+        order before the substeps enqueued next; the host stores may change
+        as soon as this returns."""
+        key, ids, outs = self._read_args(sids)
+        if bnd.sph_batch_write_field_many_async(self.handle, ids, len(key), name, outs) < 0:
+            raise bnd.SphError(bnd.last_error())
+
     def wait_read(self, ticket):
         if bnd.sph_batch_wait_read(self.handle, ticket) != 0:
             raise bnd.SphError(bnd.last_error())

@@ -333,3 +333,43 @@ def test_empty_store_fused_substeps():
     assert np.array_equal(ps.get_fields("position")[0][: sc.n],
                           np.asarray(sc.init["position"], np.float32).reshape(-1, 3))
     ps.close()
+
+
+def test_batched_writes_equal_host_uploads():
+    """sph_batch_write_field_many_async: per-substep inputs (each scene's
+    time step and gravity changed before every substep) give the results of
+    the same scenes run alone with the same values uploaded through the
+    drop-in's blocking sync; bad writes are refused."""
+    scs = mix(seed=10)
+    steps = 6
+    dts = {s.name: [float(s.param("timestep")) * (1.0 + 0.05 * k) for k in range(steps)] for s in scs}
+    gs = {s.name: [np.array([0.3 * k, -9.8, 0.1 * k], np.float32) for k in range(steps)] for s in scs}
+    b = Batch()
+    ids = [b.add(s) for s in scs]
+    for k in range(steps):
+        for s, sid in zip(scs, ids):
+            v = b.scenes[sid].views
+            v["timestep"][...] = dts[s.name][k]
+            v["gravity"][...] = gs[s.name][k]
+        b.write_fields_async(ids, "timestep")
+        b.write_fields_async(ids, "gravity")
+        # the stores may change at once: the next write overwrites them
+        for sid in ids:
+            b.scenes[sid].views["timestep"][...] = -1.0
+        b.step(1)
+    got = {s.name: np.array(b.read(sid)["position"][: s.n]) for s, sid in zip(scs, ids)}
+    with pytest.raises(Exception, match="gridres"):
+        b.write_fields_async(ids[:1], "gridres")
+    b.close()
+    for s in scs:
+        ps = s.system()
+        if s.material != "fluid":
+            ps.call_for_all_particles("init_original_position")
+            ps.compute_particle_bins()
+            ps.call_for_all_particles("compute_original_density")
+        for k in range(steps):
+            ps.set_fields(timestep=dts[s.name][k], gravity=gs[s.name][k])
+            ps.update_fused(1)
+        ps.sync_device_to_host()
+        assert np.array_equal(ps.get_fields("position")[0][: s.n], got[s.name]), s.name
+        ps.close()
