@@ -401,6 +401,10 @@ static int add_scene(sph_batch *b, psdata *scene, const char *file_list, const s
         sph_set_error("sph_batch_add: the program has no substep recipe (needs fluids, solid_corotation or solid_svk)");
         return -1;
     }
+    if (material == MAT_MIXED) {
+        sph_set_error("sph_batch_add: a mixed fluid-solid scene runs as a store of its own (create_psdata_cuda)");
+        return -1;
+    }
     BatchScene *sc = new BatchScene();
     sc->programs = programs;
     sc->material = material;

@@ -278,6 +278,7 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     L.grid_cap = 1u << 30;
     L.stream = s->stream;
     L.no_symmetry_planes = s->desc.num_symmetry_planes == 0;
+    L.has_mixed = s->desc.phase != nullptr;
     L.rigid = s->d_rigid;
     L.num_rigid = 0;
     if (!refresh_rigid(s, *data)) {
@@ -344,10 +345,26 @@ bool dispatch(Store *s, const char *name) {
         sph_launch_init_original_position(L);
         return true;
     }
+    // a mixed fluid-solid store (extension): the solid kernels cover the
+    // solid particles over their solid neighbours, and the fluid force pass
+    // adds the fluid pair terms to the elastic forces (call it after
+    // compute_forces_solids, as sph_update does)
+    const bool mixed = s->desc.phase != nullptr;
     if (k == "compute_original_density") {
         if (!need(PROG_SOLIDS, "solids")) return false;
         sph_launch_gather(L, false, false);
-        sph_launch_density(L, true);
+        if (mixed) sph_launch_original_density_mixed(L);
+        else sph_launch_density(L, true);
+        return true;
+    }
+    if (mixed && k == "compute_deformations") {
+        sph_launch_gather(L, false, false);
+        sph_launch_deformations_mixed(L);
+        return true;
+    }
+    if (mixed && k == "compute_forces_solids") {
+        sph_launch_gather(L, false, false);
+        sph_launch_forces_solids_mixed(L);
         return true;
     }
     if (k == "compute_rotations_and_strains") {
@@ -549,6 +566,11 @@ extern "C" void compute_density_device_cuda(psdata_cuda pso) {
 extern "C" void compute_forces_device_cuda(psdata_cuda pso) {
     Store *s = store_of(pso, "compute_forces");
     if (!s) { sph_fail(); return; }
+    if (s->desc.phase) {  // a mixed store: the elastic forces, then the fluid pair terms
+        call_for_all_particles_device_cuda(pso, "compute_forces_solids");
+        call_for_all_particles_device_cuda(pso, "compute_forces_fluids");
+        return;
+    }
     call_for_all_particles_device_cuda(pso, (s->programs & (PROG_COROT | PROG_SVK)) ? "compute_forces_solids"
                                                                                      : "compute_forces_fluids");
 }

@@ -4,6 +4,7 @@
 
 #include "kernels_fluid.cuh"
 #include "kernels_grid.cuh"
+#include "kernels_mixed.cuh"
 #include "kernels_rigid.cuh"
 #include "kernels_solid.cuh"
 #include "launch.h"
@@ -100,12 +101,31 @@ void sph_launch_density_fused(const Launch &L, const Launch *fluids) {
 }
 
 void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
-    if (masked)
-        k_forces_fluids_masked<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-            L.scenes, L.pair_particles, fuse_step ? 1 : 0);
-    else
-        k_forces_fluids<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-            L.scenes, L.pair_particles, fuse_step ? 1 : 0);
+    const unsigned g = grid_for(L.pair_particles, L.grid_cap);
+    const int step = fuse_step ? 1 : 0;
+    if (masked) {
+        k_forces_fluids_masked<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        if (L.has_mixed)
+            k_forces_fluids_masked<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+    } else {
+        k_forces_fluids<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        if (L.has_mixed) k_forces_fluids<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+    }
+}
+
+void sph_launch_original_density_mixed(const Launch &L) {
+    k_original_density_mixed<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+        L.scenes, L.pair_particles);
+}
+
+void sph_launch_deformations_mixed(const Launch &L) {
+    k_deformations_mixed<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+        L.scenes, L.pair_particles);
+}
+
+void sph_launch_forces_solids_mixed(const Launch &L) {
+    k_forces_solids_mixed<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
+        L.scenes, L.pair_particles);
 }
 
 void sph_launch_step_forward(const Launch &L, bool planes_only) {
@@ -227,6 +247,29 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
     sph_launch_scan(L, true);
     phase("insert");
     sph_launch_insert(L);
+    if (mat == MAT_MIXED) {
+        // fluid and solid particles in one scene (extension): the fluid
+        // recipe, with the solids' elastic passes before the force pass,
+        // which adds the fluid-solid pair terms and steps every particle
+        phase("gather");
+        sph_launch_gather(L, true, false);
+        phase("density");
+        sph_launch_density(L, false, true, false);
+        phase("deformations (solid phase)");
+        sph_launch_deformations_mixed(L);
+        phase("stresses (solid phase)");
+        sph_launch_stresses(L, false);
+        phase("forces_solids (solid phase)");
+        sph_launch_forces_solids_mixed(L);
+        phase("forces_fluids+step");
+        sph_launch_forces_fluids(L, true, true);
+        if (L.num_rigid) {
+            phase("rigid_bodies");
+            sph_launch_rigid(L);
+        }
+        phase(nullptr);
+        return;
+    }
     phase("gather");
     sph_launch_gather(L, mat == MAT_FLUID, false, mat != MAT_FLUID);
     if (mat == MAT_FLUID || !L.no_symmetry_planes) {

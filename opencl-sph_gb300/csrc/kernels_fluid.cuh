@@ -142,9 +142,17 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         if (MASK) {
             S.ncand[k] = overflow ? SPH_NCAND_SCAN : total;
             // the force pass reads a neighbour's pressure with its position
-            // and its reciprocal density with its velocity (spare w lanes)
-            S.spos[k].w = fluid_pressure(value, *S.restdens, *S.stiffness);
-            S.svel[k].w = rcp_approx(value);
+            // and its reciprocal density with its velocity (spare w lanes);
+            // a mixed scene's solid particle stores its pressure clamped at
+            // 0 and its reciprocal density negated, which marks it solid
+            float pv = fluid_pressure(value, *S.restdens, *S.stiffness);
+            float rv = rcp_approx(value);
+            if (S.phase && S.phase[i]) {
+                pv = fmaxf(pv, 0.f);
+                rv = -rv;
+            }
+            S.spos[k].w = pv;
+            S.svel[k].w = rv;
         }
     }
 }
@@ -223,8 +231,8 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
 // walks the density pass's masks, whose candidates passed r^2 <= le with
 // the same positions and arithmetic, so that test is not repeated.
 template <bool IN_RANGE = false>
-__device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3 jvel, float pj, float inv_rhoj,
-                                            Kahan3 &f) {
+__device__ __forceinline__ float fluid_pair_p(const FluidI &I, float pi, float3 jpos, float3 jvel, float pj,
+                                              float inv_rhoj, Kahan3 &f) {
     const float3 d = sub3(jpos, I.ipos);
     const float r2 = norm2(d);
     if ((!IN_RANGE && !(r2 <= I.B.le)) || r2 == 0.f) return r2;
@@ -233,7 +241,7 @@ __device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3
     const float din = __fsub_rn(I.h, dist);
     const float inv_didj = __fmul_rn(I.inv_rhoi, inv_rhoj);
     const float vterm = __fmul_rn(din, I.vk);
-    const float pterm = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fadd_rn(I.pi, pj), I.pk), rinv), din), din);
+    const float pterm = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fadd_rn(pi, pj), I.pk), rinv), din), din);
     const float3 rv = sub3(jvel, I.ivel);
     f.add(make_float3(__fmul_rn(__fmaf_rn(d.x, pterm, __fmul_rn(rv.x, vterm)), inv_didj),
                       __fmul_rn(__fmaf_rn(d.y, pterm, __fmul_rn(rv.y, vterm)), inv_didj),
@@ -241,11 +249,20 @@ __device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3
     return r2;
 }
 
+template <bool IN_RANGE = false>
+__device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3 jvel, float pj, float inv_rhoj,
+                                            Kahan3 &f) {
+    return fluid_pair_p<IN_RANGE>(I, I.pi, jpos, jvel, pj, inv_rhoj, f);
+}
+
 // The end of a fluid particle's force pass: mass, cube band, store, step.
+// `extra`: force already on the particle (a mixed scene's solid particle
+// carries its elastic force, which the fluid pair terms add to).
 __device__ __forceinline__ void fluid_finish(const SceneDesc &S, unsigned i, const FluidI &I, const Kahan3 &f,
-                                             int fuse_step) {
+                                             int fuse_step, float3 extra = make_float3(0.f, 0.f, 0.f)) {
     const float m = *S.mass;
     float3 fi = f.get() * m;
+    fi = make_float3(fi.x + extra.x, fi.y + extra.y, fi.z + extra.z);
     fi.x = cube_bound(I.ipos.x, fi.x);
     fi.y = cube_bound(I.ipos.y, fi.y);
     fi.z = cube_bound(I.ipos.z, fi.z);
@@ -253,30 +270,79 @@ __device__ __forceinline__ void fluid_finish(const SceneDesc &S, unsigned i, con
     if (fuse_step) integrate(S, i, fi, I.ivel, I.ipos);
 }
 
+// Mixed fluid-solid scenes (extension; `phase` field): a solid particle's
+// fluid pair terms cover its fluid neighbours only (its solid neighbours
+// act through the elastic force), a fluid particle's cover every neighbour;
+// a pair with a solid particle takes both pressures clamped at 0 (it
+// pushes, never pulls).
+template <bool MIXED>
+__device__ __forceinline__ bool mixed_solid(const SceneDesc &S, unsigned i) {
+    return MIXED && S.phase && S.phase[i] != 0u;
+}
+template <bool MIXED>
+__device__ __forceinline__ float3 mixed_extra(const SceneDesc &S, unsigned i, bool solid_i) {
+    return (MIXED && solid_i) ? ld3(S.force, i) : make_float3(0.f, 0.f, 0.f);
+}
+// One neighbour of the masked force walk, from its position (pressure in
+// w) and velocity (reciprocal density in w, negated for a mixed scene's
+// solid particle); adds to the neighbour count.
+template <bool MIXED>
+__device__ __forceinline__ void walk_pair(const FluidI &I, bool solid_i, float4 p, float4 v, Kahan3 &f,
+                                          unsigned &count) {
+    if (MIXED) {
+        const bool solid_j = v.w < 0.f;
+        if (solid_i && solid_j) {
+            count += norm2(sub3(xyz(p), I.ipos)) <= I.B.lt;
+            return;
+        }
+        if (solid_i || solid_j) {
+            count += fluid_pair_p<true>(I, fmaxf(I.pi, 0.f), xyz(p), xyz(v), fmaxf(p.w, 0.f), fabsf(v.w), f) <=
+                     I.B.lt;
+            return;
+        }
+    }
+    count += fluid_pair<true>(I, xyz(p), xyz(v), p.w, v.w, f) <= I.B.lt;
+}
+
 // The stencil scan: every candidate of the 27 cells, in the reference's
 // order; returns the count of candidates closer than h (j = i included).
-__device__ __forceinline__ unsigned fluid_scan(const SceneDesc &S, unsigned cell, const FluidI &I, Kahan3 &f) {
+template <bool MIXED>
+__device__ __forceinline__ unsigned fluid_scan(const SceneDesc &S, unsigned cell, const FluidI &I, Kahan3 &f,
+                                               bool solid_i) {
     const float4 *__restrict__ spos = S.spos;
     const float4 *__restrict__ svel = S.svel;
     const float *__restrict__ sdens = S.sdens;
     unsigned count = 0;
     for_each_neighbour(S, cell, [&](unsigned kk) {
+        const bool solid_j = MIXED && S.phase[min(S.cellparticles[kk], S.pnum - 1)] != 0u;
+        if (solid_i && solid_j) {
+            count += norm2(sub3(xyz(spos[kk]), I.ipos)) <= I.B.lt;
+            return;
+        }
         const float rho = sdens[kk];
-        count += fluid_pair(I, xyz(spos[kk]), xyz(svel[kk]), fluid_pressure(rho, I.rho0, I.stiff), rcp_approx(rho),
-                            f) <= I.B.lt;
+        float pi = I.pi, pj = fluid_pressure(rho, I.rho0, I.stiff);
+        if (MIXED && (solid_i || solid_j)) {
+            pi = fmaxf(pi, 0.f);
+            pj = fmaxf(pj, 0.f);
+        }
+        count += fluid_pair_p(I, pi, xyz(spos[kk]), xyz(svel[kk]), pj, rcp_approx(rho), f) <= I.B.lt;
     });
     return count;
 }
 
+template <bool MIXED>
 __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
+    if (MIXED && !S.phase) continue;  // the plain instantiation covers those
+    if (!MIXED && S.phase) continue;
     if (item < active_count(S)) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
         const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(S.svel[k]), S.sdens[k]);
+        const bool solid_i = mixed_solid<MIXED>(S, i);
         Kahan3 f;
-        fluid_scan(S, S.gridcell[i], I, f);
-        fluid_finish(S, i, I, f, fuse_step);
+        fluid_scan<MIXED>(S, S.gridcell[i], I, f, solid_i);
+        fluid_finish(S, i, I, f, fuse_step, mixed_extra<MIXED>(S, i, solid_i));
     }
     SPH_END_WORK
 }
@@ -290,13 +356,17 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
 // scene leaves to it.
 // At most 64 registers: with the current walk 64 beats 56 (0.1886 ->
 // 0.1859 ms at 1M particles), where the earlier walk ran best at 56.
+template <bool MIXED>
 __global__ void __maxnreg__(64) k_forces_fluids_masked(const SceneDesc *__restrict__ scenes, BlockMap map, int fuse_step) {
     SPH_FOR_WORK(map)
+    if (MIXED && !S.phase) continue;  // the plain instantiation covers those
+    if (!MIXED && S.phase) continue;
     if (item < active_count(S)) {
         const unsigned k = item;
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
         const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(S.svel[k]), S.sdens[k]);
         const unsigned cell = S.gridcell[i];
+        const bool solid_i = mixed_solid<MIXED>(S, i);
         Kahan3 f;
         unsigned count = 0;  // num_neighbours, which the density pass left to this one
         if (S.ncand[k] != SPH_NCAND_SCAN) {
@@ -340,19 +410,19 @@ __global__ void __maxnreg__(64) k_forces_fluids_masked(const SceneDesc *__restri
                             const unsigned t2 = (unsigned)(__ffs(m) - 1);
                             m &= m - 1u;
                             const float4 p2 = spos[b + t2], v2 = svel[b + t2];
-                            count += fluid_pair<true>(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
-                            count += fluid_pair<true>(I, xyz(p2), xyz(v2), p2.w, v2.w, f) <= I.B.lt;
+                            walk_pair<MIXED>(I, solid_i, p1, v1, f, count);
+                            walk_pair<MIXED>(I, solid_i, p2, v2, f, count);
                         } else {
-                            count += fluid_pair<true>(I, xyz(p1), xyz(v1), p1.w, v1.w, f) <= I.B.lt;
+                            walk_pair<MIXED>(I, solid_i, p1, v1, f, count);
                         }
                     }
                 }
             }
         } else {
-            count = fluid_scan(S, cell, I, f);
+            count = fluid_scan<MIXED>(S, cell, I, f, solid_i);
         }
         if (!S.num_symmetry_planes) S.num_neighbours[i] = count;
-        fluid_finish(S, i, I, f, fuse_step);
+        fluid_finish(S, i, I, f, fuse_step, mixed_extra<MIXED>(S, i, solid_i));
     }
     SPH_END_WORK
 }

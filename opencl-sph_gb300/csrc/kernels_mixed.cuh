@@ -1,0 +1,149 @@
+// kernels_mixed.cuh -- fluid and elastic solid particles in one scene
+// (extension; sm_103a).
+//
+// The reference runs one program per store (src/opencl/particle_system_host.c:
+// 184-313), so a scene is either a fluid (kernels/fluids.cl) or a solid
+// (kernels/solid_svk.cl).  A mixed scene lists both programs and carries a
+// per-particle `phase` field: 0 = fluid, 1 = St. Venant-Kirchhoff solid.
+//   - Density (common.cl:610-690) covers every neighbour, whatever its
+//     phase; a solid particle's rest density (solids.cl:99-170) covers its
+//     solid neighbours only.
+//   - A solid particle's deformation gradient and elastic pair forces
+//     (solid_svk.cl:82-367) cover its solid neighbours only, with the
+//     store's `solid_viscosity` in place of `viscosity` when present.
+//   - Every pair with at least one fluid particle takes the fluid pair term
+//     of fluids.cl:1-63 -- pressure from each particle's own density
+//     through the fluid's equation of state, plus viscosity -- which is
+//     antisymmetric, so the momentum one particle gains the other loses.
+//     A fluid particle sums it over all its neighbours; a solid particle
+//     over its fluid neighbours, added to its elastic force
+//     (k_forces_fluids_masked<true>, kernels_fluid.cuh).
+// Rigid bodies (body_dynamic 2) are fluid-phase particles and move as
+// bodies, as in a fluid scene.
+#pragma once
+
+#include "kernels_solid.cuh"
+
+// Rest density of a mixed scene's particles: the poly6 sum over neighbours
+// of the particle's own phase (j = i included), from the cell-sorted
+// positions, in the stencil's order.
+__global__ void k_original_density_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (!S.phase) continue;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        const SolidConsts C = solid_consts(S);
+        const float3 ipos = xyz(S.spos[k]);
+        const unsigned ph = S.phase[i];
+        Kahan rho;
+        for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+            const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+            if (S.phase[j] != ph) return;
+            const float r2 = norm2(sub3(xyz(S.spos[kk]), ipos));
+            if (r2 <= C.le) {
+                const float d = fmaxf(C.h2 - r2, 0.f);
+                rho.add(d * d * d);
+            }
+        });
+        S.density0[i] = poly6_density(rho.s, C.h2, C.h, C.mass);
+    }
+    SPH_END_WORK
+}
+
+// compute_deformations (solid_svk.cl:82-175) of a mixed scene's solid
+// particles over their solid neighbours: F = Apq Aqq^-1 with
+// Apq = sum W(|p|) p q^T and Aqq = sum W(|p|) q q^T over j != i, |p| <= h.
+__global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (!S.phase) continue;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        if (S.phase[i] != 0u) {
+            const SolidConsts C = solid_consts(S);
+            const float3 ipos = xyz(S.spos[k]);
+            const float3 ipos0 = ld3(S.originalpos, i);
+            float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            float aqq[6] = {0, 0, 0, 0, 0, 0};
+            for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+                if (j == i || S.phase[j] == 0u) return;
+                const float3 p = sub3(xyz(S.spos[kk]), ipos);
+                const float r2 = norm2(p);
+                if (!(r2 <= C.le)) return;
+                const float d = fmaxf(C.h2 - r2, 0.f);
+                const float w = d * d * d;
+                const float3 q = sub3(ld3(S.originalpos, j), ipos0);
+                add_outer(p * w, q, apq);
+                const float3 wq = q * w;
+                aqq[0] = __fmaf_rn(wq.x, q.x, aqq[0]);
+                aqq[1] = __fmaf_rn(wq.y, q.y, aqq[1]);
+                aqq[2] = __fmaf_rn(wq.z, q.z, aqq[2]);
+                aqq[3] = __fmaf_rn(wq.x, q.y, aqq[3]);
+                aqq[4] = __fmaf_rn(wq.x, q.z, aqq[4]);
+                aqq[5] = __fmaf_rn(wq.y, q.z, aqq[5]);
+            });
+            float inv[6];
+            sym_inverse(aqq, inv);
+            float F[9];
+            mul_as(apq, inv, F);
+            for (int c = 0; c < 9; ++c) S.deformation[9 * (size_t)i + c] = F[c];
+        }
+    }
+    SPH_END_WORK
+}
+
+// compute_forces_solids (solid_svk.cl:182-367) of a mixed scene's solid
+// particles over their solid neighbours j != i with rest or current
+// distance <= h: the elastic pair term from both stresses and the
+// Laplacian viscosity (solid_viscosity when the store has it).  Writes
+// force, force_elastic, force_viscous and cutoff_force (no symmetry
+// planes: the cut-off force is the whole force); the fluid force pass then
+// adds the particle's fluid pair terms and steps it.
+__global__ void k_forces_solids_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
+    SPH_FOR_WORK(map)
+    if (!S.phase) continue;
+    if (item < active_count(S)) {
+        const unsigned k = item;
+        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
+        if (S.phase[i] != 0u) {
+            const SolidConsts C = solid_consts(S);
+            const float3 ipos = xyz(S.spos[k]);
+            const float3 ivel = ld3(S.velocity, i);
+            const float3 ipos0 = ld3(S.originalpos, i);
+            float si[6];
+            for (int c = 0; c < 6; ++c) si[c] = S.stress[6 * (size_t)i + c];
+            const float rho0i = S.density0[i];
+            Kahan3 fe_s, fv_s;
+            for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
+                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
+                if (j == i || S.phase[j] == 0u) return;
+                const float3 jpos = xyz(S.spos[kk]);
+                const float3 x = sub3(ipos0, ld3(S.originalpos, j));
+                const float r2 = norm2(sub3(jpos, ipos));
+                if (!(norm2(x) <= C.le || r2 <= C.le)) return;
+                const float3 jvel = ld3(S.velocity, j);
+                const float vivj = C.mass * C.mass / rho0i / S.density0[j];
+                const float mrj = C.mass / S.density[j];
+                float sj[6];
+                for (int c = 0; c < 6; ++c) sj[c] = S.stress[6 * (size_t)j + c];
+                const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
+                const float3 f_ji = sym_vec(si, gx) * (-vivj);
+                const float3 f_ij = S.body_number[j] > 0 ? -f_ji : sym_vec(sj, -gx) * (-vivj);
+                const float3 fe = f_ij - f_ji;
+                const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
+                const float3 fv = (jvel - ivel) * (mrj * lap);
+                fe_s.add(fe);
+                fv_s.add(fv);
+            });
+            const float visc = S.solid_viscosity ? *S.solid_viscosity : *S.viscosity;
+            const float3 fe = fe_s.get() * 0.5f, fv = fv_s.get() * visc;
+            st3(S.force, i, fe + fv);
+            st3(S.force_elastic, i, fe);
+            st3(S.force_viscous, i, fv);
+            st3(S.cutoff_force, i, fe + fv);
+        }
+    }
+    SPH_END_WORK
+}

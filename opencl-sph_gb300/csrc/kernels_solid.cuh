@@ -487,7 +487,8 @@ __global__ void k_deformations_planes(const SceneDesc *__restrict__ scenes, Bloc
 // S = lambda tr(E) I + 2 mu E, sigma = F S F^T / det F.
 __global__ void k_stresses_svk(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
-    if (item < active_count(S)) {
+    // a mixed scene's fluid particles have no deformation gradient
+    if (item < active_count(S) && !(S.phase && S.phase[item] == 0u)) {
         float f[9], o[6];
         for (int c = 0; c < 9; ++c) f[c] = S.deformation[9 * (size_t)item + c];
         svk_stress(S, f, o);

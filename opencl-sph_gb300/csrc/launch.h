@@ -25,12 +25,17 @@ struct Launch {
     // rigid bodies of the table (device list; none when num_rigid is 0)
     const RigidWork *rigid;
     unsigned num_rigid;
+    // some scene of the table is a mixed fluid-solid scene (its phase
+    // field is set): the mixed kernels are launched too
+    bool has_mixed;
 };
 
 // At most this many rigid bodies per launch (the reduction grid's y extent).
 #define SPH_MAX_RIGID_WORK 65535u
 
-enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2 };
+// MAT_MIXED: fluid and St. Venant-Kirchhoff particles in one scene, told
+// apart by the `phase` field (extension; plain stores only)
+enum SphMaterial { MAT_FLUID = 0, MAT_COROT = 1, MAT_SVK = 2, MAT_MIXED = 3 };
 
 // Neighbour grid, the reference's kernels one by one.
 void sph_launch_find_bins(const Launch &L);
@@ -74,6 +79,13 @@ void sph_launch_deformations(const Launch &L, bool with_density = false, bool wi
 // masked: a fused substep's force pass over the first pair pass's masks;
 // fuse_step: also step_forward for the plane-free scenes it covers
 void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false, bool fuse_step = false);
+
+// Mixed fluid-solid scenes: rest density, deformation gradient and the
+// elastic pair forces of the solid particles over their solid neighbours
+// (the force pass of fluids.cl then adds the fluid-solid pair terms).
+void sph_launch_original_density_mixed(const Launch &L);
+void sph_launch_deformations_mixed(const Launch &L);
+void sph_launch_forces_solids_mixed(const Launch &L);
 
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
 void sph_launch_set_body_rotation(const Launch &L, unsigned body, const float euler[3]);

@@ -64,6 +64,11 @@ struct SceneDesc {
     const unsigned *plane_constraints_particles;
     const unsigned *body_number, *body_dynamic, *body_count;
     float *body_position, *body_euler_rotation;
+    // mixed fluid-solid scenes (extension; null otherwise): per particle 0
+    // = fluid (fluids.cl's law), 1 = elastic solid (solid_svk.cl's law),
+    // and the solids' own viscosity (the store's `viscosity` when absent)
+    const unsigned *phase;
+    const float *solid_viscosity;
     // shape, fixed when the store is created
     unsigned pnum;
     unsigned gridres[3];

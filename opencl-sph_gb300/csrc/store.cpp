@@ -168,6 +168,7 @@ unsigned sph_parse_programs(const char *file_list, std::string *err) {
 }
 
 int sph_material_of(unsigned programs) {
+    if ((programs & PROG_FLUIDS) && (programs & PROG_SVK)) return MAT_MIXED;
     if (programs & PROG_COROT) return MAT_COROT;
     if (programs & PROG_SVK) return MAT_SVK;
     if (programs & PROG_FLUIDS) return MAT_FLUID;
@@ -234,6 +235,22 @@ bool sph_resolve_scene(const psdata &h, char *d, unsigned programs, SceneDesc *d
         unsigned be = h.data_sizes[get_field_psdata(h, "body_euler_rotation")] / 12u;
         desc->body_capacity = std::min(desc->body_capacity, std::min(bp, be));
     }
+    // fluids with an elastic model in one store: the extension's mixed
+    // scene, whose particles carry a phase (0 fluid, 1 solid)
+    if ((programs & PROG_FLUIDS) && (programs & PROG_COROT)) {
+        *err = "fluids with solid_corotation in one store: the fluid-solid coupling (extension) is built for "
+               "solid_svk";
+        return false;
+    }
+    int sv = get_field_psdata(h, "solid_viscosity");
+    if ((programs & PROG_FLUIDS) && (programs & PROG_SVK)) {
+        const FieldReq kMixed[] = {{"phase", 'u', PER_PARTICLE, 1}};
+        if (!check_all(h, kMixed, P, C, "fluids with solid_svk (mixed scene)", err)) return false;
+        if (sv >= 0 && (h.data_ptrs[sv].type != T_FLOAT32 || h.data_sizes[sv] < 4u)) {
+            *err = "solid_viscosity must be a float";
+            return false;
+        }
+    }
     int wb = get_field_psdata(h, "wallbounds");
     if (wb >= 0 && (h.data_ptrs[wb].type != T_FLOAT32 || h.data_sizes[wb] < 24u)) {
         *err = "wallbounds must be 6 floats (xmin, xmax, ymin, ymax, zmin, zmax)";
@@ -281,6 +298,10 @@ bool sph_resolve_scene(const psdata &h, char *d, unsigned programs, SceneDesc *d
     desc->body_count = dev_field<const unsigned>(h, d, "body_count");
     desc->body_position = dev_field<float>(h, d, "body_position");
     desc->body_euler_rotation = dev_field<float>(h, d, "body_euler_rotation");
+    if (programs & PROG_FLUIDS && programs & PROG_SVK) {
+        desc->phase = dev_field<const unsigned>(h, d, "phase");
+        desc->solid_viscosity = sv >= 0 ? dev_field<const float>(h, d, "solid_viscosity") : nullptr;
+    }
     desc->num_scan_blocks = (C + SPH_SCAN_TILE - 1) / SPH_SCAN_TILE;
     return true;
 }

@@ -181,7 +181,7 @@ def wcsph_slab_1m(seed=0):
                        walls=True, stiffness=0.375, viscosity=0.025, name="wcsph-1m")
 
 
-def ball(radius, spacing, center):
+def ball_points(radius, spacing, center):
     """Lattice points within `radius` of `center` (x-fastest order)."""
     k = int(math.floor(radius / spacing))
     g = np.arange(-k, k + 1) * spacing
@@ -211,7 +211,7 @@ def rigid_body_scene(radius=0.05, spacing=0.01, h=0.02, center=(0.2, 0.2, 0.2), 
         body.append(np.zeros(len(f), np.uint32))
         vels.append(np.zeros((len(f), 3)))
     for k, (rad, cen, v0, w0) in enumerate(balls or [(radius, center, velocity, omega)]):
-        b = ball(rad, spacing, cen)
+        b = ball_points(rad, spacing, cen)
         parts.append(b)
         body.append(np.full(len(b), k + 1, np.uint32))
         r = b.astype(np.float64) - np.asarray(cen, dtype=np.float64)
@@ -249,6 +249,83 @@ def large_scene(seed=0):
     cube = solid_lattice(32, 32, 32, spacing=0.005, h=0.01, material="svk", youngs_modulus=5e4, poisson=0.35,
                          dt=2e-5, clamp_layers=0, jitter=5e-5, seed=seed + 1, name="large-svk-cube")
     return [fluid, cube]
+
+
+MIXED_KERNELS = "common, fluids, solids, solid_svk, rigidbody"
+
+
+def fluid_solid_scene(fluid=(12, 8, 12), cube=(6, 6, 6), cube_origin=None, cube_velocity=(0.0, 0.0, 0.0),
+                      ball=None, spacing=0.01, h=0.02, box=(0.0, 0.4), restdens=1000.0, stiffness=3.0,
+                      viscosity=0.2, youngs_modulus=5e4, poisson=0.35, solid_viscosity=6e-5,
+                      gravity=(0.0, -9.8, 0.0), dt=1e-4, jitter=1e-4, seed=0, walls=True, gridbounds=None,
+                      name=None):
+    """Fluid, an elastic St. Venant-Kirchhoff cube and optionally a rigid
+    ball in one interacting scene (the mixed-scene extension: the store
+    lists both fluids.cl and solid_svk.cl, and `phase` tells each particle's
+    law -- 0 fluid, 1 solid).  The fluid block fills the low corner of the
+    box; the cube (cube = lattice counts) sits at `cube_origin` (default:
+    resting on the fluid's surface, centred over it) with an initial
+    velocity; `ball` = (radius, center, velocity) adds a rigid body of
+    fluid-phase particles (body_dynamic 2).  Every particle carries the
+    store's mass (restdens spacing^3), so the cube and the ball are as
+    dense as the fluid.  Particle order: fluid, cube, ball."""
+    rng = np.random.default_rng(seed)
+    origin = (box[0] + spacing / 2,) * 3
+    f = lattice(*fluid, spacing, origin=origin, jitter=jitter, rng=rng)
+    if cube_origin is None:
+        top = origin[1] + (fluid[1] - 1) * spacing
+        cube_origin = (origin[0] + 0.5 * (fluid[0] - cube[0]) * spacing, top + spacing,
+                       origin[2] + 0.5 * (fluid[2] - cube[2]) * spacing)
+    c = lattice(*cube, spacing, origin=cube_origin, jitter=jitter, rng=rng)
+    parts, phase, body, vel = [f, c], [np.zeros(len(f), np.uint32), np.ones(len(c), np.uint32)], \
+        [np.zeros(len(f), np.uint32), np.zeros(len(c), np.uint32)], \
+        [np.zeros((len(f), 3)), np.tile(np.asarray(cube_velocity, np.float64), (len(c), 1))]
+    nb = 0
+    if ball is not None:
+        radius, center, v0 = ball
+        b = ball_points(radius, spacing, center)
+        parts.append(b)
+        phase.append(np.zeros(len(b), np.uint32))
+        body.append(np.ones(len(b), np.uint32))
+        vel.append(np.tile(np.asarray(v0, np.float64), (len(b), 1)))
+        nb = 1
+    pos = np.concatenate(parts).astype(np.float32)
+    n = len(pos)
+    gb = list(gridbounds) if gridbounds is not None else [box[0], box[1]] * 3
+    entries = _common_entries(n, restdens * spacing ** 3, dt, h, gravity, gb, body_count=max(nb, 1))
+    entries += [("restdens", "1", "float", restdens), ("stiffness", "1", "float", stiffness),
+                ("viscosity", "1", "float", viscosity), ("solid_viscosity", "1", "float", solid_viscosity),
+                ("youngs_modulus", "1", "float", youngs_modulus), ("poisson", "1", "float", poisson),
+                ("originalpos", "3, pnum", "float", None), ("density0", "pnum", "float", None),
+                ("deformation", "3, 3, pnum", "float", None), ("stress", "6, pnum", "float", None),
+                ("rotation", "3, 3, pnum", "float", None),
+                ("cutoff_force", "3, pnum", "float", None), ("force_elastic", "3, pnum", "float", None),
+                ("force_viscous", "3, pnum", "float", None), ("padding", "pnum", "unsigned int", None),
+                ("body_position", "3, body_count", "float", None),
+                ("body_euler_rotation", "3, body_count", "float", None),
+                ("phase", "pnum", "unsigned int", None)]
+    if walls:
+        entries.append(("wallbounds", "6", "float", [box[0], box[1]] * 3))
+    init = {"position": pos, "n": n, "velocity": np.concatenate(vel).astype(np.float32),
+            "phase": np.concatenate(phase), "body_number": np.concatenate(body),
+            "body_dynamic": np.full(max(nb, 1), 2 if nb else 0, np.uint32)}
+    sc = Scene(name or "mixed-%d" % n, "mixed", MIXED_KERNELS, entries, init, n)
+    sc.counts = {"fluid": len(f), "cube": len(c), "ball": len(parts[2]) if nb else 0}
+    return sc
+
+
+def large_fluid_solid_scene(seed=0):
+    """The large single scene as one interacting scene: 1,048,576 WCSPH
+    particles (the 128 x 64 x 128 slab of wcsph_slab_1m), a 32^3 SVK cube
+    (E = 5e4 Pa, nu = 0.35, 0.005 m spacing) resting on the slab's surface,
+    and a rigid ball of radius 0.05 m (4,169 lattice particles) dropped into
+    the slab beside it; dt = 2e-5 s.  The fluid's stiffness and viscosity
+    are the slab's (the dam break's scaled by its 1/8 particle mass); the
+    cube keeps the reference conf's solid viscosity, 6e-5."""
+    return fluid_solid_scene(fluid=(128, 64, 128), cube=(32, 32, 32), ball=(0.05, (0.16, 0.40, 0.16), (0.0, 0.0, 0.0)),
+                             spacing=0.005, h=0.01, box=(0.0, 1.0), stiffness=0.375, viscosity=0.025,
+                             youngs_modulus=5e4, poisson=0.35, solid_viscosity=6e-5, dt=2e-5, jitter=5e-5,
+                             seed=seed, name="large-fluid+cube+ball")
 
 
 def solid_lattice(nx=10, ny=10, nz=40, spacing=0.01, h=0.02, material="corot", youngs_modulus=1e5,

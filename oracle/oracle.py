@@ -62,6 +62,7 @@ def _state_type(real):
         ("has_wallbounds", c_uint), ("wallbounds", real * 6),
         ("guards", c_int), ("nthreads", c_int),
         ("body_capacity", c_uint), ("rigid_state", POINTER(c_double)), ("rigid_offset", P),
+        ("phase", U), ("has_solid_viscosity", c_uint), ("solid_viscosity", real),
     ]})
 
 RIGID_STRIDE = 64  # ORACLE_RIGID_STRIDE
@@ -109,7 +110,9 @@ class OracleScene(object):
             if name in fields:
                 arr.reshape(-1)[:] = np.asarray(fields[name], dtype=np.float64).reshape(-1)[:arr.size]
             self.a[name] = arr
-        for name in UINT_FIELDS + ["body_number", "plane_constraints_particles"]:
+        # mixed fluid-solid scenes (extension): the per-particle phase
+        extra_uint = ["phase"] if "phase" in fields else []
+        for name in UINT_FIELDS + ["body_number", "plane_constraints_particles"] + extra_uint:
             arr = np.zeros(P, dtype=np.uint32)
             if name in fields:
                 arr[:] = np.asarray(fields[name]).reshape(-1)[:P]
@@ -155,6 +158,9 @@ class OracleScene(object):
             st.wallbounds[:] = [float(x) for x in np.ravel(fields["wallbounds"])[:6]]
         st.guards = guards
         st.nthreads = nthreads
+        if "solid_viscosity" in fields:
+            st.has_solid_viscosity = 1
+            st.solid_viscosity = scal("solid_viscosity")
         # rigid bodies (extension): state per body, offsets per particle
         st.body_capacity = int(self.a["body_dynamic"].size)
         self.rigid_state = np.zeros((st.body_capacity, RIGID_STRIDE), np.float64)
@@ -224,6 +230,14 @@ class OracleScene(object):
             self.call("compute_deformations")
             self.call("compute_stresses_svk")
             self.call("compute_forces_solids_svk")
+        elif material == "mixed":
+            # fluid and SVK particles in one scene (extension): the solids'
+            # elastic passes, then the fluid pass, which adds the fluid pair
+            # terms to the solids' elastic forces
+            self.call("compute_deformations")
+            self.call("compute_stresses_svk")
+            self.call("compute_forces_solids_svk")
+            self.call("compute_forces_fluids")
         else:
             raise ValueError(material)
         self.call("step_forward")

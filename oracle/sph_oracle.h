@@ -35,6 +35,12 @@
  *     by the distance there, fluids.cl:48 and common.cl:83, producing NaN;
  *     FP32 WCSPH under tension can merge two particles exactly).
  * With guards = 0 the oracle reproduces the reference bit for bit.
+ *
+ * Mixed fluid-solid scenes (phase != NULL) are an extension with no
+ * reference counterpart: a solid particle's rest density, deformation
+ * gradient, stress and elastic forces cover its solid neighbours only; the
+ * fluid force pass gives every pair with a fluid particle the fluid pair
+ * term (fluids.cl:1-63), which a solid particle adds to its elastic force.
  */
 #ifndef SPH_ORACLE_H_
 #define SPH_ORACLE_H_
@@ -73,7 +79,12 @@ extern "C" {
     /* rigid_offset[3 * n] the particles' body-frame offsets               */ \
     unsigned int body_capacity;                                                \
     double *rigid_state;                                                       \
-    REAL *rigid_offset;
+    REAL *rigid_offset;                                                        \
+    /* mixed fluid-solid scenes (extension, not in the reference): phase  */ \
+    /* per particle (0 fluid, 1 SVK solid; NULL: one material) and the    */ \
+    /* solids' own viscosity when has_solid_viscosity                     */ \
+    unsigned int *phase;                                                       \
+    unsigned int has_solid_viscosity; REAL solid_viscosity;
 
 #define ORACLE_BODY_RIGID 2u
 #define ORACLE_RIGID_STRIDE 64

@@ -302,6 +302,8 @@ static void OF(density_pass)(OST *s, REAL *out, int with_count) {
         out[i] = 0;
         if (with_count) s->num_neighbours[i] = 0;
         O_FOR_NEIGHBOURS(s, i, j, {
+            /* a mixed scene's rest density: neighbours of i's own phase */
+            if (!with_count && s->phase && s->phase[j] != s->phase[i]) continue;
             V3 jpos = OF(v3_load)(s->position, j);
             V3 diff = OF(v3_sub)(jpos, ipos);
             REAL dist = OF(v3_len)(diff);
@@ -353,10 +355,21 @@ void OF(oracle_compute_forces_fluids)(OST *s) {
         unsigned i = (unsigned)ii;
         V3 ipos = OF(v3_load)(s->position, i), ivel = OF(v3_load)(s->velocity, i);
         V3 fi = OF(v3)(0, 0, 0);
+        /* a mixed scene's solid particle: fluid neighbours only, added to
+         * the elastic force compute_forces_solids left in force */
+        const int solid_i = s->phase && s->phase[i];
         O_FOR_NEIGHBOURS(s, i, j, {
             if (j == i) continue;
+            if (solid_i && s->phase[j]) continue;
             REAL p_i = (s->density[i] - s->restdens) * s->stiffness;
             REAL p_j = (s->density[j] - s->restdens) * s->stiffness;
+            /* a fluid-solid pair of a mixed scene pushes, never pulls: both
+             * pressures clamped at 0 (the solid's density deficit at its
+             * surface would otherwise draw fluid into it) */
+            if (s->phase && (s->phase[i] || s->phase[j])) {
+                if (p_i < 0) p_i = 0;
+                if (p_j < 0) p_j = 0;
+            }
             V3 jpos = OF(v3_load)(s->position, j), jvel = OF(v3_load)(s->velocity, j);
             V3 diff = OF(v3_sub)(jpos, ipos), relvel = OF(v3_sub)(jvel, ivel);
             REAL dist = OF(v3_len)(diff);
@@ -372,6 +385,7 @@ void OF(oracle_compute_forces_fluids)(OST *s) {
             fi = OF(v3_add)(fi, OF(v3_div)(OF(v3_add)(OF(v3_mul)(diff, pterm), OF(v3_mul)(relvel, vterm)), didj));
         })
         fi = OF(v3_mul)(fi, s->mass);
+        if (solid_i) fi = OF(v3_add)(fi, OF(v3_load)(s->force, i));
         fi.x = OF(cube_bound)(ipos.x, fi.x);
         fi.y = OF(cube_bound)(ipos.y, fi.y);
         fi.z = OF(cube_bound)(ipos.z, fi.z);
@@ -508,9 +522,12 @@ static void OF(forces_solids)(OST *s, int corot) {
     const REAL *sp = s->symmetry_planes;
     static const REAL ident[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     long n = s->n;
+    /* a mixed scene's solids take their own viscosity */
+    const REAL visc = s->has_solid_viscosity ? s->solid_viscosity : s->viscosity;
 #pragma omp parallel for schedule(dynamic, 256) num_threads(s->nthreads > 0 ? s->nthreads : 1)
     for (long ii = 0; ii < n; ++ii) {
         unsigned i = (unsigned)ii;
+        if (s->phase && !s->phase[i]) continue; /* a mixed scene's fluid particle */
         V3 ipos = OF(v3_load)(s->position, i), ivel = OF(v3_load)(s->velocity, i);
         V3 ipos0 = OF(v3_load)(s->originalpos, i);
         const REAL *ist = s->stress + 6 * (size_t)i;
@@ -518,6 +535,7 @@ static void OF(forces_solids)(OST *s, int corot) {
         V3 fe_sum = OF(v3)(0, 0, 0), fv_sum = OF(v3)(0, 0, 0);
         V3 fec = OF(v3)(0, 0, 0), fvc = OF(v3)(0, 0, 0);
         O_FOR_NEIGHBOURS(s, i, j, {
+            if (s->phase && !s->phase[j]) continue;
             V3 jpos0 = OF(v3_load)(s->originalpos, j);
             V3 x = OF(v3_sub)(ipos0, jpos0);
             V3 jpos = OF(v3_load)(s->position, j), jvel = OF(v3_load)(s->velocity, j);
@@ -573,12 +591,12 @@ static void OF(forces_solids)(OST *s, int corot) {
             }
         })
         fe_sum = OF(v3_mul)(fe_sum, (REAL)0.5f);
-        fv_sum = OF(v3_mul)(fv_sum, s->viscosity);
+        fv_sum = OF(v3_mul)(fv_sum, visc);
         OF(v3_store)(OF(v3_add)(fe_sum, fv_sum), s->force, i);
         OF(v3_store)(fe_sum, s->force_elastic, i);
         OF(v3_store)(fv_sum, s->force_viscous, i);
         fec = OF(v3_mul)(fec, (REAL)0.5f);
-        fvc = OF(v3_mul)(fvc, s->viscosity);
+        fvc = OF(v3_mul)(fvc, visc);
         OF(v3_store)(OF(v3_add)(fec, fvc), s->cutoff_force, i);
     }
 }
@@ -596,9 +614,11 @@ void OF(oracle_compute_deformations)(OST *s) {
 #pragma omp parallel for schedule(dynamic, 256) num_threads(s->nthreads > 0 ? s->nthreads : 1)
     for (long ii = 0; ii < n; ++ii) {
         unsigned i = (unsigned)ii;
+        if (s->phase && !s->phase[i]) continue; /* a mixed scene's fluid particle */
         V3 ipos = OF(v3_load)(s->position, i), ipos0 = OF(v3_load)(s->originalpos, i);
         REAL apq[9] = {0}, aqq[6] = {0};
         O_FOR_NEIGHBOURS(s, i, j, {
+            if (s->phase && !s->phase[j]) continue;
             V3 jpos = OF(v3_load)(s->position, j), jpos0 = OF(v3_load)(s->originalpos, j);
             V3 p = OF(v3_sub)(jpos, ipos), q = OF(v3_sub)(jpos0, ipos0);
             REAL w = OF(k_poly6)(OF(v3_len)(p), h);
@@ -640,6 +660,7 @@ void OF(oracle_compute_stresses_svk)(OST *s) {
     long n = s->n;
 #pragma omp parallel for schedule(static) num_threads(s->nthreads > 0 ? s->nthreads : 1)
     for (long i = 0; i < n; ++i) {
+        if (s->phase && !s->phase[i]) continue; /* a mixed scene's fluid particle */
         const REAL *F = s->deformation + 9 * i;
         REAL Ft[9], ftf[9], g[6], svk[6], tmp[9], cau[9];
         OF(transpose)(F, Ft);
