@@ -8,8 +8,9 @@ Workloads (seeded synthetic scenes; sph/scenes.py):
                1,000-65,536 particles each, log-uniform) advanced together,
                one CUDA graph per substep (default: the headline metric is
                the batched/served form against the plain per-scene loop)
-  large-scene  1,048,576 WCSPH particles with a rigid ball dropped into
-               them, plus a 32^3 SVK cube, as one batch
+  large-scene  one interacting scene: 1,048,576 WCSPH particles, a 32^3
+               SVK cube resting on them and a rigid ball dropped beside it
+               (the mixed fluid-solid extension), through the drop-in
   wcsph-1m     1,048,576-particle WCSPH slab (128 x 64 x 128 at 0.005 m,
                h = 0.01 m) in [0,1]^3: the plain single-scene drop-in path
   dam-8k       8,000-particle WCSPH dam break (20^3 at 0.01 m, h = 0.02 m)
@@ -19,17 +20,22 @@ One JSON line on rank 0.  `value` is device throughput over the K timed
 substeps (CUDA events on the work's stream; plain scenes flush the L2 with a
 256 MB write between substeps, outside the events; the batched working set
 exceeds the L2).  `e2e` repeats the measurement through the public API with
-host buffers (per step: the substep, then every scene's positions read
-into its host store).  `roofline` sets the dominant phase's algorithmic
-bytes against the measured HBM peak (phase times from live CUDA events).
+host buffers (per step: the step's inputs -- time step and gravity -- written
+from the host stores, the substep, then every scene's positions read into
+its host store).  `roofline` sets the dominant phase's algorithmic bytes
+against the measured HBM peak (phase times from live CUDA events).
 `cpu_baseline` times the CPU oracle on a bounded sample.  The default run
-also reports the plain per-scene loop, the served stream (p50/p99), the
-error against the FP64 oracle and the plain 1M scene.  With --impl
-reference the reference's own kernels (oracle/_ref, the reference's
-kernels/*.cl compiled for the host CPU with OpenMP) -- or, where they were
-not built, the C restatement -- run the same workload on all host cores.
-N > 1 GPUs run independent replicas (no collective; scenes do not shard),
-aggregated over ranks.
+also reports the batch after 500 more substeps, the plain per-scene loop,
+the stated SVK stiffness mix, the error against the FP64 oracle (small
+scenes, the dam break, the beam and the 1M slab after 1,000 substeps), the
+served stream (60 s of 50 requests/s, p50/p99) beside the plain loop
+measured one request at a time, the plain 1M slab and the large interacting
+scene.  With --impl reference the reference's own kernels (oracle/_ref, the
+reference's kernels/*.cl compiled for the host CPU with OpenMP, in stores the
+reference's own builder made) run the same workload on all host cores; that
+arm loads neither the sph package nor the CUDA library.  N > 1 GPUs run
+independent replicas (no collective; scenes do not shard), aggregated over
+ranks.
 """
 import argparse
 import ctypes
@@ -111,8 +117,26 @@ MEASURED_INST = {
 }
 
 
-def workload(name, seed):
-    from sph import scenes
+def scenes_module(standalone=False):
+    """The scene builders.  `standalone`: sph/scenes.py loaded on its own,
+    without the sph package, whose import loads the CUDA library -- the
+    reference arm builds the same scenes while mapping only the reference's
+    own CPU libraries."""
+    if not standalone:
+        from sph import scenes
+        return scenes
+    import importlib.util
+    name = "sph_scenes_standalone"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, os.path.join(PKG, "sph", "scenes.py"))
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def workload(name, seed, standalone=False):
+    scenes = scenes_module(standalone)
     if name == "wcsph-1m":
         return scenes.wcsph_slab_1m(seed), \
             ("1,048,576-particle WCSPH slab, 128x64x128 at 0.005 m, h=0.01 m, [0,1]^3 box, dt=2e-5 s, "
@@ -122,6 +146,12 @@ def workload(name, seed):
             "8,000-particle WCSPH dam break, 20^3 at 0.01 m, h=0.02 m, [0,0.4]^3 box, dt=1e-4 s"
     if name == "batched-256":
         raise SystemExit("batched-256 has no single scene")
+    if name == "large-scene":
+        return scenes.large_fluid_solid_scene(seed), \
+            ("large interacting scene: 1,048,576 WCSPH particles (128x64x128 at 0.005 m, h=0.01 m, [0,1]^3, "
+             "dt=2e-5 s, stiffness 0.375, viscosity 0.025), a 32^3 SVK cube (E=5e4 Pa, nu=0.35) resting on the "
+             "fluid and a rigid ball of radius 0.05 m (4,169 particles, body_dynamic 2) dropped beside it, all "
+             "in one store (mixed fluid-solid extension)")
     if name == "beam-4k":
         return scenes.solid_lattice(10, 10, 40, material="corot", seed=seed, name="beam-4k"), \
             "4,000-particle corotational beam 10x10x40 at 0.01 m, E=1e5 Pa, nu=0.3, 2 clamped layers, dt=5e-5 s"
@@ -262,7 +292,7 @@ def bench_plain(args, scene, torch, world):
     """The drop-in path on one scene: K CUDA-graph substeps (sph_update)."""
     from sph import bindings as bnd
     ps = scene.system()
-    if scene.material in ("corot", "svk"):
+    if scene.material != "fluid":
         _solid_setup(ps)
     n = scene.n
     cells = int(np.prod(ps.get_fields("gridres")[0]))
@@ -345,14 +375,11 @@ def run_e2e(ps, scene, steps, torch):
             "d2h_bytes_per_step": 12 * scene.n, "host_memory": "pinned", "transfers": "pipelined"}
 
 
-def batched_scenes(seed, workload="batched-256"):
-    from sph import scenes
-    if workload == "large-scene":
-        return scenes.large_scene(seed)
-    return scenes.batch_mix(256, seed=seed)
+def batched_scenes(seed, workload="batched-256", standalone=False):
+    return scenes_module(standalone).batch_mix(256, seed=seed)
 
 
-BATCHED_WORKLOADS = ("batched-256", "large-scene")
+BATCHED_WORKLOADS = ("batched-256",)
 
 
 def bench_batched(args, torch, world):
@@ -405,9 +432,17 @@ def bench_batched(args, torch, world):
     for sid in ids:
         b.pin(sid)
     b.wait_read(b.read_fields_async(ids, "position"))  # allocates the read buffers
+    b.write_fields_async(ids, "timestep")
+    b.write_fields_async(ids, "gravity")
+    b.synchronize()
+    h2d = sum(16 + 16 for _ in ids) + 2 * ((len(ids) * 24 + 255) // 256 * 256)  # fields + segment tables
     t0 = time.perf_counter()
     prev = None
     for _ in range(args.steps):
+        # each step's inputs: every scene's time step and gravity from its
+        # host store (one staged copy each, scattered on the device)
+        b.write_fields_async(ids, "timestep")
+        b.write_fields_async(ids, "gravity")
         b.step(1)
         t = b.read_fields_async(ids, "position")
         if prev is not None:
@@ -417,6 +452,22 @@ def bench_batched(args, torch, world):
     e2e_s = time.perf_counter() - t0
     for sid in ids:
         b.unpin(sid)
+    # away from the lattice start: the same batch after 500 more substeps
+    late = None
+    if not args.quick:
+        b.step(500)
+        b.synchronize()
+        ls = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(ext):
+            ls[0].record(ext)
+            b.step(args.steps)
+            ls[1].record(ext)
+        torch.cuda.synchronize()
+        late_s = ls[0].elapsed_time(ls[1]) / 1e3
+        late = {"value": n * args.steps / late_s, "ms_per_step": late_s * 1e3 / args.steps,
+                "substeps_before": max(args.warmup, 1) + 2 * args.steps + 500 + 1,
+                "scenes_with_bad_status": sum(1 for sid in ids if b.status(sid) != 0),
+                "how": "the headline batch timed again (CUDA events) after 500 further substeps"}
     status = sum(1 for sid in ids if b.status(sid) != 0)
     cells = 0
     by_mat = {"fluid": [0, 0], "corot": [0, 0], "svk": [0, 0]}
@@ -435,11 +486,14 @@ def bench_batched(args, torch, world):
         counts["svk " + ph] = tuple(by_mat["svk"])
     b.close()
     return {"scenes": scs, "n": n, "cells": cells, "counts": counts, "total_s": total_s, "clocks": clk,
-            "phases": phases, "tuned": tuned,
+            "phases": phases, "tuned": tuned, "late": late,
             "kernels_per_step": kernels_per_step, "status_scenes": status,
-            "e2e": {"value": n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 0,
+            "e2e": {"value": n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 12 * n,
-                    "host_memory": "pinned (sph_batch_pin_host)",
+                    "host_memory": "pinned (sph_batch_pin_host; a page-locked staging buffer for the writes)",
+                    "writes": "per step: every scene's time step and gravity from its host store, one staged "
+                              "host-to-device copy per field and one scatter kernel "
+                              "(sph_batch_write_field_many_async)",
                     "reads": "per step: device snapshot of every scene's positions, written to the host stores "
                              "beside the next substep (sph_batch_read_field_many_async); step s - 1's positions "
                              "are on the host before step s + 1 is enqueued"}}
@@ -475,34 +529,24 @@ def bench_plain_loop(scs, steps):
     return {"synced": n * steps / synced, "graph": n * steps / graph}
 
 
-def plain_step_model(sizes, steps=20):
-    """Measured seconds per drop-in substep (sph_update loop, one sync at
-    the end) for scenes of the mix of each material at the given sizes;
-    returns model(material, n), a log-log interpolation."""
-    from sph import scenes
-    table = {}
-    for material in scenes.MATERIALS:
-        pts = []
-        for n_target in sizes:
-            sc = scenes.mix_member(material, n_target, seed=1)
-            ps = sc.system()
-            if material != "fluid":
-                ps.call_for_all_particles("init_original_position")
-                ps.compute_particle_bins()
-                ps.call_for_all_particles("compute_original_density")
-            ps.update_fused(3)
-            ps.synchronize()
-            t0 = time.perf_counter()
-            ps.update_fused(steps)
-            ps.synchronize()
-            pts.append((sc.n, (time.perf_counter() - t0) / steps))
-            ps.close()
-        table[material] = (np.log([p[0] for p in pts]), np.log([p[1] for p in pts]))
-
-    def model(material, n):
-        xs, ys = table[material]
-        return float(np.exp(np.interp(np.log(n), xs, ys)))
-    return model
+def sequential_plain(requests):
+    """The plain per-scene loop on requests, one at a time through the
+    drop-in path as a reference driver would serve them: build the store
+    (device lattice scenes on the host), set up solids, sph_update for the
+    request's substeps, read the positions back, free.  Returns each
+    request's measured service time (seconds)."""
+    import torch  # noqa: F401  (the CUDA context is up already)
+    out = []
+    for r in requests:
+        t0 = time.perf_counter()
+        ps = r.scene.system()
+        if r.scene.material != "fluid":
+            _solid_setup(ps)
+        ps.update_fused(r.steps)
+        ps.sync_fields_device_to_host("position")
+        ps.close()
+        out.append(time.perf_counter() - t0)
+    return out
 
 
 def _chunk_profile(log):
@@ -520,10 +564,12 @@ def _chunk_profile(log):
 
 
 def bench_served(args):
-    """Poisson arrivals at 50 requests/s; each request a scene of the batched
-    mix with 2,000-262,144 particles (log-uniform) and 100-2,000 substeps
-    (uniform); continuous batching under a 150 GB budget."""
-    import math
+    """Poisson arrivals at 50 requests/s for `served_seconds`; each request a
+    scene of the batched mix with 2,000-262,144 particles (log-uniform) and
+    100-2,000 substeps (uniform); continuous batching under a 150 GB budget.
+    Beside it, the plain per-scene loop measured one request at a time on a
+    seeded 5% subsample of the same requests."""
+    import math  # noqa: F401
     from sph import scenes
     from sph.serving import Server, poisson_requests, release, sequential_fifo
 
@@ -532,13 +578,21 @@ def bench_served(args):
         return scenes.mixed_scene(rng, i, n_range=(2000, 262144), prefix="q", jitter_hash=True)
     reqs = poisson_requests(rate=50.0, duration=args.served_seconds, make_scene=make, steps_range=(100, 2000),
                             seed=args.seed)
-    srv = Server(budget_bytes=150e9, max_chunk=25, max_particles=8 << 20, keep_results=False)
+    srv = Server(budget_bytes=150e9, max_chunk=args.served_chunk, max_particles=8 << 20, keep_results=False)
     srv.prepare(reqs)
     st = srv.run(reqs, realtime=True)
     demand = sum(r.work for r in reqs) / args.served_seconds
-    model = plain_step_model([2000, 16000, 131072, 262144])
-    seq = sequential_fifo(reqs, lambda r: r.steps * model(r.scene.material, r.scene.n))
     release(reqs)
+    # the sequential plain loop, measured: every 20th request (seeded start)
+    rng = np.random.default_rng(args.seed + 1)
+    first = int(rng.integers(20))
+    sub = [r for r in reqs if r.id % 20 == first]
+    service = sequential_plain(sub)
+    seq_work = float(sum(r.work for r in sub))
+    seq_tput = seq_work / float(sum(service))
+    svc = dict(zip([r.id for r in sub], service))
+    # the subsample's own arrivals served one at a time with the measured times
+    seq_sub = sequential_fifo(sub, lambda r: svc[r.id])
     return {"requests": st["requests"], "arrival_rate_per_s": 50.0, "window_s": args.served_seconds,
             "throughput": st["throughput"], "p50_s": st["p50_s"], "p99_s": st["p99_s"],
             "makespan_s": st["makespan_s"], "peak_resident": st["peak_resident"],
@@ -547,12 +601,19 @@ def bench_served(args):
             "requests_with_bad_status": st["status_failed"],
             "offered_load": demand, "saturated": bool(demand > st["throughput"]),
             "policy": "FIFO admission by 150 GB HBM budget and 8M resident particles; scenes built on the "
-                      "device at admission; device-side substep quotas; chunks of up to 25 substeps",
-            "sequential_plain_model": {"throughput": seq["throughput"], "p50_s": seq["p50_s"],
-                                       "p99_s": seq["p99_s"],
-                                       "how": "FIFO queue of one-at-a-time drop-in solves (sph_update loops), "
-                                              "per-substep times measured on this GPU per material at 2k-262k "
-                                              "particles"}}
+                      "device at admission; device-side substep quotas; chunks of up to %d substeps"
+                      % args.served_chunk,
+            "sequential_plain": {
+                "throughput": seq_tput, "requests_measured": len(sub),
+                "particle_steps_measured": seq_work, "seconds_measured": float(sum(service)),
+                "served_vs_sequential": st["throughput"] / seq_tput,
+                "subsample_fifo": {"p50_s": seq_sub["p50_s"], "p99_s": seq_sub["p99_s"],
+                                   "makespan_s": seq_sub["makespan_s"]},
+                "how": "every 20th request of the same stream (seeded), served one at a time through the "
+                       "drop-in path (store built, solids set up, sph_update for the request's substeps, "
+                       "positions read back, store freed), each timed on the host; throughput = their "
+                       "particle-steps over the summed service times; subsample_fifo = the subsample's own "
+                       "arrivals (2.5 requests/s) served one at a time with the measured times"}}
 
 
 def fp64_error_sample(scs, steps):
@@ -611,15 +672,72 @@ def fp64_error_configs():
     return out
 
 
-def cpu_sample(scene, material, steps, nthreads, reference):
-    """Times the CPU oracle (or the reference's own kernels) on `steps`
-    substeps of the scene; returns particle-steps/s."""
+def exact_mix(args, torch):
+    """The batched configuration's mix as stated -- SVK stiffness log-uniform
+    over the whole [1e4, 1e6] Pa -- advanced 500 substeps, then timed over
+    `steps` more (CUDA events); reports the scenes whose status word is set
+    (non-finite positions: the reference's SVK formulation diverges above
+    about 1e5 Pa)."""
+    from sph import scenes
+    from sph.batch import Batch
+    scs = scenes.batch_mix(256, seed=args.seed, svk_e_range=(1e4, 1e6))
+    b = Batch()
+    ids = [b.add(x) for x in scs]
+    n = sum(x.n for x in scs)
+    b.step(500)
+    b.synchronize()
+    ext = torch.cuda.ExternalStream(b.stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    with torch.cuda.stream(ext):
+        ev[0].record(ext)
+        b.step(args.steps)
+        ev[1].record(ext)
+    torch.cuda.synchronize()
+    sec = ev[0].elapsed_time(ev[1]) / 1e3
+    bad = [x.name for x, sid in zip(scs, ids) if b.status(sid) != 0]
+    svk = [x for x in scs if x.material == "svk"]
+    b.close()
+    return {"value": n * args.steps / sec, "unit": UNIT, "ms_per_step": sec * 1e3 / args.steps,
+            "substeps_before": 500, "svk_e_range_pa": [1e4, 1e6], "svk_scenes": len(svk),
+            "scenes_with_bad_status": len(bad), "bad_scenes": bad[:20],
+            "how": "the 256-scene mix of the headline with SVK stiffness drawn from the stated [1e4, 1e6] Pa"}
+
+
+def fp64_error_1m(seed):
+    """The plain 1,048,576-particle WCSPH slab through the drop-in (FP32,
+    fused CUDA-graph substeps) after 1,000 substeps, against the FP64
+    oracle run of the same scene on all host cores."""
     from sph import bindings as bnd
-    from sph import init_data_cpu, free_data_cpu
-    ps = init_data_cpu(scene.spec)
-    v = bnd.store_views(ps)
-    for k, val in scene.init.items():
-        v[k][...] = val
+    from oracle.oracle import OracleScene
+    sc, _ = workload("wcsph-1m", seed)
+    ps = sc.system()
+    o = OracleScene(bnd.store_views(ps.psdata), "f64", nthreads=os.cpu_count() or 1)
+    ps.update_fused(1000)
+    t0 = time.perf_counter()
+    o.run("fluid", 1000)
+    oracle_s = time.perf_counter() - t0
+    ps.sync_device_to_host()
+    p = np.asarray(ps.get_fields("position")[0][: sc.n], dtype=np.float64)
+    q = o.a["position"][: sc.n]
+    out = {"substeps": 1000, "particles": sc.n, "rel_l2": float(np.linalg.norm(p - q) / np.linalg.norm(q)),
+           "max_abs_m": float(np.max(np.abs(p - q))), "status": int(ps.status()),
+           "fp64_oracle_seconds": oracle_s, "target": 1e-4}
+    ps.close()
+    return out
+
+
+def _fill(view, val):
+    arr = np.asarray(val)
+    if arr.size > 1:
+        view[tuple(slice(None, d) for d in arr.shape)] = arr.reshape(arr.shape)
+    else:
+        view[...] = arr
+
+
+def cpu_sample(scene, material, steps, nthreads, reference):
+    """Times the CPU oracle (or, with `reference`, the reference's own
+    kernels in a store the reference's own builder made) on `steps`
+    substeps of the scene; returns (particle-steps, seconds, kind)."""
     kind = "port"
     if reference:
         from oracle import ref
@@ -628,8 +746,8 @@ def cpu_sample(scene, material, steps, nthreads, reference):
     if kind == "reference":
         from oracle import ref
         rs = ref.RefStore(scene.spec)
-        for k in scene.init:
-            rs.view(k)[...] = v[k]
+        for k, val in scene.init.items():
+            _fill(rs.view(k), val)
         prog = {"fluid": "fluid", "corot": "corot", "svk": "svk"}[material]
         rec = {"fluid": ["compute_density", "compute_forces_fluids"],
                "corot": ["compute_density", "compute_rotations_and_strains", "compute_stresses",
@@ -647,30 +765,65 @@ def cpu_sample(scene, material, steps, nthreads, reference):
                 rs.call(prog, "f32", k, scene.n, nthreads)
         closer = rs.free
     else:
+        from sph import bindings as bnd
+        from sph import init_data_cpu, free_data_cpu
         from oracle.oracle import OracleScene
+        ps = init_data_cpu(scene.spec)
+        v = bnd.store_views(ps)
+        for k, val in scene.init.items():
+            _fill(v[k], val)
         orc = OracleScene(v, "f32", nthreads=nthreads)
         if material != "fluid":
             orc.setup_solid()
 
         def one():
             orc.substep(material)
-        closer = None
+
+        def closer():
+            free_data_cpu(ps)
     one()  # warm
     t0 = time.perf_counter()
     for _ in range(steps):
         one()
     el = time.perf_counter() - t0
-    if closer:
-        closer()
-    free_data_cpu(ps)
+    closer()
     return scene.n * steps, el, kind
 
 
-def cpu_workload(name, seed, budget_scenes=None):
+def cpu_workload(name, seed, standalone=False):
     if name in BATCHED_WORKLOADS:
-        scs = batched_scenes(seed, name)
-        return scs if budget_scenes is None else scs[:budget_scenes]
-    return [workload(name, seed)[0]]
+        return batched_scenes(seed, name, standalone)
+    return [workload(name, seed, standalone)[0]]
+
+
+BATCHED_DESC = ("256 independent scenes, 60% WCSPH / 25% corotational / 15% SVK, particle counts log-uniform in "
+                "[1,000, 65,536], E log-uniform [1e4, 1e6] Pa (SVK [1e4, 1e5]: the reference's SVK diverges "
+                "within 2,000 substeps above; the stated range is the exact_mix extra), Poisson uniform "
+                "[0.25, 0.45], 0.01 m spacing, h=0.02 m, seeded jitter")
+
+
+def workload_config(name, seed, standalone=False):
+    """The line's `config`, the same in both arms: the workload, its size
+    and how the L2 is kept out of the timing."""
+    if name in BATCHED_WORKLOADS:
+        scs = batched_scenes(seed, name, standalone)
+        n = sum(x.n for x in scs)
+        return {"workload": name + ": " + BATCHED_DESC, "particles": n, "scenes": len(scs),
+                "l2": "working set %.2f GB > L2 (129 MB); no flush needed" % (n * 300e-9)}
+    sc, desc = workload(name, seed, standalone)
+    return {"workload": name + ": " + desc, "particles": sc.n, "scenes": 1,
+            "l2": "flushed between timed steps (256 MB write, outside the timed events)"}
+
+
+def _plain_extra(args, name, torch, peak, peak_kind):
+    sc, desc = workload(name, args.seed)
+    p = bench_plain(args, sc, torch, 1)
+    return {"workload": name + ": " + desc, "value": p["n"] * args.steps / p["total_s"],
+            "ms_per_step": p["total_s"] * 1e3 / args.steps, "clocks": p["clocks"], "status": p["status"],
+            "kernels_per_step": p["kernels_per_step"], "phase_ms": p["phases"],
+            "roofline": _phase_roofline(p["phases"], p["n"], p["cells"], peak, peak_kind, workload=name,
+                                        clocks=p["clocks"]),
+            "e2e": p["e2e"]}
 
 
 def run_ours(args, rank, world, local_rank):
@@ -682,26 +835,20 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak_gbs()
     peak_kind = "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"
     extra = {}
+    config = workload_config(args.workload, args.seed + (0 if args.workload in BATCHED_WORKLOADS else rank))
     if args.workload in BATCHED_WORKLOADS:
         r = bench_batched(args, torch, world)
-        if args.workload == "large-scene":
-            desc = ("large scene: 1,048,576 WCSPH particles (128x64x128 at 0.005 m, h=0.01 m, [0,1]^3, dt=2e-5 s, "
-                    "stiffness 0.375, viscosity 0.025) with a rigid ball of radius 0.05 m (4,169 particles, "
-                    "body_dynamic 2) dropped into them, plus a 32^3 SVK cube (E=5e4 Pa, nu=0.35) as a second "
-                    "scene; one CUDA graph per substep")
-        else:
-            desc = ("256 independent scenes, 60% WCSPH / 25% corotational / 15% SVK, particle counts log-uniform "
-                    "in [1,000, 65,536], E log-uniform [1e4, 1e6] Pa (SVK [1e4, 1e5]: the reference's SVK "
-                    "diverges within 2,000 substeps above), Poisson uniform [0.25, 0.45], 0.01 m spacing, "
-                    "h=0.02 m, seeded jitter; one CUDA graph per substep over all scenes")
         t = r.get("tuned")
-        path = ("batched form (sph_batch_step); launch shape chosen by sph.autotune: block %d, pair block %d, "
-                "grid cap %d" % (t["block"], t["pair_block"], t["grid_cap"]) if t else
-                "batched form (sph_batch_step), launch shape: block 256, pair block 128, no grid cap")
+        extra["path"] = ("batched form (sph_batch_step), one CUDA graph per substep over all scenes; launch shape "
+                         "chosen by sph.autotune: block %d, pair block %d, grid cap %d"
+                         % (t["block"], t["pair_block"], t["grid_cap"]) if t else
+                         "batched form (sph_batch_step), one CUDA graph per substep over all scenes; launch "
+                         "shape: block 256, pair block 128, no grid cap")
         if t:
             extra["autotune"] = t
-        l2 = "working set %.2f GB > L2 (129 MB); no flush needed" % (r["n"] * 300e-9)
-        if rank == 0 and not args.quick and args.workload == "batched-256":
+        if r.get("late"):
+            extra["late_state"] = r["late"]
+        if rank == 0 and not args.quick:
             pl = bench_plain_loop(r["scenes"], max(3, args.steps // 2))
             batched = r["n"] * args.steps / r["total_s"]
             extra["plain_per_scene"] = {
@@ -711,21 +858,19 @@ def run_ours(args, rank, world, local_rank):
                        "synced_value = one substep per call, waiting for each (the reference's blocking calls)"}
             extra["batched_vs_plain"] = batched / pl["graph"]
             extra["batched_vs_plain_synced"] = batched / pl["synced"]
+            extra["exact_mix"] = exact_mix(args, torch)
             extra["fp64_error"] = fp64_error_sample(r["scenes"], 100)
             extra["fp64_error_configs"] = fp64_error_configs()
             extra["served"] = bench_served(args)
-            sc1m, d1m = workload("wcsph-1m", args.seed)
-            p1 = bench_plain(args, sc1m, torch, 1)
-            extra["plain_1m"] = {"workload": "wcsph-1m: " + d1m, "value": p1["n"] * args.steps / p1["total_s"],
-                                 "ms_per_step": p1["total_s"] * 1e3 / args.steps,
-                                 "roofline": _phase_roofline(p1["phases"], p1["n"], p1["cells"], peak, peak_kind,
-                                                             workload="wcsph-1m", clocks=p1["clocks"]),
-                                 "e2e": p1["e2e"]}
+            extra["plain_1m"] = _plain_extra(args, "wcsph-1m", torch, peak, peak_kind)
+            extra["large_scene"] = _plain_extra(args, "large-scene", torch, peak, peak_kind)
+            extra["fp64_error_1m"] = fp64_error_1m(args.seed)
     else:
-        scene, desc = workload(args.workload, args.seed + rank)
+        scene, _ = workload(args.workload, args.seed + rank)
         r = bench_plain(args, scene, torch, world)
-        path = "plain single scene, one CUDA-graph substep per step (sph_update)"
-        l2 = "flushed between timed steps (256 MB write, outside the timed events)"
+        extra["path"] = "plain single scene, one CUDA-graph substep per step (sph_update)"
+    extra["cells"] = r["cells"]
+    extra["parallelism"] = "replicas (no collective)" if world > 1 else "single GPU"
     if "pairs" in r and r["phases"]:
         ph = r["phases"]
         step_s = r["total_s"] / args.steps
@@ -756,8 +901,7 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice scenes, seed %d)" % args.seed,
-        "config": {"workload": args.workload + ": " + desc, "particles": n, "cells": r["cells"], "path": path,
-                   "l2": l2, "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": config,
         "clocks": r["clocks"],
         "e2e": r["e2e"],
         "gpu_launches": r["kernels_per_step"] * args.steps,
@@ -769,19 +913,24 @@ def run_ours(args, rank, world, local_rank):
 
 
 def run_reference(args, rank, world):
+    """The reference's own kernels (kernels/*.cl compiled for the host CPU
+    into oracle/_ref, run by OpenMP over all host cores) in stores its own
+    builder made, on the same workload: `steps` substeps of every scene.
+    Neither the sph package nor the CUDA library is loaded."""
     if rank != 0:
         return None
-    scs = cpu_workload(args.workload, args.seed)
+    scs = cpu_workload(args.workload, args.seed, standalone=True)
     nthreads = os.cpu_count() or 1
     work = 0
     el = 0.0
-    kind = "port"
-    for s in scs:
-        w, e, kind = cpu_sample(s, s.material, args.steps, nthreads, reference=True)
+    kinds = set()
+    for x in scs:
+        w, e, kind = cpu_sample(x, x.material, args.steps, nthreads, reference=True)
         work += w
         el += e
+        kinds.add(kind)
     value = work / el
-    desc = args.workload
+    kind = "reference" if kinds == {"reference"} else "port"
     return {
         "impl": "reference",
         "metric": METRIC,
@@ -796,9 +945,10 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice scenes, seed %d)" % args.seed,
-        "config": {"workload": desc, "particles": sum(s.n for s in scs), "scenes": len(scs)},
+        "config": workload_config(args.workload, args.seed, standalone=True),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": kind,
-                         "sample": "%d full substeps of every scene of the workload" % args.steps},
+                         "sample": "%d full substeps of every scene of the workload (the reference's kernels in "
+                                   "stores its own builder made)" % args.steps},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -814,8 +964,10 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-steps", type=int, default=3, help="substeps in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--quick", action="store_true", help="skip the plain loop, served, FP64 and 1M extras")
-    ap.add_argument("--served-seconds", type=float, default=8.0, help="arrival window of the served stream")
+    ap.add_argument("--quick", action="store_true",
+                    help="skip the late-state, plain loop, exact mix, served, FP64, 1M and large-scene extras")
+    ap.add_argument("--served-seconds", type=float, default=60.0, help="arrival window of the served stream")
+    ap.add_argument("--served-chunk", type=int, default=25, help="substeps per serving chunk")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
