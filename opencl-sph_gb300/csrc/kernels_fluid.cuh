@@ -37,98 +37,8 @@
 // lattice); 256 measured the same and took twice the shared memory.
 #define SPH_STAGE 128
 
-// Row staging by the bulk-copy engine (TMA, cp.async.bulk): each warp owns
-// two staging buffers of SPH_STAGE float4 and one mbarrier per buffer.  The
-// copy of row r + 1 is issued (by lane 0: expect_tx on the buffer's
-// mbarrier, then the bulk copy, which completes the transaction) before
-// row r is tested, so the copy runs under the tests; the warp then waits on
-// row r + 1's barrier phase.  A row union is a contiguous range of the
-// 16-byte aligned float4 copy, so the copy's addresses and size are
-// multiples of 16 bytes.  Every wait is bounded: a wait that runs out
-// (which a correct copy never does) sets STATUS_STAGING_TIMEOUT, and the
-// warp reads global memory for the rest of the launch, draining its
-// outstanding copies (bounded again) before it exits.
 __host__ __device__ constexpr size_t density_smem_bytes(unsigned block) {
-    return (2 * sizeof(float4) * SPH_STAGE + 16) * (block / 32);
-}
-
-#define SPH_MBAR_SPINS (1u << 20)
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-struct RowStage {
-    float4 *buf;        // two buffers of SPH_STAGE float4
-    uint32_t sbuf;      // shared address of buffer 0
-    uint32_t bar;       // shared address of buffer 0's mbarrier (buffer 1's at +8)
-    // bit t: parity of buffer t's next phase; bit 2 + t: a copy into buffer
-    // t is outstanding; bit 4: a wait ran out (no more bulk copies)
-    uint32_t flags;
-};
-
-__device__ __forceinline__ void stage_init(RowStage &R, float4 *warp_smem, unsigned lane) {
-    R.buf = warp_smem;
-    R.sbuf = smem_u32(warp_smem);
-    R.bar = smem_u32(warp_smem + 2 * SPH_STAGE);
-    R.flags = 0;
-    if (lane == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(R.bar) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(R.bar + 8) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncwarp();
-}
-
-// Lane 0 copies spos[ub, ue) into buffer t; the other lanes record it.
-__device__ __forceinline__ void stage_issue(RowStage &R, int t, const float4 *src, unsigned count, unsigned lane) {
-    const uint32_t bytes = count * (uint32_t)sizeof(float4);
-    const uint32_t bar = R.bar + 8u * t;
-    if (lane == 0) {
-        // the warp's generic reads of the buffer (ordered by the __syncwarp
-        // that ended its last row) come before the async proxy's writes
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         R.sbuf + (uint32_t)(t * SPH_STAGE * sizeof(float4))),
-                     "l"(src), "r"(bytes), "r"(bar)
-                     : "memory");
-    }
-    R.flags |= 4u << t;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (uint32_t it = 0; it < SPH_MBAR_SPINS; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// Waits (warp-wide, bounded) for buffer t's copy; false: the warp reads
-// global memory from now on.
-__device__ __forceinline__ bool stage_wait(RowStage &R, int t, unsigned *status, unsigned lane) {
-    const bool ok = __all_sync(SPH_FULL_MASK, mbar_wait_bounded(R.bar + 8u * t, (R.flags >> t) & 1u));
-    if (ok) {
-        R.flags ^= 1u << t;
-        R.flags &= ~(4u << t);
-    } else {
-        R.flags |= 16u;
-        if (lane == 0) atomicOr(status, (unsigned)STATUS_STAGING_TIMEOUT);
-    }
-    return ok;
-}
-
-// Before the warp exits: a copy left outstanding by a wait that ran out is
-// waited for once more (bounded), so that no copy lands after the launch.
-__device__ __forceinline__ void stage_drain(RowStage &R) {
-    for (int t = 0; t < 2; ++t)
-        if (R.flags & (4u << t)) (void)mbar_wait_bounded(R.bar + 8u * t, (R.flags >> t) & 1u);
+    return sizeof(float4) * SPH_STAGE * (block / 32);
 }
 
 // p = (rho - rho0) stiffness (fluids.cl:33-36), rounded as written.
@@ -138,7 +48,7 @@ __device__ __forceinline__ float fluid_pressure(float rho, float rho0, float sti
 
 template <bool PLANES, bool MASK>
 __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsigned item, unsigned lane,
-                                            RowStage &R, int original) {
+                                            float4 *__restrict__ wstage, int original) {
     const bool active = item < n;
     const unsigned k = item;
     const unsigned i = active ? min(S.cellparticles[k], S.pnum - 1) : 0u;
@@ -156,30 +66,18 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
     bool overflow = false;
     const StencilRows rows(S, active ? S.gridcell[i] : 0u);
     const float4 *__restrict__ spos = S.spos;
-    // row r's bounds for this lane and the warp's union of them; the union
-    // is staged when it fits a buffer
-    auto row_union = [&](int r, unsigned &b, unsigned &e, unsigned &ub, unsigned &ue) -> bool {
-        b = e = 0;
-        if (active) rows.row(S, r, &b, &e);
-        ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
-        ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
-        return ub < ue && ue - ub <= SPH_STAGE && !(R.flags & 16u);
-    };
-    unsigned b, e, ub, ue;
-    bool staged = row_union(0, b, e, ub, ue);
-    if (staged) stage_issue(R, 0, spos + ub, ue - ub, lane);
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
-        const int cur = r & 1;
-        // the next row's copy runs while this row is tested
-        unsigned nb = 0, ne = 0, nub = 0, nue = 0;
-        bool nstaged = false;
-        if (r < 8) {
-            nstaged = row_union(r + 1, nb, ne, nub, nue);
-            if (nstaged) stage_issue(R, cur ^ 1, spos + nub, nue - nub, lane);
+        unsigned b = 0, e = 0;
+        if (active) rows.row(S, r, &b, &e);
+        const unsigned ub = __reduce_min_sync(SPH_FULL_MASK, b < e ? b : 0xffffffffu);
+        const unsigned ue = __reduce_max_sync(SPH_FULL_MASK, b < e ? e : 0u);
+        const bool staged = ub < ue && ue - ub <= SPH_STAGE;
+        if (staged) {
+            __syncwarp();
+            for (unsigned t = lane; t < ue - ub; t += 32) wstage[t] = spos[ub + t];
+            __syncwarp();
         }
-        if (staged) staged = stage_wait(R, cur, S.status, lane);
-        const float4 *wstage = R.buf + cur * SPH_STAGE;
         const unsigned len = e - b;
         // the row's mask in two words, each filled by its own loop below
         // (a 32-bit shift per neighbour, no test of the candidate's place)
@@ -231,13 +129,6 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             overflow |= len > 64;
             total += len;
         }
-        // every lane is done with this row's buffer before it is refilled
-        __syncwarp();
-        b = nb;
-        e = ne;
-        ub = nub;
-        ue = nue;
-        staged = nstaged && !(R.flags & 16u);
     }
     if (active) {
         const float value = poly6_density(rho.s, h2, h, *S.mass);
@@ -273,21 +164,18 @@ template <bool PLANES>
 __global__ void __launch_bounds__(512, 2)
     k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask, int skip_solids) {
     extern __shared__ float4 sm_stage[];
+    float4 *wstage = sm_stage + (threadIdx.x >> 5) * SPH_STAGE;
     const unsigned lane = threadIdx.x & 31u;
-    // per warp: two staging buffers, then the two mbarriers
-    RowStage R;
-    stage_init(R, sm_stage + (threadIdx.x >> 5) * (2 * SPH_STAGE + 1), lane);
     SPH_FOR_WORK(map)
     if ((S.num_symmetry_planes != 0) != PLANES) continue;
     // in a fused substep a plane-free solid's first solid pass sums its density
     if (skip_solids && !PLANES && (S.programs & (PROG_COROT | PROG_SVK))) continue;
     const unsigned n = active_count(S);
     if (want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original)
-        density_one<PLANES, true>(S, n, item, lane, R, original);
+        density_one<PLANES, true>(S, n, item, lane, wstage, original);
     else
-        density_one<PLANES, false>(S, n, item, lane, R, original);
+        density_one<PLANES, false>(S, n, item, lane, wstage, original);
     SPH_END_WORK
-    stage_drain(R);
 }
 
 // APPLY_CUBE_BOUNDS(ipos, f, -2.0, 2.0) (common.cl:37-43): a repulsive

@@ -31,8 +31,6 @@ enum SphProgram : unsigned {
 enum SphStatus : unsigned {
     STATUS_NONFINITE = 1u << 0,       // a non-finite position was written
     STATUS_OUTSIDE_GRID = 1u << 1,    // a particle was binned outside gridbounds
-    STATUS_STAGING_TIMEOUT = 1u << 2, // a bulk copy into shared memory did not complete within its wait
-                                      // (the pass read global memory instead)
 };
 
 // Cells with more particles than this are ordered by the block-wide
