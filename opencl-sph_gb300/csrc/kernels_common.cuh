@@ -112,6 +112,24 @@ struct Kahan3 {
     __device__ __forceinline__ void add(float3 v) { x.add(v.x); y.add(v.y); z.add(v.z); }
     __device__ __forceinline__ float3 get() const { return make_float3(x.s, y.s, z.s); }
 };
+// Blocked compensated sum of float3 terms: the terms of one stencil row are
+// added in order into a row sum (rounded adds, no compensation), and each
+// row's sum into the total with Kahan compensation.  end_row() closes a row;
+// every walk over a particle's stencil calls it once for each of the nine
+// rows, empty or outside the grid, so that two walks over the same
+// neighbours in the same order give the same bits.
+struct BlockSum3 {
+    float3 row = make_float3(0.f, 0.f, 0.f);
+    Kahan3 total;
+    __device__ __forceinline__ void add(float3 v) {
+        row = make_float3(__fadd_rn(row.x, v.x), __fadd_rn(row.y, v.y), __fadd_rn(row.z, v.z));
+    }
+    __device__ __forceinline__ void end_row() {
+        total.add(row);
+        row = make_float3(0.f, 0.f, 0.f);
+    }
+    __device__ __forceinline__ float3 get() const { return total.get(); }
+};
 
 __device__ __forceinline__ float3 ld3(const float *p, size_t i) {
     return make_float3(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
@@ -135,8 +153,10 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) { return make_flo
 // of one (z, y) row are consecutive in the sort, each row is one contiguous
 // range [celloffset[first], celloffset[last] + gridcount[last]).  `f(kk)` is
 // called for every sorted neighbour index kk in the reference's order.
-template <class F>
-__device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned cell, F &&f) {
+// `row_end()` is called after each of the nine rows (dz outer, dy inner),
+// including rows outside the grid.
+template <class F, class G>
+__device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned cell, F &&f, G &&row_end) {
     const unsigned R0 = S.gridres[0], R1 = S.gridres[1], R2 = S.gridres[2];
     const unsigned layer = R0 * R1;
     const unsigned cz = cell / layer;
@@ -149,17 +169,22 @@ __device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned 
     const unsigned *__restrict__ cnt = S.gridcount;
     for (int dz = -1; dz <= 1; ++dz) {
         int z = (int)cz + dz;
-        if (z < 0 || z >= (int)R2) continue;
         for (int dy = -1; dy <= 1; ++dy) {
             int y = (int)cy + dy;
-            if (y < 0 || y >= (int)R1) continue;
-            unsigned row = (unsigned)z * layer + (unsigned)y * R0;
-            unsigned b = __ldg(off + row + x0);
-            unsigned e = __ldg(off + row + x1) + __ldg(cnt + row + x1);
-            if (e > S.pnum) e = S.pnum;  // only reachable with inconsistent host-written tables
-            for (unsigned kk = b; kk < e; ++kk) f(kk);
+            if (z >= 0 && z < (int)R2 && y >= 0 && y < (int)R1) {
+                unsigned row = (unsigned)z * layer + (unsigned)y * R0;
+                unsigned b = __ldg(off + row + x0);
+                unsigned e = __ldg(off + row + x1) + __ldg(cnt + row + x1);
+                if (e > S.pnum) e = S.pnum;  // only reachable with inconsistent host-written tables
+                for (unsigned kk = b; kk < e; ++kk) f(kk);
+            }
+            row_end();
         }
     }
+}
+template <class F>
+__device__ __forceinline__ void for_each_neighbour(const SceneDesc &S, unsigned cell, F &&f) {
+    for_each_neighbour(S, cell, f, [] {});
 }
 
 // Row r of particle k's stencil (dz outer, dy inner, as the reference's
@@ -237,8 +262,9 @@ __device__ __forceinline__ unsigned long long load_row_mask(const SceneDesc &S, 
 // PREFETCH: the next row's bounds and low mask word are loaded while a row
 // is walked (it pays in the corotational pass 2; the solid force passes,
 // at their register cap, run slower with it).
-template <bool PREFETCH = false, class F>
-__device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {
+template <bool PREFETCH = false, class F, class G>
+__device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f,
+                                                G &&row_end) {
     unsigned nb = 0, ne = 0, nlo = 0;
     if (PREFETCH) {
         rows.row(S, 0, &nb, &ne);
@@ -276,7 +302,12 @@ __device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, 
                 f(b + t);
             }
         }
+        row_end();
     }
+}
+template <bool PREFETCH = false, class F>
+__device__ __forceinline__ void for_each_masked(const SceneDesc &S, unsigned k, const StencilRows &rows, F &&f) {
+    for_each_masked<PREFETCH>(S, k, rows, f, [] {});
 }
 
 // ---- symmetry planes (the SYMMETRY blocks, e.g. common.cl:647-686) ----------

@@ -24,6 +24,9 @@
 // one cell read the same address: a broadcast).  Values, order and
 // arithmetic are those of a direct walk; a union wider than the buffer (a
 // warp that spans two grid rows) is read from global memory instead.
+// The sum is blocked: each stencil row's terms are added in candidate
+// order, and the nine row sums with Kahan compensation (one compensated
+// add per row instead of per neighbour).
 //
 // With `want_mask` (fused fluid substeps, where positions cannot change
 // before the force pass) each fluid particle also records, per row, which
@@ -82,11 +85,14 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         // the row's mask in two words, each filled by its own loop below
         // (a 32-bit shift per neighbour, no test of the candidate's place)
         unsigned lo = 0, hi = 0;
+        // the row's density terms in candidate order; the row sums are
+        // added with Kahan compensation (blocked summation)
+        float rowsum = 0.f;
         auto visit = [&](float3 jpos, unsigned *word, unsigned bit) {
             const float r2 = norm2(sub3(jpos, ipos));
             if (r2 <= B.le) {
                 const float d = fmaxf(h2 - r2, 0.f);
-                rho.add(d * d * d);
+                rowsum = __fadd_rn(rowsum, d * d * d);
                 // a fused plane-free substep counts in the force pass
                 if (!MASK || PLANES) count += r2 <= B.lt;
                 if (MASK && word) *word |= 1u << bit;
@@ -102,7 +108,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
                     const float m2 = norm2(sub3(ref, ipos));
                     if (m2 <= B.lt) {
                         const float d = fmaxf(h2 - m2, 0.f);
-                        rho.add(d * d * d);
+                        rowsum = __fadd_rn(rowsum, d * d * d);
                         ++count;
                     }
                 }
@@ -123,6 +129,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             for (unsigned t = n1; t < n2; ++t) visit(xyz(spos[b + t]), &hi, t - 32u);
             for (unsigned t = n2; t < len; ++t) visit(xyz(spos[b + t]), nullptr, 0u);
         }
+        rho.add(rowsum);
         if (MASK && active) {
             const unsigned long long bits = ((unsigned long long)hi << 32) | lo;
             store_row_mask(S, k, r, len, bits);
@@ -232,7 +239,7 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
 // the same positions and arithmetic, so that test is not repeated.
 template <bool IN_RANGE = false>
 __device__ __forceinline__ float fluid_pair_p(const FluidI &I, float pi, float3 jpos, float3 jvel, float pj,
-                                              float inv_rhoj, Kahan3 &f) {
+                                              float inv_rhoj, BlockSum3 &f) {
     const float3 d = sub3(jpos, I.ipos);
     const float r2 = norm2(d);
     if ((!IN_RANGE && !(r2 <= I.B.le)) || r2 == 0.f) return r2;
@@ -251,14 +258,14 @@ __device__ __forceinline__ float fluid_pair_p(const FluidI &I, float pi, float3 
 
 template <bool IN_RANGE = false>
 __device__ __forceinline__ float fluid_pair(const FluidI &I, float3 jpos, float3 jvel, float pj, float inv_rhoj,
-                                            Kahan3 &f) {
+                                            BlockSum3 &f) {
     return fluid_pair_p<IN_RANGE>(I, I.pi, jpos, jvel, pj, inv_rhoj, f);
 }
 
 // The end of a fluid particle's force pass: mass, cube band, store, step.
 // `extra`: force already on the particle (a mixed scene's solid particle
 // carries its elastic force, which the fluid pair terms add to).
-__device__ __forceinline__ void fluid_finish(const SceneDesc &S, unsigned i, const FluidI &I, const Kahan3 &f,
+__device__ __forceinline__ void fluid_finish(const SceneDesc &S, unsigned i, const FluidI &I, const BlockSum3 &f,
                                              int fuse_step, float3 extra = make_float3(0.f, 0.f, 0.f)) {
     const float m = *S.mass;
     float3 fi = f.get() * m;
@@ -287,7 +294,7 @@ __device__ __forceinline__ float3 mixed_extra(const SceneDesc &S, unsigned i, bo
 // w) and velocity (reciprocal density in w, negated for a mixed scene's
 // solid particle); adds to the neighbour count.
 template <bool MIXED>
-__device__ __forceinline__ void walk_pair(const FluidI &I, bool solid_i, float4 p, float4 v, Kahan3 &f,
+__device__ __forceinline__ void walk_pair(const FluidI &I, bool solid_i, float4 p, float4 v, BlockSum3 &f,
                                           unsigned &count) {
     if (MIXED) {
         const bool solid_j = v.w < 0.f;
@@ -307,7 +314,7 @@ __device__ __forceinline__ void walk_pair(const FluidI &I, bool solid_i, float4 
 // The stencil scan: every candidate of the 27 cells, in the reference's
 // order; returns the count of candidates closer than h (j = i included).
 template <bool MIXED>
-__device__ __forceinline__ unsigned fluid_scan(const SceneDesc &S, unsigned cell, const FluidI &I, Kahan3 &f,
+__device__ __forceinline__ unsigned fluid_scan(const SceneDesc &S, unsigned cell, const FluidI &I, BlockSum3 &f,
                                                bool solid_i) {
     const float4 *__restrict__ spos = S.spos;
     const float4 *__restrict__ svel = S.svel;
@@ -326,7 +333,7 @@ __device__ __forceinline__ unsigned fluid_scan(const SceneDesc &S, unsigned cell
             pj = fmaxf(pj, 0.f);
         }
         count += fluid_pair_p(I, pi, xyz(spos[kk]), xyz(svel[kk]), pj, rcp_approx(rho), f) <= I.B.lt;
-    });
+    }, [&] { f.end_row(); });
     return count;
 }
 
@@ -340,7 +347,7 @@ __global__ void k_forces_fluids(const SceneDesc *__restrict__ scenes, BlockMap m
         const unsigned i = min(S.cellparticles[k], S.pnum - 1);
         const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(S.svel[k]), S.sdens[k]);
         const bool solid_i = mixed_solid<MIXED>(S, i);
-        Kahan3 f;
+        BlockSum3 f;
         fluid_scan<MIXED>(S, S.gridcell[i], I, f, solid_i);
         fluid_finish(S, i, I, f, fuse_step, mixed_extra<MIXED>(S, i, solid_i));
     }
@@ -367,7 +374,7 @@ __global__ void __maxnreg__(64) k_forces_fluids_masked(const SceneDesc *__restri
         const FluidI I = fluid_i(S, xyz(S.spos[k]), xyz(S.svel[k]), S.sdens[k]);
         const unsigned cell = S.gridcell[i];
         const bool solid_i = mixed_solid<MIXED>(S, i);
-        Kahan3 f;
+        BlockSum3 f;
         unsigned count = 0;  // num_neighbours, which the density pass left to this one
         if (S.ncand[k] != SPH_NCAND_SCAN) {
             count = 1;  // k itself (r^2 = 0), whose mask bit the walk clears
@@ -417,6 +424,7 @@ __global__ void __maxnreg__(64) k_forces_fluids_masked(const SceneDesc *__restri
                         }
                     }
                 }
+                f.end_row();
             }
         } else {
             count = fluid_scan<MIXED>(S, cell, I, f, solid_i);

@@ -611,7 +611,8 @@ __global__ void k_forces_solids_planes(const SceneDesc *__restrict__ scenes, Blo
 // mask bits (|p| <= h or |q| <= h, k itself excluded) and the bits of the
 // chunk's current neighbours (|p| <= h, k itself included).  Then a walk
 // over those neighbours, in candidate order, adds each one's density term
-// (the density pass's sum, in its order) and for j != i runs sum(p, q, w),
+// (the density pass's blocked sum, in its order: row sums in candidate
+// order, Kahan-added row by row) and for j != i runs sum(p, q, w),
 // w = (h^2 - |p|^2)^3.  The scan loop thus stays free of the sums' work,
 // which otherwise every lane would issue whenever any lane of its warp met
 // a neighbour, and every sum sees the neighbours in the order a plain scan
@@ -633,6 +634,7 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
         unsigned b, e;
         rows.row(S, r, &b, &e);
         const unsigned len = e - b;
+        float rowsum = 0.f;  // the row's density terms, as the density pass sums them
 #pragma unroll 1
         for (unsigned c0 = 0; c0 < len; c0 += 32) {
             const unsigned cb = b + c0, cn = min(len - c0, 32u);
@@ -656,11 +658,12 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
                 const float r2 = norm2(p);
                 const float d = fmaxf(C.h2 - r2, 0.f);
                 const float w = d * d * d;
-                rho.add(w);
+                rowsum = __fadd_rn(rowsum, w);
                 count += r2 <= C.lt;
                 if (kk != k) sum(p, sub3(xyz(spos0[kk]), ipos0), w);
             }
         }
+        rho.add(rowsum);
         overflow |= len > 64;
         total += len;
     }
