@@ -94,16 +94,17 @@ PHASE_BYTES = {
 # (one launch after two warm-up substeps, `bench.py --quick --steps 2
 # --warmup 3` of the same workload), taken with the register caps and
 # kernels of this source: k_rotations_and_strains at 72 registers, the
-# solid force passes at 80, the fluid force pass at 64.
+# solid force passes at 80, the fluid force pass at 64; the density and
+# fluid force passes with their sums blocked per cell row.
 MEASURED_TRAFFIC = {
-    ("wcsph-1m", "density"): 44.99e6,                           # k_density<false>
-    ("wcsph-1m", "forces_fluids+step"): 116.57e6,               # k_forces_fluids_masked<false>
-    ("batched-256", "density"): 263.80e6,                       # k_density<false> (masks, pressure, 1/density too)
-    ("batched-256", "fluid forces+step"): 365.43e6,             # k_forces_fluids_masked<false>
-    ("batched-256", "corotational rotations"): 255.75e6,        # k_rotations_and_strains (with the stress law)
-    ("batched-256", "corotational forces+step"): 241.96e6,      # k_forces_solids<1, 1> (with the step)
-    ("batched-256", "svk deformations"): 105.68e6,              # k_deformations (with the stress law)
-    ("batched-256", "svk forces+step"): 161.81e6,               # k_forces_solids<0, 1> (with the step)
+    ("wcsph-1m", "density"): 44.84e6,                           # k_density<false>
+    ("wcsph-1m", "forces_fluids+step"): 116.79e6,               # k_forces_fluids_masked<false>
+    ("batched-256", "density"): 262.96e6,                       # k_density<false> (masks, pressure, 1/density too)
+    ("batched-256", "fluid forces+step"): 365.68e6,             # k_forces_fluids_masked<false>
+    ("batched-256", "corotational rotations"): 255.51e6,        # k_rotations_and_strains (with the stress law)
+    ("batched-256", "corotational forces+step"): 241.63e6,      # k_forces_solids<1, 1> (with the step)
+    ("batched-256", "svk deformations"): 105.74e6,              # k_deformations (with the stress law)
+    ("batched-256", "svk forces+step"): 161.73e6,               # k_forces_solids<0, 1> (with the step)
 }
 
 # Warp instructions per launch of the same kernels (ncu
@@ -111,13 +112,13 @@ MEASURED_TRAFFIC = {
 # live phase time they give the issue rate, against 4 warp instructions per
 # SM per clock.
 MEASURED_INST = {
-    ("wcsph-1m", "density"): 183.51e6,
-    ("wcsph-1m", "forces_fluids+step"): 173.29e6,
-    ("batched-256", "density"): 472.37e6,
-    ("batched-256", "fluid forces+step"): 444.68e6,
-    ("batched-256", "corotational rotations"): 486.72e6,
+    ("wcsph-1m", "density"): 183.40e6,
+    ("wcsph-1m", "forces_fluids+step"): 156.37e6,
+    ("batched-256", "density"): 465.40e6,
+    ("batched-256", "fluid forces+step"): 402.00e6,
+    ("batched-256", "corotational rotations"): 479.59e6,
     ("batched-256", "corotational forces+step"): 260.60e6,
-    ("batched-256", "svk deformations"): 384.30e6,
+    ("batched-256", "svk deformations"): 378.54e6,
     ("batched-256", "svk forces+step"): 259.39e6,
 }
 
