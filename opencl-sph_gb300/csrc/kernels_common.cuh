@@ -52,6 +52,26 @@ __device__ __forceinline__ float3 sub3(float3 a, float3 b) {
 __device__ __forceinline__ float norm2(float3 d) {
     return __fadd_rn(__fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y)), __fmul_rn(d.z, d.z));
 }
+// norm2(sub3(a, b)) with the x and y lanes in packed FP32x2 instructions
+// (sm_100 and later; each lane rounds as the scalar instruction does, and
+// a + (-b) is a - b exactly): the same value in 6 instructions instead of
+// 8.  `b` is passed as its negated x, y pair and its z.
+struct NegPoint {
+    float2 nxy;
+    float z;
+};
+__device__ __forceinline__ NegPoint neg_point(float3 b) {
+    NegPoint o;
+    o.nxy = make_float2(-b.x, -b.y);
+    o.z = b.z;
+    return o;
+}
+__device__ __forceinline__ float dist2(float4 a, const NegPoint &b) {
+    const float2 dxy = __fadd2_rn(make_float2(a.x, a.y), b.nxy);
+    const float dz = __fsub_rn(a.z, b.z);
+    const float2 sq = __fmul2_rn(dxy, dxy);
+    return __fadd_rn(__fadd_rn(sq.x, sq.y), __fmul_rn(dz, dz));
+}
 __device__ __forceinline__ float dot3(float3 a, float3 b) {
     return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 }

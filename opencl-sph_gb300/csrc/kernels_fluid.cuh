@@ -59,6 +59,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
     const DistBounds B = dist_bounds(h);
     const float h2 = __fmul_rn(h, h);
     const float3 ipos = active ? xyz(S.spos[k]) : make_float3(0.f, 0.f, 0.f);
+    const NegPoint nip = neg_point(ipos);
     Planes P;
     if (PLANES) {
         load_planes(S, ipos, h, P);
@@ -88,8 +89,8 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         // the row's density terms in candidate order; the row sums are
         // added with Kahan compensation (blocked summation)
         float rowsum = 0.f;
-        auto visit = [&](float3 jpos, unsigned *word, unsigned bit) {
-            const float r2 = norm2(sub3(jpos, ipos));
+        auto visit = [&](float4 j4, unsigned *word, unsigned bit) {
+            const float r2 = dist2(j4, nip);
             if (r2 <= B.le) {
                 const float d = fmaxf(h2 - r2, 0.f);
                 rowsum = __fadd_rn(rowsum, d * d * d);
@@ -98,6 +99,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
                 if (MASK && word) *word |= 1u << bit;
             }
             if (PLANES && P.imask) {
+                const float3 jpos = xyz(j4);
                 const unsigned jm = plane_jmask(P, jpos, h);
                 // subsets of jm in increasing order: the reference's
                 // plane_bits order restricted to the subsets it keeps
@@ -120,14 +122,14 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
         if (staged) {
             const float4 *src = wstage + (b - ub);
 #pragma unroll 4
-            for (unsigned t = 0; t < n1; ++t) visit(xyz(src[t]), &lo, t);
+            for (unsigned t = 0; t < n1; ++t) visit(src[t], &lo, t);
 #pragma unroll 4
-            for (unsigned t = n1; t < n2; ++t) visit(xyz(src[t]), &hi, t - 32u);
-            for (unsigned t = n2; t < len; ++t) visit(xyz(src[t]), nullptr, 0u);
+            for (unsigned t = n1; t < n2; ++t) visit(src[t], &hi, t - 32u);
+            for (unsigned t = n2; t < len; ++t) visit(src[t], nullptr, 0u);
         } else {
-            for (unsigned t = 0; t < n1; ++t) visit(xyz(spos[b + t]), &lo, t);
-            for (unsigned t = n1; t < n2; ++t) visit(xyz(spos[b + t]), &hi, t - 32u);
-            for (unsigned t = n2; t < len; ++t) visit(xyz(spos[b + t]), nullptr, 0u);
+            for (unsigned t = 0; t < n1; ++t) visit(spos[b + t], &lo, t);
+            for (unsigned t = n1; t < n2; ++t) visit(spos[b + t], &hi, t - 32u);
+            for (unsigned t = n2; t < len; ++t) visit(spos[b + t], nullptr, 0u);
         }
         rho.add(rowsum);
         if (MASK && active) {

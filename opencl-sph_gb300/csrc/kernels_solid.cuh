@@ -629,6 +629,7 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
                                                 unsigned &count, unsigned &total, bool &overflow, Sum &&sum) {
     const float4 *__restrict__ spos = S.spos;
     const float4 *__restrict__ spos0 = S.spos0;
+    const NegPoint nip = neg_point(ipos), nip0 = neg_point(ipos0);
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         unsigned b, e;
@@ -642,8 +643,8 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
 #pragma unroll 4
             for (unsigned t = 0; t < cn; ++t) {
                 const unsigned kk = cb + t;
-                const float r2 = norm2(sub3(xyz(spos[kk]), ipos));
-                const float q2 = norm2(sub3(xyz(spos0[kk]), ipos0));
+                const float r2 = dist2(spos[kk], nip);
+                const float q2 = dist2(spos0[kk], nip0);
                 const unsigned bit = 1u << t;
                 if (r2 <= C.le) near |= bit;
                 if (r2 <= C.le || q2 <= C.le) bits |= bit;
@@ -755,8 +756,9 @@ __global__ void __maxnreg__(72) k_rotations_and_strains(const SceneDesc *__restr
 }
 
 // compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
-// the sorted copies, recording the candidate masks.
-__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density,
+// the sorted copies, recording the candidate masks.  At most 64 registers
+// (80 unbounded, no spills at 64): eight 128-thread blocks per SM.
+__global__ void __maxnreg__(64) k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density,
                                int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
