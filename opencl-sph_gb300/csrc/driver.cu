@@ -279,6 +279,7 @@ Store *create_store(psdata *data, const char *file_list, std::string *err) {
     L.stream = s->stream;
     L.no_symmetry_planes = s->desc.num_symmetry_planes == 0;
     L.has_mixed = s->desc.phase != nullptr;
+    L.all_mixed = L.has_mixed;  // one scene per store
     L.rigid = s->d_rigid;
     L.num_rigid = 0;
     if (!refresh_rigid(s, *data)) {
@@ -358,12 +359,12 @@ bool dispatch(Store *s, const char *name) {
         return true;
     }
     if (mixed && k == "compute_deformations") {
-        sph_launch_gather(L, false, false);
+        sph_launch_gather(L, false, false, true);
         sph_launch_deformations_mixed(L);
         return true;
     }
     if (mixed && k == "compute_forces_solids") {
-        sph_launch_gather(L, false, false);
+        sph_launch_gather(L, false, false, true);
         sph_launch_forces_solids_mixed(L);
         return true;
     }

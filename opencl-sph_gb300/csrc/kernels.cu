@@ -104,11 +104,12 @@ void sph_launch_forces_fluids(const Launch &L, bool fuse_step, bool masked) {
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
     const int step = fuse_step ? 1 : 0;
     if (masked) {
-        k_forces_fluids_masked<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        if (!L.all_mixed)
+            k_forces_fluids_masked<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
         if (L.has_mixed)
             k_forces_fluids_masked<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
     } else {
-        k_forces_fluids<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
+        if (!L.all_mixed) k_forces_fluids<false><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
         if (L.has_mixed) k_forces_fluids<true><<<g, L.pair_block, 0, L.stream>>>(L.scenes, L.pair_particles, step);
     }
 }
@@ -252,7 +253,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
         // recipe, with the solids' elastic passes before the force pass,
         // which adds the fluid-solid pair terms and steps every particle
         phase("gather");
-        sph_launch_gather(L, true, false);
+        sph_launch_gather(L, true, false, true);
         phase("density");
         sph_launch_density(L, false, true, false);
         phase("deformations (solid phase)");
@@ -298,9 +299,9 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
 void sph_launch_rigid(const Launch &L) {
     if (!L.num_rigid || !L.rigid) return;
     const dim3 grid(SPH_RIGID_BLOCKS, L.num_rigid);
-    k_rigid_reduce<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
-    k_rigid_integrate<<<(L.num_rigid + 63) / 64, 64, 0, L.stream>>>(L.scenes, L.rigid, L.num_rigid);
-    k_rigid_scatter<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
+    k_rigid_reduce<<<grid, 32, 0, L.stream>>>(L.scenes, L.rigid);
+    k_rigid_integrate<<<L.num_rigid, 32, 0, L.stream>>>(L.scenes, L.rigid, L.num_rigid);
+    k_rigid_scatter<<<grid, SPH_RIGID_SCATTER_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
 }
 
 void sph_launch_rigid_reset(const Launch &L) {

@@ -360,7 +360,9 @@ __global__ void __launch_bounds__(1024) k_sort_big_cells(const SceneDesc *__rest
 
 // Cell-sorted copies: spos[k] = position[cellparticles[k]] (and velocity,
 // density when asked; for solids also the rest position with the body
-// number, and 1/density0 in the velocity copy's w).  Gathers once so the pair loops stream float4s.
+// number -- and in a mixed scene SPH_SOLID_PHASE_BIT for a solid-phase
+// particle -- and 1/density0 in the velocity copy's w).  Gathers once so
+// the pair loops stream float4s.
 __global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int with_vel, int with_dens,
                          int with_solid) {
     SPH_FOR_WORK(map)
@@ -378,7 +380,9 @@ __global__ void k_gather(const SceneDesc *__restrict__ scenes, BlockMap map, int
         if (solid) {
             // rest position, and the body number's bits in w
             const float3 p0 = ld3(S.originalpos, i);
-            S.spos0[item] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(S.body_number[i]));
+            unsigned w = S.body_number[i];
+            if (S.phase && S.phase[i]) w |= SPH_SOLID_PHASE_BIT;
+            S.spos0[item] = make_float4(p0.x, p0.y, p0.z, __uint_as_float(w));
         }
     }
     SPH_END_WORK

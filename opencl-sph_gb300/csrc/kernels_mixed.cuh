@@ -51,30 +51,40 @@ __global__ void k_original_density_mixed(const SceneDesc *__restrict__ scenes, B
     SPH_END_WORK
 }
 
+// A candidate kk of a mixed scene's solid particle k is a solid partner
+// when it is another particle (kk != k) of the solid phase: both read from
+// the sorted rest-position copy (spos0, gathered with the phase bit), so
+// the test needs no dependent load through cellparticles.
+__device__ __forceinline__ bool solid_partner(float4 q4, unsigned kk, unsigned k) {
+    return kk != k && (__float_as_uint(q4.w) & SPH_SOLID_PHASE_BIT) != 0u;
+}
+
 // compute_deformations (solid_svk.cl:82-175) of a mixed scene's solid
 // particles over their solid neighbours: F = Apq Aqq^-1 with
 // Apq = sum W(|p|) p q^T and Aqq = sum W(|p|) q q^T over j != i, |p| <= h.
+// Needs the sorted copies gathered with the rest positions.
 __global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
-    if (!S.phase) continue;
+    if (!S.phase || !S.spos0) continue;
     if (item < active_count(S)) {
         const unsigned k = item;
-        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
-        if (S.phase[i] != 0u) {
+        const float4 k0 = S.spos0[k];
+        if (__float_as_uint(k0.w) & SPH_SOLID_PHASE_BIT) {
+            const unsigned i = min(S.cellparticles[k], S.pnum - 1);
             const SolidConsts C = solid_consts(S);
             const float3 ipos = xyz(S.spos[k]);
-            const float3 ipos0 = ld3(S.originalpos, i);
+            const float3 ipos0 = xyz(k0);
             float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             float aqq[6] = {0, 0, 0, 0, 0, 0};
             for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
-                if (j == i || S.phase[j] == 0u) return;
+                const float4 q4 = S.spos0[kk];
+                if (!solid_partner(q4, kk, k)) return;
                 const float3 p = sub3(xyz(S.spos[kk]), ipos);
                 const float r2 = norm2(p);
                 if (!(r2 <= C.le)) return;
                 const float d = fmaxf(C.h2 - r2, 0.f);
                 const float w = d * d * d;
-                const float3 q = sub3(ld3(S.originalpos, j), ipos0);
+                const float3 q = sub3(xyz(q4), ipos0);
                 add_outer(p * w, q, apq);
                 const float3 wq = q * w;
                 aqq[0] = __fmaf_rn(wq.x, q.x, aqq[0]);
@@ -100,29 +110,33 @@ __global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, Block
 // Laplacian viscosity (solid_viscosity when the store has it).  Writes
 // force, force_elastic, force_viscous and cutoff_force (no symmetry
 // planes: the cut-off force is the whole force); the fluid force pass then
-// adds the particle's fluid pair terms and steps it.
+// adds the particle's fluid pair terms and steps it.  The candidate tests
+// read the sorted copies (gathered with the rest positions); the fields of
+// j are read for the neighbours only.
 __global__ void k_forces_solids_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
     SPH_FOR_WORK(map)
-    if (!S.phase) continue;
+    if (!S.phase || !S.spos0) continue;
     if (item < active_count(S)) {
         const unsigned k = item;
-        const unsigned i = min(S.cellparticles[k], S.pnum - 1);
-        if (S.phase[i] != 0u) {
+        const float4 k0 = S.spos0[k];
+        if (__float_as_uint(k0.w) & SPH_SOLID_PHASE_BIT) {
+            const unsigned i = min(S.cellparticles[k], S.pnum - 1);
             const SolidConsts C = solid_consts(S);
             const float3 ipos = xyz(S.spos[k]);
             const float3 ivel = ld3(S.velocity, i);
-            const float3 ipos0 = ld3(S.originalpos, i);
+            const float3 ipos0 = xyz(k0);
             float si[6];
             for (int c = 0; c < 6; ++c) si[c] = S.stress[6 * (size_t)i + c];
             const float rho0i = S.density0[i];
             Kahan3 fe_s, fv_s;
             for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
-                if (j == i || S.phase[j] == 0u) return;
+                const float4 q4 = S.spos0[kk];
+                if (!solid_partner(q4, kk, k)) return;
                 const float3 jpos = xyz(S.spos[kk]);
-                const float3 x = sub3(ipos0, ld3(S.originalpos, j));
+                const float3 x = sub3(ipos0, xyz(q4));
                 const float r2 = norm2(sub3(jpos, ipos));
                 if (!(norm2(x) <= C.le || r2 <= C.le)) return;
+                const unsigned j = min(S.cellparticles[kk], S.pnum - 1);
                 const float3 jvel = ld3(S.velocity, j);
                 const float vivj = C.mass * C.mass / rho0i / S.density0[j];
                 const float mrj = C.mass / S.density[j];
@@ -130,7 +144,8 @@ __global__ void k_forces_solids_mixed(const SceneDesc *__restrict__ scenes, Bloc
                 for (int c = 0; c < 6; ++c) sj[c] = S.stress[6 * (size_t)j + c];
                 const float3 gx = spiky_grad(x, C.h, C.kv, C.le);
                 const float3 f_ji = sym_vec(si, gx) * (-vivj);
-                const float3 f_ij = S.body_number[j] > 0 ? -f_ji : sym_vec(sj, -gx) * (-vivj);
+                const bool jbody = (__float_as_uint(q4.w) & ~SPH_SOLID_PHASE_BIT) != 0u;
+                const float3 f_ij = jbody ? -f_ji : sym_vec(sj, -gx) * (-vivj);
                 const float3 fe = f_ij - f_ji;
                 const float lap = r2 <= C.le ? C.kv * (C.h - sqrtf(r2)) : 0.f;
                 const float3 fv = (jvel - ivel) * (mrj * lap);

@@ -15,11 +15,17 @@
 // first substep, and again after the host rewrites positions, velocities
 // or body tables.
 //
-// Sums are deterministic: each of SPH_RIGID_BLOCKS blocks sums a fixed
-// stride of the body's particle range (per thread in index order, then a
-// fixed shuffle tree and warp order), and the per-block partials are added
-// in block order.  A body's result is therefore the same alone and in any
+// Sums are deterministic: each of SPH_RIGID_BLOCKS one-warp blocks sums a
+// fixed stride of the body's particle range (per lane in index order, then
+// the lanes' sums in lane order), and the per-block partials are added in
+// block order.  A body's result is therefore the same alone and in any
 // batch.
+//
+// FP64 arithmetic runs at a small fraction of the FP32 rate on this part
+// (each warp instruction occupies the unit for many cycles whatever the
+// number of active lanes), so the kernels spend as few FP64 warp
+// instructions as they can: no shuffle trees (a column sum per value, one
+// lane per value), one warp per body for the body's step.
 #pragma once
 
 #include "kernels_common.cuh"
@@ -69,29 +75,13 @@ __device__ __forceinline__ bool body_skips_step(const SceneDesc &S, unsigned i) 
     return dyn == 0u || dyn == SPH_BODY_RIGID;
 }
 
-// Fixed-order block reduction of one double (sum, min or max).
-template <int OP>
-__device__ __forceinline__ double rigid_block_reduce(double v, double *smem) {
-    for (int o = 16; o > 0; o >>= 1) {
-        const double u = __shfl_down_sync(SPH_FULL_MASK, v, o);
-        v = OP == 0 ? v + u : OP == 1 ? fmin(v, u) : fmax(v, u);
-    }
-    const unsigned warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
-    __syncthreads();
-    if (lane == 0) smem[warp] = v;
-    __syncthreads();
-    double r = smem[0];
-    for (unsigned w = 1; w < (blockDim.x >> 5); ++w) {
-        const double u = smem[w];
-        r = OP == 0 ? r + u : OP == 1 ? fmin(r, u) : fmax(r, u);
-    }
-    return r;  // the same value in every thread
-}
-
-// grid (SPH_RIGID_BLOCKS, rigid bodies), SPH_RIGID_THREADS threads
-__global__ void __launch_bounds__(SPH_RIGID_THREADS)
+// grid (SPH_RIGID_BLOCKS, rigid bodies), one warp per block: lane l sums
+// particles lo + 32 b + l, lo + 32 (b + B) + l, ... in index order; lane q
+// then adds value q of the 32 lanes in lane order.
+__global__ void __launch_bounds__(32)
     k_rigid_reduce(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work) {
-    __shared__ double smem[SPH_RIGID_THREADS / 32];
+    __shared__ double cols[RQ_SUMS][33];  // value q of lane l (padded rows)
+    const unsigned lane = threadIdx.x;
     const RigidWork w = work[blockIdx.y];
     const SceneDesc &S = scenes[w.scene];
     if (scene_idle(S) || !S.rigid_state || w.body == 0 || w.body > S.body_capacity) return;
@@ -106,8 +96,8 @@ __global__ void __launch_bounds__(SPH_RIGID_THREADS)
     double acc[RQ_SUMS];
 #pragma unroll
     for (int q = 0; q < RQ_SUMS; ++q) acc[q] = 0.0;
-    double mn = 4294967296.0, mx = -1.0;
-    for (unsigned i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
+    unsigned mn = 0xffffffffu, mx1 = 0;  // lowest index, highest index + 1 (0: none)
+    for (unsigned i = lo + blockIdx.x * 32u + lane; i < hi; i += gridDim.x * 32u) {
         if (!rigid_particle_of(S, i, w.body)) continue;
         const float3 xf = ld3(S.position, i), vf = ld3(S.velocity, i), ff = ld3(S.force, i);
         const double x = xf.x, y = xf.y, z = xf.z;
@@ -135,20 +125,23 @@ __global__ void __launch_bounds__(SPH_RIGID_THREADS)
         acc[RQ_XF] += y * fz - z * fy;
         acc[RQ_XF + 1] += z * fx - x * fz;
         acc[RQ_XF + 2] += x * fy - y * fx;
-        mn = fmin(mn, (double)i);
-        mx = fmax(mx, (double)i);
+        mn = min(mn, i);
+        mx1 = max(mx1, i + 1u);
     }
-    double *part = S.rigid_partial + ((size_t)(w.body - 1) * SPH_RIGID_BLOCKS + blockIdx.x) * SPH_RIGID_Q;
 #pragma unroll
-    for (int q = 0; q < RQ_SUMS; ++q) {
-        const double r = rigid_block_reduce<0>(acc[q], smem);
-        if (threadIdx.x == 0) part[q] = r;
+    for (int q = 0; q < RQ_SUMS; ++q) cols[q][lane] = acc[q];
+    __syncwarp();
+    double *part = S.rigid_partial + ((size_t)(w.body - 1) * SPH_RIGID_BLOCKS + blockIdx.x) * SPH_RIGID_Q;
+    if (lane < RQ_SUMS) {
+        double v = cols[lane][0];
+        for (int l = 1; l < 32; ++l) v += cols[lane][l];
+        part[lane] = v;
     }
-    const double rmn = rigid_block_reduce<1>(mn, smem);
-    const double rmx = rigid_block_reduce<2>(mx, smem);
-    if (threadIdx.x == 0) {
-        part[RQ_MIN] = rmn;
-        part[RQ_MAX] = rmx;
+    const unsigned rmn = __reduce_min_sync(SPH_FULL_MASK, mn);
+    const unsigned rmx1 = __reduce_max_sync(SPH_FULL_MASK, mx1);
+    if (lane == 0) {
+        part[RQ_MIN] = rmn == 0xffffffffu ? 4294967296.0 : (double)rmn;
+        part[RQ_MAX] = rmx1 == 0u ? -1.0 : (double)(rmx1 - 1u);
     }
 }
 
@@ -194,26 +187,38 @@ __device__ __forceinline__ void sym_inverse(const double I[9], double out[9]) {
     out[8] = (I[0] * I[4] - I[1] * I[3]) * inv;
 }
 
-// One thread per rigid body: the partials' sums, set-up when due, and the
-// body's substep.
-__global__ void k_rigid_integrate(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work,
-                                  unsigned num) {
-    const unsigned p = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per rigid body (grid: rigid bodies): lane q adds the blocks'
+// partials of value q in block order (the index range's min and max in
+// lanes RQ_MIN and RQ_MAX); lane 0 then sets the body up when due and takes
+// its substep.
+__global__ void __launch_bounds__(32)
+    k_rigid_integrate(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work, unsigned num) {
+    __shared__ double sum[SPH_RIGID_Q];
+    const unsigned p = blockIdx.x, lane = threadIdx.x;
     if (p >= num) return;
     const RigidWork wk = work[p];
     const SceneDesc &S = scenes[wk.scene];
     if (scene_idle(S) || !S.rigid_state || wk.body == 0 || wk.body > S.body_capacity) return;
     double *st = S.rigid_state + (size_t)(wk.body - 1) * SPH_RIGID_STRIDE;
     const double *part = S.rigid_partial + (size_t)(wk.body - 1) * SPH_RIGID_BLOCKS * SPH_RIGID_Q;
-    double sum[RQ_SUMS];
-    for (int q = 0; q < RQ_SUMS; ++q) sum[q] = 0.0;
-    double mn = 4294967296.0, mx = -1.0;
-    for (int blk = 0; blk < SPH_RIGID_BLOCKS; ++blk) {
-        const double *pb = part + (size_t)blk * SPH_RIGID_Q;
-        for (int q = 0; q < RQ_SUMS; ++q) sum[q] += pb[q];
-        mn = fmin(mn, pb[RQ_MIN]);
-        mx = fmax(mx, pb[RQ_MAX]);
+    if (lane < SPH_RIGID_Q) {
+        // the min and max as integers on the bit patterns: the partials'
+        // indices are whole and >= 0, their sentinels 2^32 and -1, so
+        // signed 64-bit order is numeric order (no extra FP64 work)
+        double v = 0.0;
+        long long mnb = __double_as_longlong(4294967296.0), mxb = __double_as_longlong(-1.0);
+        for (int blk = 0; blk < SPH_RIGID_BLOCKS; ++blk) {
+            const double u = part[(size_t)blk * SPH_RIGID_Q + lane];
+            v += u;
+            const long long ub = __double_as_longlong(u);
+            mnb = min(mnb, ub);
+            mxb = max(mxb, ub);
+        }
+        sum[lane] = lane == RQ_MIN ? __longlong_as_double(mnb) : lane == RQ_MAX ? __longlong_as_double(mxb) : v;
     }
+    __syncwarp();
+    if (lane != 0) return;
+    const double mn = sum[RQ_MIN], mx = sum[RQ_MAX];
     if (sum[RQ_N] == 0.0) {
         st[RS_FLAG] = 0.0;  // no particles (yet): set up when some appear
         return;
@@ -294,8 +299,9 @@ __global__ void k_rigid_integrate(const SceneDesc *__restrict__ scenes, const Ri
         for (int k = 0; k < 3; ++k) S.body_position[3 * (wk.body - 1) + k] = (float)c[k];
 }
 
-// grid (SPH_RIGID_BLOCKS, rigid bodies): puts the body's particles on it.
-__global__ void __launch_bounds__(SPH_RIGID_THREADS)
+// grid (SPH_RIGID_BLOCKS, rigid bodies), SPH_RIGID_SCATTER_THREADS
+// threads: puts the body's particles on it.
+__global__ void __launch_bounds__(SPH_RIGID_SCATTER_THREADS)
     k_rigid_scatter(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work) {
     const RigidWork wk = work[blockIdx.y];
     const SceneDesc &S = scenes[wk.scene];

@@ -28,6 +28,9 @@ struct Launch {
     // some scene of the table is a mixed fluid-solid scene (its phase
     // field is set): the mixed kernels are launched too
     bool has_mixed;
+    // every scene of the table is mixed: the plain-fluid instantiations,
+    // which skip mixed scenes, are not launched (false is always safe)
+    bool all_mixed;
 };
 
 // At most this many rigid bodies per launch (the reduction grid's y extent).

@@ -117,8 +117,12 @@ struct SceneDesc {
 // 0 (fixed) and any other value (free particles) keep the reference's
 // meaning.
 #define SPH_BODY_RIGID 2u
-#define SPH_RIGID_BLOCKS 32     // reduction blocks per body
-#define SPH_RIGID_THREADS 256
+// In a mixed fluid-solid scene (extension) the sorted rest-position copy's
+// w lane holds the body number's bits with this bit set for a solid-phase
+// particle.
+#define SPH_SOLID_PHASE_BIT 0x80000000u
+#define SPH_RIGID_BLOCKS 32     // reduction blocks per body, one warp each
+#define SPH_RIGID_SCATTER_THREADS 256
 #define SPH_RIGID_Q 24          // reduced quantities per body
 #define SPH_RIGID_STRIDE 64     // doubles of state per body
 
