@@ -338,6 +338,64 @@ def bench_plain(args, scene, torch, world):
             "status": status, "kernels_per_step": kernels_per_step, "pairs": pairs}
 
 
+# The reference drivers' update recipes (scripts/sph/systems.py:113-189),
+# kernel by kernel through call_for_all_particles after
+# compute_particle_bins.
+NAMED_RECIPES = {
+    "fluid": ("compute_density", "compute_forces_fluids", "step_forward"),
+    "corot": ("compute_density", "compute_rotations_and_strains", "compute_stresses", "compute_forces_solids",
+              "step_forward"),
+    "svk": ("compute_density", "compute_deformations", "compute_stresses", "compute_forces_solids",
+            "step_forward"),
+    # the mixed-scene extension's recipe (the solids' elastic passes, then
+    # the fluid force pass, which adds the fluid pair terms)
+    "mixed": ("compute_density", "compute_deformations", "compute_stresses", "compute_forces_solids",
+              "compute_forces_fluids", "step_forward"),
+}
+
+
+def bench_named(args, scene, torch):
+    """The drop-in's named path, the one an unmodified reference driver
+    takes: per substep compute_particle_bins and the material's kernels by
+    name (each pair call re-gathers the sorted copies from the fields and
+    scans the stencil; no masks), on the same scene as the fused substep.
+    Device time with CUDA events on the store's stream, L2 flushed between
+    substeps as for the fused line."""
+    from sph import bindings as bnd
+    ps = scene.system()
+    if scene.material != "fluid":
+        _solid_setup(ps)
+    recipe = NAMED_RECIPES[scene.material]
+
+    def substep():
+        ps.compute_particle_bins()
+        for k in recipe:
+            ps.call_for_all_particles(k)
+
+    ext = torch.cuda.ExternalStream(bnd.sph_stream(ps.psdata_opencl))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(max(args.warmup, 1)):
+        substep()
+    ps.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with torch.cuda.stream(ext):
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(ext)
+            substep()
+            ends[k].record(ext)
+    torch.cuda.synchronize()
+    total_s = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / 1e3
+    status = ps.status()
+    ps.close()
+    return {"value": scene.n * args.steps / total_s, "unit": UNIT, "ms_per_step": total_s * 1e3 / args.steps,
+            "status": status, "recipe": ["compute_particle_bins"] + list(recipe),
+            "how": "the reference driver's update() recipe by name (call_for_all_particles per kernel), "
+                   "CUDA events on the store's stream, L2 flushed between substeps"}
+
+
 def pair_counts(ps):
     """Pair evaluations of one substep of the store's current state: stencil
     candidates (every particle against the 27 cells around its own, from
@@ -821,15 +879,18 @@ def workload_config(name, seed, standalone=False):
             "l2": "flushed between timed steps (256 MB write, outside the timed events)"}
 
 
-def _plain_extra(args, name, torch, peak, peak_kind):
+def _plain_extra(args, name, torch, peak, peak_kind, named=False):
     sc, desc = workload(name, args.seed)
     p = bench_plain(args, sc, torch, 1)
-    return {"workload": name + ": " + desc, "value": p["n"] * args.steps / p["total_s"],
-            "ms_per_step": p["total_s"] * 1e3 / args.steps, "clocks": p["clocks"], "status": p["status"],
-            "kernels_per_step": p["kernels_per_step"], "phase_ms": p["phases"],
-            "roofline": _phase_roofline(p["phases"], p["n"], p["cells"], peak, peak_kind, workload=name,
-                                        clocks=p["clocks"]),
-            "e2e": p["e2e"]}
+    out = {"workload": name + ": " + desc, "value": p["n"] * args.steps / p["total_s"],
+           "ms_per_step": p["total_s"] * 1e3 / args.steps, "clocks": p["clocks"], "status": p["status"],
+           "kernels_per_step": p["kernels_per_step"], "phase_ms": p["phases"],
+           "roofline": _phase_roofline(p["phases"], p["n"], p["cells"], peak, peak_kind, workload=name,
+                                       clocks=p["clocks"]),
+           "e2e": p["e2e"]}
+    if named:
+        out["plain_named"] = bench_named(args, sc, torch)
+    return out
 
 
 def run_ours(args, rank, world, local_rank):
@@ -868,13 +929,15 @@ def run_ours(args, rank, world, local_rank):
             extra["fp64_error"] = fp64_error_sample(r["scenes"], 100)
             extra["fp64_error_configs"] = fp64_error_configs()
             extra["served"] = bench_served(args)
-            extra["plain_1m"] = _plain_extra(args, "wcsph-1m", torch, peak, peak_kind)
+            extra["plain_1m"] = _plain_extra(args, "wcsph-1m", torch, peak, peak_kind, named=True)
             extra["large_scene"] = _plain_extra(args, "large-scene", torch, peak, peak_kind)
             extra["fp64_error_1m"] = fp64_error_1m(args.seed)
     else:
         scene, _ = workload(args.workload, args.seed + rank)
         r = bench_plain(args, scene, torch, world)
         extra["path"] = "plain single scene, one CUDA-graph substep per step (sph_update)"
+        if rank == 0 and scene.material in NAMED_RECIPES:
+            extra["plain_named"] = bench_named(args, scene, torch)
     extra["cells"] = r["cells"]
     extra["parallelism"] = "replicas (no collective)" if world > 1 else "single GPU"
     if "pairs" in r and r["phases"]:

@@ -299,9 +299,9 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
 void sph_launch_rigid(const Launch &L) {
     if (!L.num_rigid || !L.rigid) return;
     const dim3 grid(SPH_RIGID_BLOCKS, L.num_rigid);
-    k_rigid_reduce<<<grid, 32, 0, L.stream>>>(L.scenes, L.rigid);
+    k_rigid_reduce<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
     k_rigid_integrate<<<L.num_rigid, 32, 0, L.stream>>>(L.scenes, L.rigid, L.num_rigid);
-    k_rigid_scatter<<<grid, SPH_RIGID_SCATTER_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
+    k_rigid_scatter<<<grid, SPH_RIGID_THREADS, 0, L.stream>>>(L.scenes, L.rigid);
 }
 
 void sph_launch_rigid_reset(const Launch &L) {

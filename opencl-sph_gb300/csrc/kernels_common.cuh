@@ -138,15 +138,20 @@ struct Kahan3 {
 // every walk over a particle's stencil calls it once for each of the nine
 // rows, empty or outside the grid, so that two walks over the same
 // neighbours in the same order give the same bits.
+// The row sum's x and y lanes are one packed FP32x2 add.
 struct BlockSum3 {
-    float3 row = make_float3(0.f, 0.f, 0.f);
+    float2 rxy = make_float2(0.f, 0.f);
+    float rz = 0.f;
     Kahan3 total;
-    __device__ __forceinline__ void add(float3 v) {
-        row = make_float3(__fadd_rn(row.x, v.x), __fadd_rn(row.y, v.y), __fadd_rn(row.z, v.z));
+    __device__ __forceinline__ void add2(float2 vxy, float vz) {
+        rxy = __fadd2_rn(rxy, vxy);
+        rz = __fadd_rn(rz, vz);
     }
+    __device__ __forceinline__ void add(float3 v) { add2(make_float2(v.x, v.y), v.z); }
     __device__ __forceinline__ void end_row() {
-        total.add(row);
-        row = make_float3(0.f, 0.f, 0.f);
+        total.add(make_float3(rxy.x, rxy.y, rz));
+        rxy = make_float2(0.f, 0.f);
+        rz = 0.f;
     }
     __device__ __forceinline__ float3 get() const { return total.get(); }
 };

@@ -209,6 +209,7 @@ __device__ __forceinline__ void integrate(const SceneDesc &S, unsigned i, float3
 // Particle i's side of the fluid pair term.
 struct FluidI {
     float3 ipos, ivel;
+    float2 nxy, nvxy;  // -ipos and -ivel's x, y lanes (the packed differences)
     float inv_rhoi, pi, h, rho0, stiff, visc, kv;
     float vk, pk;  // visc kv and -kv / 2, the pair term's constant factors
     DistBounds B;
@@ -218,6 +219,8 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
     FluidI I;
     I.ipos = ipos;
     I.ivel = ivel;
+    I.nxy = make_float2(-ipos.x, -ipos.y);
+    I.nvxy = make_float2(-ivel.x, -ivel.y);
     I.inv_rhoi = rcp_approx(rhoi);
     I.h = *S.h;
     I.B = dist_bounds(I.h);
@@ -242,8 +245,12 @@ __device__ __forceinline__ FluidI fluid_i(const SceneDesc &S, float3 ipos, float
 template <bool IN_RANGE = false>
 __device__ __forceinline__ float fluid_pair_p(const FluidI &I, float pi, float3 jpos, float3 jvel, float pj,
                                               float inv_rhoj, BlockSum3 &f) {
-    const float3 d = sub3(jpos, I.ipos);
-    const float r2 = norm2(d);
+    // d = x_j - x_i and r^2 as sub3 and norm2 compute them, the x and y
+    // lanes in packed FP32x2 instructions (each lane rounded alike)
+    const float2 dxy = __fadd2_rn(make_float2(jpos.x, jpos.y), I.nxy);
+    const float dz = __fsub_rn(jpos.z, I.ipos.z);
+    const float2 sq = __fmul2_rn(dxy, dxy);
+    const float r2 = __fadd_rn(__fadd_rn(sq.x, sq.y), __fmul_rn(dz, dz));
     if ((!IN_RANGE && !(r2 <= I.B.le)) || r2 == 0.f) return r2;
     const float rinv = rsqrtf(r2);
     const float dist = __fmul_rn(r2, rinv);
@@ -251,10 +258,13 @@ __device__ __forceinline__ float fluid_pair_p(const FluidI &I, float pi, float3 
     const float inv_didj = __fmul_rn(I.inv_rhoi, inv_rhoj);
     const float vterm = __fmul_rn(din, I.vk);
     const float pterm = __fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(__fadd_rn(pi, pj), I.pk), rinv), din), din);
-    const float3 rv = sub3(jvel, I.ivel);
-    f.add(make_float3(__fmul_rn(__fmaf_rn(d.x, pterm, __fmul_rn(rv.x, vterm)), inv_didj),
-                      __fmul_rn(__fmaf_rn(d.y, pterm, __fmul_rn(rv.y, vterm)), inv_didj),
-                      __fmul_rn(__fmaf_rn(d.z, pterm, __fmul_rn(rv.z, vterm)), inv_didj)));
+    // (d pterm + (v_j - v_i) vterm) / (rho_i rho_j), per lane as
+    // __fmul_rn(__fmaf_rn(d, pterm, __fmul_rn(rv, vterm)), inv_didj)
+    const float2 rvxy = __fadd2_rn(make_float2(jvel.x, jvel.y), I.nvxy);
+    const float rvz = __fsub_rn(jvel.z, I.ivel.z);
+    const float2 fxy = __fmul2_rn(__ffma2_rn(dxy, make_float2(pterm, pterm), __fmul2_rn(rvxy, make_float2(vterm, vterm))),
+                                  make_float2(inv_didj, inv_didj));
+    f.add2(fxy, __fmul_rn(__fmaf_rn(dz, pterm, __fmul_rn(rvz, vterm)), inv_didj));
     return r2;
 }
 

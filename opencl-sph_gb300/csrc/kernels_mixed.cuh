@@ -59,6 +59,25 @@ __device__ __forceinline__ bool solid_partner(float4 q4, unsigned kk, unsigned k
     return kk != k && (__float_as_uint(q4.w) & SPH_SOLID_PHASE_BIT) != 0u;
 }
 
+// f(kk, p4, q4) for particle k's stencil candidates in the reference's
+// order, with the candidate's sorted position and rest position loaded at
+// the top of each step: the row loop is unrolled by 4, so four candidates'
+// loads are in flight before the first one's tests (the solid particles of
+// a mixed scene are too few warps to hide the latency otherwise).
+template <class F>
+__device__ __forceinline__ void for_each_candidate_sorted(const SceneDesc &S, unsigned cell, F &&f) {
+    const StencilRows rows(S, cell);
+    const float4 *__restrict__ spos = S.spos;
+    const float4 *__restrict__ spos0 = S.spos0;
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        unsigned b, e;
+        rows.row(S, r, &b, &e);
+#pragma unroll 4
+        for (unsigned kk = b; kk < e; ++kk) f(kk, spos[kk], spos0[kk]);
+    }
+}
+
 // compute_deformations (solid_svk.cl:82-175) of a mixed scene's solid
 // particles over their solid neighbours: F = Apq Aqq^-1 with
 // Apq = sum W(|p|) p q^T and Aqq = sum W(|p|) q q^T over j != i, |p| <= h.
@@ -76,10 +95,9 @@ __global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, Block
             const float3 ipos0 = xyz(k0);
             float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             float aqq[6] = {0, 0, 0, 0, 0, 0};
-            for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-                const float4 q4 = S.spos0[kk];
+            for_each_candidate_sorted(S, S.gridcell[i], [&](unsigned kk, float4 p4, float4 q4) {
                 if (!solid_partner(q4, kk, k)) return;
-                const float3 p = sub3(xyz(S.spos[kk]), ipos);
+                const float3 p = sub3(xyz(p4), ipos);
                 const float r2 = norm2(p);
                 if (!(r2 <= C.le)) return;
                 const float d = fmaxf(C.h2 - r2, 0.f);
@@ -129,10 +147,9 @@ __global__ void k_forces_solids_mixed(const SceneDesc *__restrict__ scenes, Bloc
             for (int c = 0; c < 6; ++c) si[c] = S.stress[6 * (size_t)i + c];
             const float rho0i = S.density0[i];
             Kahan3 fe_s, fv_s;
-            for_each_neighbour(S, S.gridcell[i], [&](unsigned kk) {
-                const float4 q4 = S.spos0[kk];
+            for_each_candidate_sorted(S, S.gridcell[i], [&](unsigned kk, float4 p4, float4 q4) {
                 if (!solid_partner(q4, kk, k)) return;
-                const float3 jpos = xyz(S.spos[kk]);
+                const float3 jpos = xyz(p4);
                 const float3 x = sub3(ipos0, xyz(q4));
                 const float r2 = norm2(sub3(jpos, ipos));
                 if (!(norm2(x) <= C.le || r2 <= C.le)) return;

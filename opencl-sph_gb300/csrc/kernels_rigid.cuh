@@ -15,17 +15,18 @@
 // first substep, and again after the host rewrites positions, velocities
 // or body tables.
 //
-// Sums are deterministic: each of SPH_RIGID_BLOCKS one-warp blocks sums a
-// fixed stride of the body's particle range (per lane in index order, then
-// the lanes' sums in lane order), and the per-block partials are added in
-// block order.  A body's result is therefore the same alone and in any
+// Sums are deterministic: each of SPH_RIGID_BLOCKS blocks sums a fixed
+// stride of the body's particle range (per thread in index order, then the
+// lanes' sums in lane order and the warps' in warp order), and the
+// per-block partials are added in block order.  A body's result is therefore the same alone and in any
 // batch.
 //
 // FP64 arithmetic runs at a small fraction of the FP32 rate on this part
 // (each warp instruction occupies the unit for many cycles whatever the
 // number of active lanes), so the kernels spend as few FP64 warp
 // instructions as they can: no shuffle trees (a column sum per value, one
-// lane per value), one warp per body for the body's step.
+// lane per value, through shared memory), one warp per body for the body's
+// step.
 #pragma once
 
 #include "kernels_common.cuh"
@@ -75,13 +76,18 @@ __device__ __forceinline__ bool body_skips_step(const SceneDesc &S, unsigned i) 
     return dyn == 0u || dyn == SPH_BODY_RIGID;
 }
 
-// grid (SPH_RIGID_BLOCKS, rigid bodies), one warp per block: lane l sums
-// particles lo + 32 b + l, lo + 32 (b + B) + l, ... in index order; lane q
-// then adds value q of the 32 lanes in lane order.
-__global__ void __launch_bounds__(32)
+// grid (SPH_RIGID_BLOCKS, rigid bodies), SPH_RIGID_THREADS threads: thread
+// t of block b sums particles lo + T b + t, lo + T (b + B) + t, ... in index
+// order (T threads, B blocks); lane q of each warp then adds value q of its
+// warp's 32 lanes in lane order, and lane q of warp 0 the warps' sums in
+// warp order.
+__global__ void __launch_bounds__(SPH_RIGID_THREADS)
     k_rigid_reduce(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work) {
-    __shared__ double cols[RQ_SUMS][33];  // value q of lane l (padded rows)
-    const unsigned lane = threadIdx.x;
+    constexpr int W = SPH_RIGID_THREADS / 32;
+    __shared__ double cols[W][RQ_SUMS][33];  // value q of lane l, per warp (padded rows)
+    __shared__ double wsum[W][RQ_SUMS];
+    __shared__ unsigned wmin[W], wmax1[W];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const RigidWork w = work[blockIdx.y];
     const SceneDesc &S = scenes[w.scene];
     if (scene_idle(S) || !S.rigid_state || w.body == 0 || w.body > S.body_capacity) return;
@@ -97,7 +103,7 @@ __global__ void __launch_bounds__(32)
 #pragma unroll
     for (int q = 0; q < RQ_SUMS; ++q) acc[q] = 0.0;
     unsigned mn = 0xffffffffu, mx1 = 0;  // lowest index, highest index + 1 (0: none)
-    for (unsigned i = lo + blockIdx.x * 32u + lane; i < hi; i += gridDim.x * 32u) {
+    for (unsigned i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x) {
         if (!rigid_particle_of(S, i, w.body)) continue;
         const float3 xf = ld3(S.position, i), vf = ld3(S.velocity, i), ff = ld3(S.force, i);
         const double x = xf.x, y = xf.y, z = xf.z;
@@ -129,19 +135,35 @@ __global__ void __launch_bounds__(32)
         mx1 = max(mx1, i + 1u);
     }
 #pragma unroll
-    for (int q = 0; q < RQ_SUMS; ++q) cols[q][lane] = acc[q];
+    for (int q = 0; q < RQ_SUMS; ++q) cols[warp][q][lane] = acc[q];
     __syncwarp();
-    double *part = S.rigid_partial + ((size_t)(w.body - 1) * SPH_RIGID_BLOCKS + blockIdx.x) * SPH_RIGID_Q;
     if (lane < RQ_SUMS) {
-        double v = cols[lane][0];
-        for (int l = 1; l < 32; ++l) v += cols[lane][l];
-        part[lane] = v;
+        double v = cols[warp][lane][0];
+        for (int l = 1; l < 32; ++l) v += cols[warp][lane][l];
+        wsum[warp][lane] = v;
     }
     const unsigned rmn = __reduce_min_sync(SPH_FULL_MASK, mn);
     const unsigned rmx1 = __reduce_max_sync(SPH_FULL_MASK, mx1);
     if (lane == 0) {
-        part[RQ_MIN] = rmn == 0xffffffffu ? 4294967296.0 : (double)rmn;
-        part[RQ_MAX] = rmx1 == 0u ? -1.0 : (double)(rmx1 - 1u);
+        wmin[warp] = rmn;
+        wmax1[warp] = rmx1;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    double *part = S.rigid_partial + ((size_t)(w.body - 1) * SPH_RIGID_BLOCKS + blockIdx.x) * SPH_RIGID_Q;
+    if (lane < RQ_SUMS) {
+        double v = wsum[0][lane];
+        for (int u = 1; u < W; ++u) v += wsum[u][lane];
+        part[lane] = v;
+    }
+    if (lane == 0) {
+        unsigned bmn = wmin[0], bmx1 = wmax1[0];
+        for (int u = 1; u < W; ++u) {
+            bmn = min(bmn, wmin[u]);
+            bmx1 = max(bmx1, wmax1[u]);
+        }
+        part[RQ_MIN] = bmn == 0xffffffffu ? 4294967296.0 : (double)bmn;
+        part[RQ_MAX] = bmx1 == 0u ? -1.0 : (double)(bmx1 - 1u);
     }
 }
 
@@ -299,9 +321,9 @@ __global__ void __launch_bounds__(32)
         for (int k = 0; k < 3; ++k) S.body_position[3 * (wk.body - 1) + k] = (float)c[k];
 }
 
-// grid (SPH_RIGID_BLOCKS, rigid bodies), SPH_RIGID_SCATTER_THREADS
-// threads: puts the body's particles on it.
-__global__ void __launch_bounds__(SPH_RIGID_SCATTER_THREADS)
+// grid (SPH_RIGID_BLOCKS, rigid bodies), SPH_RIGID_THREADS threads: puts
+// the body's particles on it.
+__global__ void __launch_bounds__(SPH_RIGID_THREADS)
     k_rigid_scatter(const SceneDesc *__restrict__ scenes, const RigidWork *__restrict__ work) {
     const RigidWork wk = work[blockIdx.y];
     const SceneDesc &S = scenes[wk.scene];

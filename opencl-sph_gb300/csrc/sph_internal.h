@@ -121,8 +121,8 @@ struct SceneDesc {
 // w lane holds the body number's bits with this bit set for a solid-phase
 // particle.
 #define SPH_SOLID_PHASE_BIT 0x80000000u
-#define SPH_RIGID_BLOCKS 32     // reduction blocks per body, one warp each
-#define SPH_RIGID_SCATTER_THREADS 256
+#define SPH_RIGID_BLOCKS 32     // reduction blocks per body
+#define SPH_RIGID_THREADS 256
 #define SPH_RIGID_Q 24          // reduced quantities per body
 #define SPH_RIGID_STRIDE 64     // doubles of state per body
 
