@@ -360,7 +360,7 @@ bool dispatch(Store *s, const char *name) {
     }
     if (mixed && k == "compute_deformations") {
         sph_launch_gather(L, false, false, true);
-        sph_launch_deformations_mixed(L);
+        sph_launch_deformations_mixed(L, false);
         return true;
     }
     if (mixed && k == "compute_forces_solids") {

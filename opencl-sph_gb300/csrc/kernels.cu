@@ -119,9 +119,9 @@ void sph_launch_original_density_mixed(const Launch &L) {
         L.scenes, L.pair_particles);
 }
 
-void sph_launch_deformations_mixed(const Launch &L) {
+void sph_launch_deformations_mixed(const Launch &L, bool masked) {
     k_deformations_mixed<<<grid_for(L.pair_particles, L.grid_cap), L.pair_block, 0, L.stream>>>(
-        L.scenes, L.pair_particles);
+        L.scenes, L.pair_particles, masked ? 1 : 0);
 }
 
 void sph_launch_forces_solids_mixed(const Launch &L) {
@@ -257,7 +257,7 @@ void sph_launch_substep(const Launch &L, SphMaterial mat, PhaseMark mark, void *
         phase("density");
         sph_launch_density(L, false, true, false);
         phase("deformations (solid phase)");
-        sph_launch_deformations_mixed(L);
+        sph_launch_deformations_mixed(L, true);
         phase("stresses (solid phase)");
         sph_launch_stresses(L, false);
         phase("forces_solids (solid phase)");

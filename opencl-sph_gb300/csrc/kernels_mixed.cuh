@@ -81,8 +81,12 @@ __device__ __forceinline__ void for_each_candidate_sorted(const SceneDesc &S, un
 // compute_deformations (solid_svk.cl:82-175) of a mixed scene's solid
 // particles over their solid neighbours: F = Apq Aqq^-1 with
 // Apq = sum W(|p|) p q^T and Aqq = sum W(|p|) q q^T over j != i, |p| <= h.
-// Needs the sorted copies gathered with the rest positions.
-__global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, BlockMap map) {
+// Needs the sorted copies gathered with the rest positions.  `masked` (a
+// fused substep, after the density pass of the same positions): walks the
+// density pass's candidate masks, which hold exactly the candidates with
+// |p| <= h, in candidate order, so the sums are those of the scan (which a
+// named call runs).
+__global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, BlockMap map, int masked) {
     SPH_FOR_WORK(map)
     if (!S.phase || !S.spos0) continue;
     if (item < active_count(S)) {
@@ -95,7 +99,7 @@ __global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, Block
             const float3 ipos0 = xyz(k0);
             float apq[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             float aqq[6] = {0, 0, 0, 0, 0, 0};
-            for_each_candidate_sorted(S, S.gridcell[i], [&](unsigned kk, float4 p4, float4 q4) {
+            auto visit = [&](unsigned kk, float4 p4, float4 q4) {
                 if (!solid_partner(q4, kk, k)) return;
                 const float3 p = sub3(xyz(p4), ipos);
                 const float r2 = norm2(p);
@@ -111,7 +115,12 @@ __global__ void k_deformations_mixed(const SceneDesc *__restrict__ scenes, Block
                 aqq[3] = __fmaf_rn(wq.x, q.y, aqq[3]);
                 aqq[4] = __fmaf_rn(wq.x, q.z, aqq[4]);
                 aqq[5] = __fmaf_rn(wq.y, q.z, aqq[5]);
-            });
+            };
+            if (masked && S.ncand[k] != SPH_NCAND_SCAN)
+                for_each_masked(S, k, StencilRows(S, S.gridcell[i]),
+                                [&](unsigned kk) { visit(kk, S.spos[kk], S.spos0[kk]); });
+            else
+                for_each_candidate_sorted(S, S.gridcell[i], visit);
             float inv[6];
             sym_inverse(aqq, inv);
             float F[9];

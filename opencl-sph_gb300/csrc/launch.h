@@ -87,7 +87,7 @@ void sph_launch_forces_solids(const Launch &L, bool corot, bool masked = false, 
 // elastic pair forces of the solid particles over their solid neighbours
 // (the force pass of fluids.cl then adds the fluid-solid pair terms).
 void sph_launch_original_density_mixed(const Launch &L);
-void sph_launch_deformations_mixed(const Launch &L);
+void sph_launch_deformations_mixed(const Launch &L, bool masked);
 void sph_launch_forces_solids_mixed(const Launch &L);
 
 void sph_launch_set_body_position(const Launch &L, unsigned body, const float pos[3]);
