@@ -675,9 +675,10 @@ __device__ __forceinline__ void scan_solid_rows(const SceneDesc &S, unsigned k, 
 // with |p| <= h and records the masks, R = polar(Apq), pass 2 sums D over
 // the masked candidates with |q| <= h.  Body particles keep their rotation and strain
 // (their masks are still recorded).  Also writes the sorted rotation copy.
-// At most 72 registers (96 unbounded; ~60 bytes spill to L1): seven
-// 128-thread blocks per SM; 80 gave six (0.640 -> 0.597 ms on batched-256).
-__global__ void __maxnreg__(72) k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map,
+// At most 64 registers (about 100 bytes spill to L1): eight 128-thread
+// blocks per SM.  On batched-256, with the packed distance tests: 64 ->
+// 0.581 ms, 72 -> 0.590 ms, 80 -> 0.626 ms.
+__global__ void __maxnreg__(64) k_rotations_and_strains(const SceneDesc *__restrict__ scenes, BlockMap map,
                                                         int with_density, int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
@@ -756,9 +757,9 @@ __global__ void __maxnreg__(72) k_rotations_and_strains(const SceneDesc *__restr
 }
 
 // compute_deformations (solid_svk.cl:82-175) for plane-free scenes, from
-// the sorted copies, recording the candidate masks.  At most 64 registers
-// (80 unbounded, no spills at 64): eight 128-thread blocks per SM.
-__global__ void __maxnreg__(64) k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density,
+// the sorted copies, recording the candidate masks.  No register cap (80):
+// on batched-256 uncapped 0.441 ms, 72 -> 0.446 ms, 64 -> 0.451 ms.
+__global__ void k_deformations(const SceneDesc *__restrict__ scenes, BlockMap map, int with_density,
                                int with_stress) {
     SPH_FOR_WORK(map)
     if (S.num_symmetry_planes || !S.spos0) continue;  // sorted copies exist with solids.cl
