@@ -359,12 +359,17 @@ __device__ __forceinline__ void load_planes(const SceneDesc &S, float3 ipos, flo
 }
 
 // Planes of the i-live set that j also passes (|n.(x_j - p)| in [1e-5, h]).
+// The reference tests (double)jd < 1.0e-5; jd converts to double exactly
+// and 1e-5 lies strictly between two floats, so the test holds iff jd <=
+// 0x1.4f8b58p-17f, the float just below it (FP32, no FP64 instruction per
+// candidate).
+#define SPH_PLANE_EPS_BELOW 0x1.4f8b58p-17f
 __device__ __forceinline__ unsigned plane_jmask(const Planes &P, float3 jpos, float h) {
     unsigned m = 0;
     for (unsigned k = 0; k < P.count; ++k) {
         if (!(P.imask & (1u << k))) continue;
         float jd = fabsf(dot3(P.n[k], sub3(jpos, P.p[k])));
-        if (!(jd > h) && !((double)jd < 1.0e-5)) m |= 1u << k;
+        if (!(jd > h) && !(jd <= SPH_PLANE_EPS_BELOW)) m |= 1u << k;
     }
     return m;
 }

@@ -189,12 +189,19 @@ __global__ void __launch_bounds__(512, 2)
 
 // APPLY_CUBE_BOUNDS(ipos, f, -2.0, 2.0) (common.cl:37-43): a repulsive
 // band 0.2 wide inside [-2, 2]^3; the bounds are double literals, so the
-// tests and the update are evaluated in double as in the source.
+// tests and the update are evaluated in double as in the source.  The tests
+// (double)p < -2 + (double)0.2f and (double)p > 2 - (double)0.2f run in FP32
+// without changing a result: p converts to double exactly, and the bounds
+// (-+1.7999999970197678) lie strictly between two floats, so they hold iff
+// p <= -0x1.cccccep+0 or p >= 0x1.cccccep+0, the floats just outside them.
+// Only a particle inside the band takes the double update; FP64 warp
+// instructions are slow on this part, and the test runs for every particle.
+#define SPH_CUBE_BAND_LO (-0x1.cccccep+0f)
+#define SPH_CUBE_BAND_HI (0x1.cccccep+0f)
 __device__ __forceinline__ float cube_bound(float p, float f) {
-    const double mn = -2.0, mx = 2.0, band = (double)0.2f;
-    double dp = (double)p;
-    if (dp < mn + band) return (float)((double)f + (1.0 / (-(mn) + dp) - 5.0));
-    if (dp > mx - band) return (float)((double)f - (1.0 / (mx - dp) - 5.0));
+    const double mn = -2.0, mx = 2.0;
+    if (p <= SPH_CUBE_BAND_LO) return (float)((double)f + (1.0 / (-(mn) + (double)p) - 5.0));
+    if (p >= SPH_CUBE_BAND_HI) return (float)((double)f - (1.0 / (mx - (double)p) - 5.0));
     return f;
 }
 

@@ -120,6 +120,30 @@ def test_forces_on_identical_inputs():
     ps.close()
 
 
+@pytest.mark.parametrize("box", [(-1.9, -1.5), (1.7, 2.1)])
+def test_forces_in_the_cube_band(box):
+    """APPLY_CUBE_BOUNDS (common.cl:37-43): a block straddling the band
+    0.2 inside -2 or 2 on every axis, so some particles take the band's
+    double-precision update and the others the plain force; the band's
+    tests run in FP32 against the floats just outside its bounds."""
+    sc = scenes.wcsph_block(12, 12, 12, box=box, jitter=1e-3, seed=7, walls=False)
+    pos = np.asarray(sc.init["position"][: sc.n])
+    inside = (pos <= -1.8000000715255737) | (pos >= 1.8000000715255737)
+    assert inside.any() and (~inside).any()
+    ps = sc.system()
+    orc = oracle_of(ps)
+    orc.call("compute_particle_bins")
+    orc.call("compute_density")
+    ps.compute_particle_bins()
+    ps.set_fields(density=orc.a["density"])
+    ps.call_for_all_particles("compute_forces_fluids")
+    orc.call("compute_forces_fluids")
+    ps.sync_device_to_host()
+    f = ps.get_fields("force")[0][: sc.n]
+    assert max_rel(f, orc.a["force"][: sc.n]) <= 1e-4
+    ps.close()
+
+
 @pytest.mark.parametrize("walls", [False, True])
 def test_trajectory_named_and_fused(walls):
     """N substeps through the reference's kernel names and through the
