@@ -10,7 +10,10 @@ properties that hold at any size:
   - each of the 256 scenes of the batched workload advanced inside the full
     batch equals itself advanced alone (bit for bit), and none raises a
     status bit;
-  - the rigid ball of the large scene keeps its shape.
+  - the rigid ball of the large scene keeps its shape;
+  - the interacting large scene (1M fluid, 32^3 SVK cube, rigid ball in one
+    store) gives the same bits through the named recipe (scans) and the
+    fused substeps (mask walks), and its ball stays rigid.
 """
 import os
 
@@ -121,3 +124,34 @@ def test_large_scene_ball_stays_rigid():
     assert np.max(np.abs(x1 - x0)) > 1e-7  # it moved
     assert ps.status() == 0
     ps.close()
+
+
+def test_large_interacting_scene_named_equals_fused():
+    sc = scenes.large_fluid_solid_scene(seed=0)
+    a, b = sc.system(), sc.system()
+    for ps in (a, b):
+        ps.call_for_all_particles("init_original_position")
+        ps.compute_particle_bins()
+        ps.call_for_all_particles("compute_original_density")
+    steps = 5
+    a.update_fused(steps)
+    for _ in range(steps):
+        b.compute_particle_bins()
+        for k in ("compute_density", "compute_deformations", "compute_stresses", "compute_forces_solids",
+                  "compute_forces_fluids", "step_forward"):
+            b.call_for_all_particles(k)
+    a.sync_device_to_host()
+    b.sync_device_to_host()
+    n = sc.n
+    for f in ("position", "velocity", "force", "deformation", "density"):
+        assert np.array_equal(a.get_fields(f)[0][:n], b.get_fields(f)[0][:n]), f
+    body = np.asarray(sc.init["body_number"])[:n] == 1
+    x0 = np.asarray(sc.init["position"], dtype=np.float64)[:n][body]
+    x1 = a.get_fields("position")[0][:n][body].astype(np.float64)
+    sub = np.random.default_rng(1).choice(len(x0), size=min(600, len(x0)), replace=False)
+    d0 = np.sqrt((((x0[sub][:, None] - x0[sub][None]) ** 2).sum(-1)))
+    d1 = np.sqrt((((x1[sub][:, None] - x1[sub][None]) ** 2).sum(-1)))
+    assert np.max(np.abs(d1 - d0)) <= 2e-6
+    assert a.status() == 0 and b.status() == 0
+    a.close()
+    b.close()
