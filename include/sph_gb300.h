@@ -355,6 +355,11 @@ int sph_batch_wait_read(sph_batch *batch, long long ticket);
  * Returns a non-negative count of writes so far, or -1. */
 int sph_batch_write_field_many_async(sph_batch *batch, const int *ids, unsigned int count, const char *field,
                                      psdata *const *ins);
+/* The same for fields[0 .. nfields) at once: one staging buffer, one
+ * host-to-device copy and one scatter kernel for every field of every
+ * scene (a controller's per-substep inputs, e.g. time step and gravity). */
+int sph_batch_write_fields_many_async(sph_batch *batch, const int *ids, unsigned int count, unsigned int nfields,
+                                      const char *const *fields, psdata *const *ins);
 /* Waits for every read enqueued so far. */
 int sph_batch_wait_reads(sph_batch *batch);
 /* Runs `reps` substeps of the batch as individual launches with CUDA events

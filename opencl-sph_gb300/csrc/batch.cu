@@ -697,8 +697,10 @@ extern "C" long long sph_batch_read_field_many_async(sph_batch *b, const int *id
         const size_t off = out->data_offsets[f], sz = out->data_sizes[f];
         segs[k] = CopySeg{sc->mem + off, nullptr, (unsigned long long)sz};
         dst[k] = sc->host + off;
-        at[k] = total;
-        total += (sz + 15) / 16 * 16;
+        // the snapshot copy at the field's offset within 16 bytes, so that
+        // the copy kernel moves 16-byte words (the buffer is 256-aligned)
+        at[k] = total + ((uintptr_t)(sc->mem + off) & 15u);
+        total = (at[k] + sz + 15) / 16 * 16;
         if (sz > max_bytes) max_bytes = sz;
     }
     const int t = (int)(b->tickets & 1);
@@ -773,11 +775,13 @@ static bool write_allowed(const BatchScene *sc, const char *field, const char *w
     return true;
 }
 
-extern "C" int sph_batch_write_field_many_async(sph_batch *b, const int *ids, unsigned int count, const char *field,
-                                                psdata *const *ins) {
-    const char *what = "sph_batch_write_field_many_async";
-    if (!b || !count || !ids || !ins || !field) {
-        sph_set_error("%s: no batch, ids, stores or field", what);
+// Writes fields[0 .. nfields) of the scenes ids[0 .. count) from their host
+// stores: one staging buffer, one host-to-device copy and one scatter for
+// all of them.
+static int write_many(sph_batch *b, const int *ids, unsigned count, const char *const *fields, unsigned nfields,
+                      psdata *const *ins, const char *what) {
+    if (!b || !count || !ids || !ins || !fields || !nfields) {
+        sph_set_error("%s: no batch, ids, stores or fields", what);
         return -1;
     }
     if (!b->write_done[0]) {
@@ -785,29 +789,38 @@ extern "C" int sph_batch_write_field_many_async(sph_batch *b, const int *ids, un
             if (!ok(cudaEventCreateWithFlags(&b->write_done[t], cudaEventDisableTiming), what)) return -1;
     }
     // layout of a turn's staging buffer: the segment table, then each
-    // scene's bytes at a 16-byte aligned offset
-    std::vector<CopySeg> segs(count);
-    std::vector<const char *> src(count);
-    std::vector<size_t> at(count);
-    const size_t table = (count * sizeof(CopySeg) + 255) / 256 * 256;
+    // scene's bytes of each field at a 16-byte aligned offset
+    const size_t nseg = (size_t)count * nfields;
+    std::vector<CopySeg> segs(nseg);
+    std::vector<const char *> src(nseg);
+    std::vector<size_t> at(nseg);
+    const size_t table = (nseg * sizeof(CopySeg) + 255) / 256 * 256;
     size_t total = table;
     unsigned long long max_bytes = 0;
-    for (unsigned k = 0; k < count; ++k) {
-        BatchScene *sc = scene_of(b, ids[k], what);
-        if (!sc) return -1;
-        const psdata *in = ins[k];
-        const int f = in ? get_field_psdata(*in, field) : -1;
-        if (f < 0 || psdata_data_size(*in) != sc->blob_size) {
-            sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field);
+    for (unsigned q = 0; q < nfields; ++q) {
+        const char *field = fields[q];
+        if (!field) {
+            sph_set_error("%s: no field name", what);
             return -1;
         }
-        if (!write_allowed(sc, field, what, ids[k])) return -1;
-        const size_t off = in->data_offsets[f], sz = in->data_sizes[f];
-        segs[k] = CopySeg{nullptr, sc->mem + off, (unsigned long long)sz};
-        src[k] = static_cast<const char *>(in->data) + off;
-        at[k] = total;
-        total += (sz + 15) / 16 * 16;
-        if (sz > max_bytes) max_bytes = sz;
+        for (unsigned k = 0; k < count; ++k) {
+            BatchScene *sc = scene_of(b, ids[k], what);
+            if (!sc) return -1;
+            const psdata *in = ins[k];
+            const int f = in ? get_field_psdata(*in, field) : -1;
+            if (f < 0 || psdata_data_size(*in) != sc->blob_size) {
+                sph_set_error("%s: no field '%s' in a store of the scene's layout", what, field);
+                return -1;
+            }
+            if (!write_allowed(sc, field, what, ids[k])) return -1;
+            const size_t off = in->data_offsets[f], sz = in->data_sizes[f];
+            const size_t j = (size_t)q * count + k;
+            segs[j] = CopySeg{nullptr, sc->mem + off, (unsigned long long)sz};
+            src[j] = static_cast<const char *>(in->data) + off;
+            at[j] = total;
+            total += (sz + 15) / 16 * 16;
+            if (sz > max_bytes) max_bytes = sz;
+        }
     }
     const int t = (int)(b->wtickets & 1);
     // turn t's staging buffer is free once its copy two writes back is done
@@ -822,19 +835,30 @@ extern "C" int sph_batch_write_field_many_async(sph_batch *b, const int *ids, un
     }
     if (!grow(b, &b->wstage_dev[t], &b->wstage_dev_cap[t], total, b->stream, what)) return -1;
     char *dev = b->wstage_dev[t];
-    for (unsigned k = 0; k < count; ++k) {
-        segs[k].src = dev + at[k];
-        memcpy(b->wstage_host[t] + at[k], src[k], (size_t)segs[k].bytes);
+    for (size_t j = 0; j < nseg; ++j) {
+        segs[j].src = dev + at[j];
+        memcpy(b->wstage_host[t] + at[j], src[j], (size_t)segs[j].bytes);
     }
-    memcpy(b->wstage_host[t], segs.data(), count * sizeof(CopySeg));
+    memcpy(b->wstage_host[t], segs.data(), nseg * sizeof(CopySeg));
     // one host-to-device copy of the table and the bytes, in stream order
     // before the substeps enqueued after this call, then the scatter
     if (!ok(cudaMemcpyAsync(dev, b->wstage_host[t], total, cudaMemcpyHostToDevice, b->stream), what) ||
         !ok(cudaEventRecord(b->write_done[t], b->stream), what))
         return -1;
-    sph_launch_copy_segments(reinterpret_cast<const CopySeg *>(dev), count, max_bytes, b->stream);
+    sph_launch_copy_segments(reinterpret_cast<const CopySeg *>(dev), (unsigned)nseg, max_bytes, b->stream);
     if (sph_check_launch(what) != cudaSuccess) return -1;
     return (int)(b->wtickets++ & 0x7fffffff);
+}
+
+extern "C" int sph_batch_write_field_many_async(sph_batch *b, const int *ids, unsigned int count, const char *field,
+                                                psdata *const *ins) {
+    return write_many(b, ids, count, &field, 1, ins, "sph_batch_write_field_many_async");
+}
+
+extern "C" int sph_batch_write_fields_many_async(sph_batch *b, const int *ids, unsigned int count,
+                                                 unsigned int nfields, const char *const *fields,
+                                                 psdata *const *ins) {
+    return write_many(b, ids, count, fields, nfields, ins, "sph_batch_write_fields_many_async");
 }
 
 extern "C" int sph_batch_wait_read(sph_batch *b, long long ticket) {

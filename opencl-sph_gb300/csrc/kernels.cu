@@ -366,12 +366,17 @@ __global__ void k_copy_segments(const CopySeg *__restrict__ segs, unsigned first
     const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uintptr_t align = (uintptr_t)g.src | (uintptr_t)g.dst;
     size_t done = 0;
-    if (align % 16 == 0) {
-        const size_t n = g.bytes / 16;
-        const uint4 *s = reinterpret_cast<const uint4 *>(g.src);
-        uint4 *d = reinterpret_cast<uint4 *>(g.dst);
+    if ((((uintptr_t)g.src ^ (uintptr_t)g.dst) & 15u) == 0) {
+        // source and destination at the same offset within 16 bytes: the
+        // bytes up to the first 16-byte boundary, 16-byte words, the tail
+        size_t head = (16u - ((uintptr_t)g.src & 15u)) & 15u;
+        if (head > g.bytes) head = g.bytes;
+        for (size_t c = t0; c < head; c += stride) g.dst[c] = g.src[c];
+        const size_t n = (g.bytes - head) / 16;
+        const uint4 *s = reinterpret_cast<const uint4 *>(g.src + head);
+        uint4 *d = reinterpret_cast<uint4 *>(g.dst + head);
         for (size_t w = t0; w < n; w += stride) d[w] = s[w];
-        done = n * 16;
+        done = head + n * 16;
     } else if (align % 4 == 0) {
         const size_t n = g.bytes / 4;
         const unsigned *s = reinterpret_cast<const unsigned *>(g.src);

@@ -164,13 +164,20 @@ class Batch(object):
             raise bnd.SphError(bnd.last_error())
         return t
 
-    def write_fields_async(self, sids, name):
-        """Enqueues a write of one field of several scenes from their host
-        stores (one host-to-device copy and one scatter kernel), in stream
-        order before the substeps enqueued next; the host stores may change
-        as soon as this returns."""
+    def write_fields_async(self, sids, *names):
+        """Enqueues a write of the named fields of several scenes from their
+        host stores (one host-to-device copy and one scatter kernel for all
+        of them), in stream order before the substeps enqueued next; the
+        host stores may change as soon as this returns."""
+        if not names:
+            raise ValueError("no field to write")
         key, ids, outs = self._read_args(sids)
-        if bnd.sph_batch_write_field_many_async(self.handle, ids, len(key), name, outs) < 0:
+        if len(names) == 1:
+            rc = bnd.sph_batch_write_field_many_async(self.handle, ids, len(key), names[0], outs)
+        else:
+            arr = (ctypes.c_char_p * len(names))(*[n.encode() for n in names])
+            rc = bnd.sph_batch_write_fields_many_async(self.handle, ids, len(key), len(names), arr, outs)
+        if rc < 0:
             raise bnd.SphError(bnd.last_error())
 
     def wait_read(self, ticket):

@@ -240,6 +240,8 @@ _SIGS = {
     "sph_batch_wait_read": ([c_void_p, ctypes.c_longlong], c_int),
     "sph_batch_write_field_many_async": ([c_void_p, POINTER(c_int), c_uint, String, POINTER(POINTER(psdata))],
                                          c_int),
+    "sph_batch_write_fields_many_async": ([c_void_p, POINTER(c_int), c_uint, c_uint, POINTER(c_char_p),
+                                           POINTER(POINTER(psdata))], c_int),
     "sph_batch_wait_reads": ([c_void_p], c_int),
     "sph_batch_profile": ([c_void_p, c_uint, POINTER(c_float), POINTER(c_char_p), c_uint], c_int),
     "sph_batch_bytes": ([c_void_p], c_size_t),

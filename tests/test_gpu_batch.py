@@ -336,7 +336,7 @@ def test_empty_store_fused_substeps():
 
 
 def test_batched_writes_equal_host_uploads():
-    """sph_batch_write_field_many_async: per-substep inputs (each scene's
+    """sph_batch_write_field_many_async and its several-field form: per-substep inputs (each scene's
     time step and gravity changed before every substep) give the results of
     the same scenes run alone with the same values uploaded through the
     drop-in's blocking sync; bad writes are refused."""
@@ -351,8 +351,12 @@ def test_batched_writes_equal_host_uploads():
             v = b.scenes[sid].views
             v["timestep"][...] = dts[s.name][k]
             v["gravity"][...] = gs[s.name][k]
-        b.write_fields_async(ids, "timestep")
-        b.write_fields_async(ids, "gravity")
+        if k % 2:
+            # both fields in one call (sph_batch_write_fields_many_async)
+            b.write_fields_async(ids, "timestep", "gravity")
+        else:
+            b.write_fields_async(ids, "timestep")
+            b.write_fields_async(ids, "gravity")
         # the stores may change at once: the next write overwrites them
         for sid in ids:
             b.scenes[sid].views["timestep"][...] = -1.0
@@ -360,6 +364,8 @@ def test_batched_writes_equal_host_uploads():
     got = {s.name: np.array(b.read(sid)["position"][: s.n]) for s, sid in zip(scs, ids)}
     with pytest.raises(Exception, match="gridres"):
         b.write_fields_async(ids[:1], "gridres")
+    with pytest.raises(Exception, match="gridres"):
+        b.write_fields_async(ids[:1], "timestep", "gridres")
     b.close()
     for s in scs:
         ps = s.system()
