@@ -89,8 +89,10 @@ struct Store {
     char *rec_mem = nullptr;
     RecordPlan rec{};
     std::vector<std::string> rec_fields;
-    // sph_pin_host: the host blob, page-locked by this store
+    // sph_pin_host: the host blob, page-locked by this store, and its
+    // device-side address (mapped), or null
     void *pinned = nullptr;
+    char *pinned_dev = nullptr;
     // sph_read_fields_async: reads take turns over two snapshot buffers;
     // the stream `reads` copies a snapshot into the host store while later
     // substeps run on `stream`
@@ -650,8 +652,11 @@ extern "C" int sph_pin_host(psdata data, psdata_cuda pso) {
         sph_set_error("%s: another host store is pinned for this device store (sph_unpin_host first)", what);
         return -1;
     }
-    if (!cuda_ok(cudaHostRegister(data.data, s->blob_size, cudaHostRegisterDefault), what)) return -1;
+    if (!cuda_ok(cudaHostRegister(data.data, s->blob_size, cudaHostRegisterMapped), what)) return -1;
     s->pinned = data.data;
+    void *dev = nullptr;
+    s->pinned_dev = cudaHostGetDevicePointer(&dev, data.data, 0) == cudaSuccess ? static_cast<char *>(dev) : nullptr;
+    cudaGetLastError();  // a store without a device-side address keeps the copy-engine writes
     return 0;
 }
 
@@ -664,6 +669,7 @@ extern "C" int sph_unpin_host(psdata_cuda pso) {
     if (!cuda_ok(cudaStreamSynchronize(s->stream), what) || !drain_reads(s, what)) return -1;
     void *p = s->pinned;
     s->pinned = nullptr;
+    s->pinned_dev = nullptr;
     return cuda_ok(cudaHostUnregister(p), what) ? 0 : -1;
 }
 
@@ -677,9 +683,27 @@ extern "C" int sph_write_fields_async(psdata data, psdata_cuda pso, size_t num_f
     }
     if (names_shape(names, num_fields) && !shape_unchanged(s, data, what)) return -1;
     bool rigid = false;
+    // a pinned store's few small fields go by one copy kernel reading the
+    // mapped host store (no copy engine: see InlineSegs), others by copies
+    InlineSegs inl{};
+    size_t inl_bytes = 0;
+    const bool inline_ok = s->pinned == data.data && s->pinned_dev && num_fields <= SPH_INLINE_SEGS;
     for (size_t i = 0; i < num_fields; ++i) {
-        if (names[i] && !copy_field(s, data, names[i], true)) return -1;
-        rigid = rigid || (names[i] && touches_rigid_setup(names[i]));
+        if (!names[i]) continue;
+        rigid = rigid || touches_rigid_setup(names[i]);
+        const int f = get_field_psdata(data, names[i]);
+        if (inline_ok && f >= 0 && data.data_offsets[f] + data.data_sizes[f] <= s->blob_size &&
+            inl_bytes + data.data_sizes[f] <= 65536) {
+            const size_t off = data.data_offsets[f], sz = data.data_sizes[f];
+            inl.seg[inl.count++] = CopySeg{s->pinned_dev + off, s->d_blob + off, (unsigned long long)sz};
+            inl_bytes += sz;
+            continue;
+        }
+        if (!copy_field(s, data, names[i], true)) return -1;
+    }
+    if (inl.count) {
+        sph_launch_copy_inline(inl, s->stream);
+        if (sph_check_launch(what) != cudaSuccess) return -1;
     }
     if (rigid && s->desc.rigid_state) {
         if (!refresh_rigid(s, data)) return -1;

@@ -387,6 +387,25 @@ __global__ void k_copy_segments(const CopySeg *__restrict__ segs, unsigned first
     for (size_t c = done + t0; c < g.bytes; c += stride) g.dst[c] = g.src[c];
 }
 
+// One block copies a few small segments, in 4-byte words where both ends
+// are 4-byte aligned, else bytes.
+__global__ void k_copy_inline(InlineSegs segs) {
+    for (unsigned q = 0; q < segs.count && q < SPH_INLINE_SEGS; ++q) {
+        const CopySeg g = segs.seg[q];
+        if ((((uintptr_t)g.src | (uintptr_t)g.dst | (uintptr_t)g.bytes) & 3u) == 0) {
+            const unsigned *s = reinterpret_cast<const unsigned *>(g.src);
+            unsigned *d = reinterpret_cast<unsigned *>(g.dst);
+            for (size_t w = threadIdx.x; w < g.bytes / 4; w += blockDim.x) d[w] = s[w];
+        } else {
+            for (size_t c = threadIdx.x; c < g.bytes; c += blockDim.x) g.dst[c] = g.src[c];
+        }
+    }
+}
+
+void sph_launch_copy_inline(const InlineSegs &segs, cudaStream_t stream) {
+    k_copy_inline<<<1, 256, 0, stream>>>(segs);
+}
+
 void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long long max_bytes,
                               cudaStream_t stream) {
     const unsigned long long per_block = 256ull * 16 * 4;  // four 16-byte words per thread

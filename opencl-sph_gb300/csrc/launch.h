@@ -137,6 +137,16 @@ struct CopySeg {
     char *dst;
     unsigned long long bytes;
 };
+// A few segments passed by value (no table to upload first): a store's
+// small per-substep writes, read by the kernel from the mapped pinned host
+// store, so they take no copy engine (a host-to-device copy would queue
+// behind the device-to-host copies of the reads in flight).
+#define SPH_INLINE_SEGS 8
+struct InlineSegs {
+    CopySeg seg[SPH_INLINE_SEGS];
+    unsigned count;
+};
+void sph_launch_copy_inline(const InlineSegs &segs, cudaStream_t stream);
 // Copies segs[0 .. count) (a device table) in one launch per 65,535
 // segments; `max_bytes` is the largest segment.
 void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long long max_bytes,

@@ -288,8 +288,11 @@ def test_async_store_transfers_match_blocking_syncs():
     b.update_fused(4)
     for ps in (a, b):
         ps.get_fields("gravity")[0][:] = (0.5, -3.0, 0.25)
-    a.write_fields_async("gravity")
-    b.sync_fields_host_to_device("gravity")
+        ps.get_fields("timestep")[0][:] = 0.9 * ps.get_fields("timestep")[0]
+    # (a pinned store's small fields go by one copy kernel reading the
+    # mapped host store)
+    a.write_fields_async("gravity", "timestep")
+    b.sync_fields_host_to_device("gravity", "timestep")
     prev = None
     for _ in range(5):
         a.update_fused(1)
