@@ -554,8 +554,8 @@ def bench_batched(args, torch, world):
             "e2e": {"value": n * args.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": 12 * n,
                     "host_memory": "pinned (sph_batch_pin_host; a page-locked staging buffer for the writes)",
-                    "writes": "per step: every scene's time step and gravity from its host store, one staged "
-                              "host-to-device copy and one scatter kernel for both fields "
+                    "writes": "per step: every scene's time step and gravity from its host store, staged in "
+                              "page-locked memory and scattered into the scenes by one kernel that reads it "
                               "(sph_batch_write_fields_many_async)",
                     "reads": "per step: device snapshot of every scene's positions, written to the host stores "
                              "beside the next substep (sph_batch_read_field_many_async); step s - 1's positions "

@@ -348,8 +348,8 @@ int sph_batch_wait_read(sph_batch *batch, long long ticket);
  * store ins[k] is copied into scene ids[k], in stream order before the
  * substeps enqueued after this call.  The bytes are taken from the stores
  * during the call (into a page-locked staging buffer), so the stores may
- * change as soon as it returns; one host-to-device copy and one scatter
- * kernel carry every scene's bytes.  gridres and pnum cannot be written
+ * change as soon as it returns; one scatter kernel, reading the staging
+ * buffer over the host link, carries every scene's bytes.  gridres and pnum cannot be written
  * (they size the scene's tables), nor, in a scene with rigid bodies, the
  * fields the bodies are set up from (position, velocity, n, body tables).
  * Returns a non-negative count of writes so far, or -1. */

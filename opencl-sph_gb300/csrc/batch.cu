@@ -833,20 +833,32 @@ static int write_many(sph_batch *b, const int *ids, unsigned count, const char *
         if (!ok(cudaMallocHost((void **)&b->wstage_host[t], c), what)) return -1;
         b->wstage_host_cap[t] = c;
     }
-    if (!grow(b, &b->wstage_dev[t], &b->wstage_dev_cap[t], total, b->stream, what)) return -1;
-    char *dev = b->wstage_dev[t];
+    // the scatter reads the page-locked staging buffer where it lies (its
+    // device-side address), so the write takes no copy engine and does not
+    // queue behind the device-to-host copies of reads in flight; without
+    // such an address, one host-to-device copy into a device buffer first
+    void *mapped = nullptr;
+    char *dev = cudaHostGetDevicePointer(&mapped, b->wstage_host[t], 0) == cudaSuccess
+                    ? static_cast<char *>(mapped)
+                    : nullptr;
+    cudaGetLastError();
+    const bool zero_copy = dev != nullptr;
+    if (!zero_copy) {
+        if (!grow(b, &b->wstage_dev[t], &b->wstage_dev_cap[t], total, b->stream, what)) return -1;
+        dev = b->wstage_dev[t];
+    }
     for (size_t j = 0; j < nseg; ++j) {
         segs[j].src = dev + at[j];
         memcpy(b->wstage_host[t] + at[j], src[j], (size_t)segs[j].bytes);
     }
     memcpy(b->wstage_host[t], segs.data(), nseg * sizeof(CopySeg));
-    // one host-to-device copy of the table and the bytes, in stream order
-    // before the substeps enqueued after this call, then the scatter
-    if (!ok(cudaMemcpyAsync(dev, b->wstage_host[t], total, cudaMemcpyHostToDevice, b->stream), what) ||
-        !ok(cudaEventRecord(b->write_done[t], b->stream), what))
+    // in stream order before the substeps enqueued after this call
+    if (!zero_copy && !ok(cudaMemcpyAsync(dev, b->wstage_host[t], total, cudaMemcpyHostToDevice, b->stream), what))
         return -1;
     sph_launch_copy_segments(reinterpret_cast<const CopySeg *>(dev), (unsigned)nseg, max_bytes, b->stream);
-    if (sph_check_launch(what) != cudaSuccess) return -1;
+    // the staging buffer is free again once the scatter (or the copy) has
+    // read it
+    if (sph_check_launch(what) != cudaSuccess || !ok(cudaEventRecord(b->write_done[t], b->stream), what)) return -1;
     return (int)(b->wtickets++ & 0x7fffffff);
 }
 
