@@ -4,7 +4,8 @@
 // Pair passes run one thread per cell-sorted particle k (i =
 // cellparticles[k]) so a warp covers a few neighbouring cells and shares
 // their neighbour rows in L1; neighbours are streamed from the float4
-// copies built by k_gather.  Sums are Kahan-compensated FP32.
+// copies built by k_gather.  Sums are FP32, blocked per stencil row: a
+// row's terms added in order, the nine row sums with Kahan compensation.
 #pragma once
 
 #include "kernels_common.cuh"

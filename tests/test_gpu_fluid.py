@@ -6,7 +6,8 @@ on the same store.  Tolerances:
   - integer and index outputs (gridcell, gridcount, celloffset,
     cellparticles, num_neighbours): bit-exact;
   - density: max |d| <= 1e-5 of max |rho| (poly6 evaluated from r^2 and
-    summed with Kahan compensation, the oracle sums pow() terms plainly);
+    summed per stencil row with the row sums Kahan-compensated, the oracle
+    sums pow() terms plainly);
   - forces: max |d| <= 1e-4 of max |f| on identical inputs;
   - positions after N substeps: relative L2 error <= 1e-5.
 """
