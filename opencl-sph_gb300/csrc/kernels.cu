@@ -375,6 +375,7 @@ __global__ void k_copy_segments(const CopySeg *__restrict__ segs, unsigned first
         const size_t n = (g.bytes - head) / 16;
         const uint4 *s = reinterpret_cast<const uint4 *>(g.src + head);
         uint4 *d = reinterpret_cast<uint4 *>(g.dst + head);
+#pragma unroll 4
         for (size_t w = t0; w < n; w += stride) d[w] = s[w];
         done = head + n * 16;
     } else if (align % 4 == 0) {
@@ -408,7 +409,10 @@ void sph_launch_copy_inline(const InlineSegs &segs, cudaStream_t stream) {
 
 void sph_launch_copy_segments(const CopySeg *segs, unsigned count, unsigned long long max_bytes,
                               cudaStream_t stream) {
-    const unsigned long long per_block = 256ull * 16 * 4;  // four 16-byte words per thread
+    // 64 KB per block (sixteen 16-byte words per thread, four in flight):
+    // a segment's blocks share gridDim.x, so the large segments' count
+    // sets it and the small segments' extra blocks exit at once
+    const unsigned long long per_block = 256ull * 16 * 16;
     unsigned gx = (unsigned)((max_bytes + per_block - 1) / per_block);
     gx = gx < 1 ? 1 : gx > 256 ? 256 : gx;
     for (unsigned first = 0; first < count; first += 65535u) {
