@@ -652,7 +652,12 @@ extern "C" int sph_pin_host(psdata data, psdata_cuda pso) {
         sph_set_error("%s: another host store is pinned for this device store (sph_unpin_host first)", what);
         return -1;
     }
-    if (!cuda_ok(cudaHostRegister(data.data, s->blob_size, cudaHostRegisterMapped), what)) return -1;
+    // mapped, so that small writes can be read in place by a kernel; a
+    // device that cannot map host memory gets the plain page-locking
+    if (cudaHostRegister(data.data, s->blob_size, cudaHostRegisterMapped) != cudaSuccess) {
+        cudaGetLastError();
+        if (!cuda_ok(cudaHostRegister(data.data, s->blob_size, cudaHostRegisterDefault), what)) return -1;
+    }
     s->pinned = data.data;
     void *dev = nullptr;
     s->pinned_dev = cudaHostGetDevicePointer(&dev, data.data, 0) == cudaSuccess ? static_cast<char *>(dev) : nullptr;
