@@ -93,6 +93,12 @@ struct Store {
     // device-side address (mapped), or null
     void *pinned = nullptr;
     char *pinned_dev = nullptr;
+    // calls through the store's entry points, and the call that recorded
+    // the candidate masks in a named compute_density (0: none): a named
+    // compute_forces_fluids that comes right after it, with no other call
+    // between, finds the positions, velocities, densities and cell tables
+    // the masks were recorded from, and walks them
+    unsigned long long calls = 0, mask_call = 0;
     // sph_read_fields_async: reads take turns over two snapshot buffers;
     // the stream `reads` copies a snapshot into the host store while later
     // substeps run on `stream`
@@ -119,6 +125,7 @@ Store *store_of(const psdata_cuda &pso, const char *what) {
         sph_set_error("%s: not a live device store (created by create_psdata_cuda and not freed)", what);
         return nullptr;
     }
+    ++s->calls;
     return s;
 }
 
@@ -328,6 +335,15 @@ bool dispatch(Store *s, const char *name) {
     if (k == "copy_celloffset_to_backup") return true;
     if (k == "insert_particles_in_bin_array") { sph_launch_insert(L); return true; }
     if (k == "compute_density") {
+        if ((P & PROG_FLUIDS) && !s->desc.phase && s->desc.nbmask) {
+            // a fluid store: the masked pass (with the count), after a
+            // gather of positions and velocities, so that the next call may
+            // be the masked force pass
+            sph_launch_gather(L, true, false);
+            sph_launch_density(L, false, true, false, true);
+            s->mask_call = s->calls;
+            return true;
+        }
         sph_launch_gather(L, false, false);
         sph_launch_density(L, false);
         return true;
@@ -339,6 +355,13 @@ bool dispatch(Store *s, const char *name) {
     }
     if (k == "compute_forces_fluids") {
         if (!need(PROG_FLUIDS, "fluids")) return false;
+        if (s->mask_call && s->calls == s->mask_call + 1) {
+            // right after the masked compute_density: its sorted copies,
+            // pressures, reciprocal densities and masks are current; the
+            // walk gives the scan's bits (and the same neighbour count)
+            sph_launch_forces_fluids(L, false, true);
+            return true;
+        }
         sph_launch_gather(L, true, true);
         sph_launch_forces_fluids(L, false);
         return true;

@@ -23,8 +23,12 @@ cudaError_t sph_prepare_kernels() {
     size_t want = density_smem_bytes(1024);
     if (max_optin > 0 && want > (size_t)max_optin) want = (size_t)max_optin;
     cudaError_t e = cudaFuncSetAttribute(k_density<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_density<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_density<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_density<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)want);
     return e;
 }
 
@@ -80,14 +84,18 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid) {
                                                                           dens ? 1 : 0, solid ? 1 : 0);
 }
 
-void sph_launch_density(const Launch &L, bool original, bool mask, bool skip_solids) {
+void sph_launch_density(const Launch &L, bool original, bool mask, bool skip_solids, bool count) {
     const size_t smem = density_smem_bytes(L.pair_block);
     const unsigned g = grid_for(L.pair_particles, L.grid_cap);
-    k_density<false><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0, mask ? 1 : 0,
-                                                          skip_solids ? 1 : 0);
-    if (!L.no_symmetry_planes)
-        k_density<true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, original ? 1 : 0,
-                                                             mask ? 1 : 0, 0);
+    const int o = original ? 1 : 0, m = mask ? 1 : 0, sk = skip_solids ? 1 : 0;
+    if (mask && count) {
+        k_density<false, true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, o, m, sk);
+        if (!L.no_symmetry_planes)
+            k_density<true, true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, o, m, 0);
+        return;
+    }
+    k_density<false><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, o, m, sk);
+    if (!L.no_symmetry_planes) k_density<true><<<g, L.pair_block, smem, L.stream>>>(L.scenes, L.pair_particles, o, m, 0);
 }
 
 void sph_launch_density_fused(const Launch &L, const Launch *fluids) {

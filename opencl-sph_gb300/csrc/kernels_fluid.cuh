@@ -50,7 +50,9 @@ __device__ __forceinline__ float fluid_pressure(float rho, float rho0, float sti
     return __fmul_rn(__fsub_rn(rho, rho0), stiff);
 }
 
-template <bool PLANES, bool MASK>
+// COUNT: a masked pass that also counts num_neighbours (a named
+// compute_density, whose caller may read the count before the force pass).
+template <bool PLANES, bool MASK, bool COUNT = false>
 __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsigned item, unsigned lane,
                                             float4 *__restrict__ wstage, int original) {
     const bool active = item < n;
@@ -96,7 +98,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
                 const float d = fmaxf(h2 - r2, 0.f);
                 rowsum = __fadd_rn(rowsum, d * d * d);
                 // a fused plane-free substep counts in the force pass
-                if (!MASK || PLANES) count += r2 <= B.lt;
+                if (!MASK || PLANES || COUNT) count += r2 <= B.lt;
                 if (MASK && word) *word |= 1u << bit;
             }
             if (PLANES && P.imask) {
@@ -146,7 +148,7 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
             S.density0[i] = value;
         } else {
             S.density[i] = value;
-            if (!MASK || PLANES) S.num_neighbours[i] = count;
+            if (!MASK || PLANES || COUNT) S.num_neighbours[i] = count;
             S.sdens[k] = value;
         }
         if (MASK) {
@@ -169,8 +171,10 @@ __device__ __forceinline__ void density_one(const SceneDesc &S, unsigned n, unsi
 
 // Two instantiations, each skipping the other's scenes: the plane variant
 // (launched only when some scene has symmetry planes) keeps the common
-// plane-free loop free of its registers.
-template <bool PLANES>
+// plane-free loop free of its registers.  COUNT: the masked pass counts
+// num_neighbours too (a named compute_density recording masks); a kernel
+// of its own, so the fused substep's keeps its register allocation.
+template <bool PLANES, bool COUNT = false>
 __global__ void __launch_bounds__(512, 2)
     k_density(const SceneDesc *__restrict__ scenes, BlockMap map, int original, int want_mask, int skip_solids) {
     extern __shared__ float4 sm_stage[];
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(512, 2)
     if (skip_solids && !PLANES && (S.programs & (PROG_COROT | PROG_SVK))) continue;
     const unsigned n = active_count(S);
     if (want_mask && S.nbmask && (S.programs & PROG_FLUIDS) && !original)
-        density_one<PLANES, true>(S, n, item, lane, wstage, original);
+        density_one<PLANES, true, COUNT>(S, n, item, lane, wstage, original);
     else
         density_one<PLANES, false>(S, n, item, lane, wstage, original);
     SPH_END_WORK

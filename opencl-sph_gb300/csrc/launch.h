@@ -58,7 +58,10 @@ void sph_launch_gather(const Launch &L, bool vel, bool dens, bool solid = false)
 
 // skip_solids: a fused substep, where a plane-free solid's first solid pass
 // sums its density
-void sph_launch_density(const Launch &L, bool original, bool mask = false, bool skip_solids = false);
+// mask: record the candidate masks (fused substeps); count: count
+// num_neighbours in the masked pass too (a named compute_density)
+void sph_launch_density(const Launch &L, bool original, bool mask = false, bool skip_solids = false,
+                        bool count = false);
 // The fused batched density: the plane-free instantiation over `fluids`'
 // pair map only (plane-free solids sum their density in their first solid
 // pass), the plane instantiation over every scene of L when some has

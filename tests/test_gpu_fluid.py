@@ -145,6 +145,44 @@ def test_forces_in_the_cube_band(box):
     ps.close()
 
 
+@pytest.mark.parametrize("planes", [False, True])
+def test_named_forces_walk_masks_only_right_after_density(planes):
+    """A named compute_forces_fluids called right after a named
+    compute_density walks the masks that pass recorded; with any call in
+    between (here a status query) it scans.  Both give the same bits, and
+    the count the density pass left is the force pass's."""
+    sc = scenes.wcsph_block(12, 10, 12, jitter=1e-3, seed=12)
+    if planes:
+        # mirror planes through the box corner, normals along the axes
+        sc.entries = [("symmetry_planes", "3, 2, 3", "float", None) if e[0] == "symmetry_planes" else e
+                      for e in sc.entries]
+        sp = np.zeros((3, 2, 3), np.float32)
+        for k in range(3):
+            sp[k, 1, k] = 1.0
+        sc.init = dict(sc.init, symmetry_planes=sp)
+    a, b = sc.system(), sc.system()
+    rng = np.random.default_rng(3)
+    vel = rng.normal(0, 0.05, size=(sc.n, 3)).astype(np.float32)
+    for ps in (a, b):
+        ps.set_fields(velocity=vel)
+        ps.compute_particle_bins()
+        ps.call_for_all_particles("compute_density")
+    a.call_for_all_particles("compute_forces_fluids")  # the masked walk
+    assert b.status() == 0  # a call in between: the scan
+    b.call_for_all_particles("compute_forces_fluids")
+    a.sync_device_to_host()
+    b.sync_device_to_host()
+    n = sc.n
+    for f in ("force", "density", "num_neighbours"):
+        assert np.array_equal(a.get_fields(f)[0][:n], b.get_fields(f)[0][:n]), f
+    orc = oracle_of(b)
+    orc.call("compute_particle_bins")
+    orc.call("compute_density")
+    assert np.array_equal(a.get_fields("num_neighbours")[0][:n], orc.a["num_neighbours"][:n])
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("walls", [False, True])
 def test_trajectory_named_and_fused(walls):
     """N substeps through the reference's kernel names and through the
