@@ -99,6 +99,11 @@ struct Store {
     // between, finds the positions, velocities, densities and cell tables
     // the masks were recorded from, and walks them
     unsigned long long calls = 0, mask_call = 0;
+    // the same for the solid recipe: the call of a named first solid pass
+    // (which records its masks), and of a compute_stresses right after it
+    // (which then writes the sorted stress copies): a compute_forces_solids
+    // right after that walks the masks from the sorted copies
+    unsigned long long solid_call = 0, stress_call = 0;
     // sph_read_fields_async: reads take turns over two snapshot buffers;
     // the stream `reads` copies a snapshot into the host store while later
     // substeps run on `stream`
@@ -397,21 +402,38 @@ bool dispatch(Store *s, const char *name) {
         if (!need(PROG_COROT, "solid_corotation")) return false;
         sph_launch_gather(L, false, false, true);
         sph_launch_rotations_and_strains(L);
+        s->solid_call = s->desc.sstress ? s->calls : 0;
         return true;
     }
     if (k == "compute_deformations") {
         if (!need(PROG_SVK, "solid_svk")) return false;
         sph_launch_gather(L, false, false, true);
         sph_launch_deformations(L);
+        s->solid_call = s->desc.sstress ? s->calls : 0;
         return true;
     }
     if (k == "compute_stresses") {
         if (!need(PROG_COROT | PROG_SVK, "solid_corotation or solid_svk")) return false;
+        if (s->solid_call && s->calls == s->solid_call + 1) {
+            // right after the first solid pass: the stress law writes the
+            // sorted copies too (same field values), for the masked walk
+            sph_launch_stresses(L, (P & PROG_COROT) != 0, true, false);
+            s->stress_call = s->calls;
+            return true;
+        }
         sph_launch_stresses(L, (P & PROG_COROT) != 0);
         return true;
     }
     if (k == "compute_forces_solids") {
         if (!need(PROG_COROT | PROG_SVK, "solid_corotation or solid_svk")) return false;
+        if (s->stress_call && s->calls == s->stress_call + 1) {
+            // right after that compute_stresses: the positions, velocities,
+            // rest positions and masks of the first pass and the sorted
+            // stresses are current; the walk gives the scan's bits (scenes
+            // with symmetry planes scan, as in a fused substep)
+            sph_launch_forces_solids(L, (P & PROG_COROT) != 0, true, false);
+            return true;
+        }
         sph_launch_gather(L, false, false);
         sph_launch_forces_solids(L, (P & PROG_COROT) != 0);
         return true;

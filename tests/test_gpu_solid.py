@@ -142,6 +142,37 @@ def test_solid_trajectory(material, planes):
     ps2.close()
 
 
+@pytest.mark.parametrize("planes", [False, True])
+@pytest.mark.parametrize("material", ["corot", "svk"])
+def test_named_solid_forces_walk_masks_only_in_the_recipe_chain(material, planes):
+    """compute_forces_solids called right after compute_stresses, itself
+    right after the first solid pass (the reference drivers' order), walks
+    the first pass's masks over the sorted copies; with any call in between
+    it scans the fields.  Both give the same bits."""
+    sc, a = _solid(material, planes, seed=9, jitter=1e-4)
+    _, b = _solid(material, planes, seed=9, jitter=1e-4)
+    first = MATERIAL[material][0]
+    for ps in (a, b):
+        ps.call_for_all_particles("init_original_position")
+        ps.compute_particle_bins()
+        ps.call_for_all_particles("compute_original_density")
+        ps.update_fused(3)  # a deformed state
+        ps.compute_particle_bins()
+        ps.call_for_all_particles("compute_density")
+        ps.call_for_all_particles(first)
+        ps.call_for_all_particles("compute_stresses")
+    a.call_for_all_particles("compute_forces_solids")  # the masked walk
+    assert b.status() == 0  # a call in between: the scan
+    b.call_for_all_particles("compute_forces_solids")
+    a.sync_device_to_host()
+    b.sync_device_to_host()
+    n = sc.n
+    for f in ("force", "force_elastic", "force_viscous", "cutoff_force", "stress"):
+        assert np.array_equal(a.get_fields(f)[0][:n], b.get_fields(f)[0][:n]), f
+    a.close()
+    b.close()
+
+
 def test_plane_constraints():
     sc = scenes.solid_lattice(6, 6, 6, material="corot", jitter=1e-3, seed=2)
     sc.entries = [("plane_constraints", "3, 2, 4", "float", None) if e[0] == "plane_constraints" else e
