@@ -34,7 +34,7 @@ def _rank(rank, world, port, out):
 
 def test_replica_aggregation_two_ranks():
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()
     out = mgr.dict()
     mp.start_processes(_rank, args=(2, port, out), nprocs=2, start_method="spawn", join=True)
     for r in (0, 1):
