@@ -39,7 +39,16 @@ def init_data_from_string(spec, kernel_files):
 
 
 def init_data_from_dict(config):
-    pass
+    """As init_data, from a dict keyed by the .conf section names
+    (``psdata_specification``, ``opencl_kernel_files``); a section may be
+    its text or a list of its lines.  The reference declares this function
+    with an empty body (scripts/sph/__init__.py:25-26)."""
+    def section(name):
+        if name not in config:
+            raise KeyError("init_data_from_dict: config lacks the [{}] section".format(name))
+        text = config[name]
+        return text if isinstance(text, str) else "\n".join(text)
+    return init_data_from_string(section("psdata_specification"), section("opencl_kernel_files"))
 
 
 def free_data(psdata, psdata_opencl):

@@ -115,3 +115,20 @@ def test_host_fields():
     assert bnd.get_host_field_psdata(ctypes.byref(ps), "other") == -1
     del buf
     free_data_cpu(ps)
+
+
+def test_init_data_from_dict(monkeypatch):
+    import sph
+    spec = LAYOUTS["scene/wcsph"]["spec"]
+    seen = []
+    # the device store needs a GPU: record the kernel-file section instead
+    monkeypatch.setattr(sph, "init_data_opencl", lambda ps, files: seen.append(files) or "device")
+    for form in (spec, spec.splitlines()):
+        ps, dev = sph.init_data_from_dict({"psdata_specification": form, "opencl_kernel_files": "common, fluids"})
+        assert dev == "device" and seen[-1] == "common, fluids"
+        ref = init_data_cpu(spec)
+        assert layout_of(ps) == layout_of(ref)
+        free_data_cpu(ps)
+        free_data_cpu(ref)
+    with pytest.raises(KeyError):
+        sph.init_data_from_dict({"psdata_specification": spec})
