@@ -256,7 +256,8 @@ class FluidSystem(ParticleSystem):
     config = os.path.join(_CONF_DIR, "fluid.conf")
 
     def setup(self):
-        pass
+        """A fluid keeps no rest state (no original positions or rest
+        densities), so there is nothing to set up before update()."""
 
     def update(self):
         bnd.compute_particle_bins_device_opencl(self.psdata_opencl)
