@@ -1,0 +1,181 @@
+"""The store builder against the reference's own builder on seeded random
+specifications (CPU).
+
+Each specification is drawn from the grammar that src/build_psdata.c parses
+(create_psdata_field_spec, build_psdata.c:183-313): a line per field,
+`name | dims | type | defaults`, dimensions given as numbers (strtol base
+0: decimal, hex, octal) or as the name of an earlier unsigned scalar,
+every type spelling of src/stringly.c (char, unsigned int / uint, int,
+float / float32, double / float64), default values in the spellings
+strtol/strtof/strtod accept, comment and blank lines, and irregular
+spacing.  Both builders make the store; names, dimensions, entry sizes,
+data sizes, offsets (including the first field's wrapped alignment,
+build_psdata.c:381), field types, the grid arrays and every byte of the
+data blob must agree.
+
+Specifications stay inside what the reference defines: the three grid
+fields are present with one float type (build_psdata.c:43-84 dereferences
+and asserts them), a named dimension refers to a scalar that has a value
+(get_value reads its data), a multi-dimensional field's first dimension is
+not zero (its alignment divides by it), and default values either cover
+the whole field or are absent (a partial list makes the reference copy
+past its buffer).
+
+Runs where oracle/_ref/libref_psdata.so was built from the reference's
+sources; skipped elsewhere.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import ref
+from sph import bindings as bnd
+
+pytestmark = pytest.mark.skipif(not ref.available("psdata"), reason="reference builder not built")
+
+SIZES = {"char": 1, "unsigned int": 4, "uint": 4, "int": 4, "float": 4, "float32": 4, "double": 8, "float64": 8}
+PARSED = {"unsigned int", "int", "float", "double"}  # types whose default values the reference reads
+N_SPECS = 2000
+
+
+def _int_text(rng, v):
+    form = rng.integers(4)
+    if form == 0 and v >= 0:
+        return hex(v)
+    if form == 1 and 0 <= v < 4096:
+        return "0" + oct(v)[2:] if v else "0"
+    return str(v)
+
+
+def _value_text(rng, t):
+    if t in ("float", "double"):
+        x = float(rng.standard_normal() * 10.0 ** int(rng.integers(-8, 9)))
+        form = rng.integers(5)
+        if form == 0:
+            return repr(x)
+        if form == 1:
+            return "%.4e" % x
+        if form == 2:
+            return str(int(rng.integers(-300, 300)))
+        if form == 3:
+            return "0x1.8p%d" % int(rng.integers(-20, 20))
+        return "%.9g" % x
+    if t == "int":
+        return _int_text(rng, int(rng.integers(-2 ** 31, 2 ** 31)))
+    # unsigned int: strtol, then the conversion to unsigned
+    v = int(rng.integers(-50, 2 ** 32)) if rng.integers(4) else int(rng.integers(-50, 50))
+    return _int_text(rng, v)
+
+
+def _type_text(rng, t):
+    if t == "unsigned int" and rng.integers(3) == 0:
+        return "unsigned   int"
+    return t
+
+
+def _line(rng, parts):
+    sep = [" | ", "|", " |  ", "  | "][int(rng.integers(4))]
+    return sep.join(parts)
+
+
+def random_spec(rng):
+    """One specification: pnum first, then the other fields in drawn order
+    with smoothingradius and gridbounds placed among them."""
+    real = "double" if rng.integers(3) == 0 else "float"
+    pnum = int(rng.integers(1, 65))
+    h = float(np.float32(rng.uniform(0.02, 0.5)))
+    lo = [float(np.float32(rng.uniform(-2.0, 0.0))) for _ in range(3)]
+    hi = [float(np.float32(lo[d] + h * rng.uniform(1.5, 30.0))) for d in range(3)]
+    bounds = ", ".join("%r, %r" % (lo[d], hi[d]) for d in range(3))
+    lines = [_line(rng, ["pnum", "1", _type_text(rng, "unsigned int"), _int_text(rng, pnum)])]
+    scalars = {"pnum": pnum}  # unsigned scalars with values: usable as dimensions by name
+    for f in range(int(rng.integers(0, 10))):
+        name = "f%d_%d" % (f, int(rng.integers(1000)))
+        if rng.integers(4) == 0:
+            v = int(rng.integers(0, 7))
+            scalars[name] = v
+            lines.append(_line(rng, [name, "1", "unsigned int", str(v)]))
+            continue
+        t = list(SIZES)[int(rng.integers(len(SIZES)))]
+        ndim = int(rng.integers(1, 5))
+        dims, words = [], []
+        for d in range(ndim):
+            choice = rng.integers(5)
+            # a multi-dimensional field's first dimension may not be zero
+            may_be_zero = d > 0 or ndim == 1
+            known = [k for k in scalars if may_be_zero or scalars[k] > 0]
+            if choice == 0 and known:
+                k = known[int(rng.integers(len(known)))]
+                dims.append(scalars[k])
+                words.append(k)
+            elif choice == 1 and may_be_zero:
+                dims.append(0)  # a name no earlier field has: dimension 0
+                words.append("nosuch%d" % f)
+            else:
+                v = int(rng.integers(1, 7))
+                dims.append(v)
+                words.append(_int_text(rng, v))
+        entries = int(np.prod(dims))
+        parts = [name, (", " if rng.integers(2) else ",").join(words), _type_text(rng, t)]
+        if t in PARSED and entries * SIZES[t] <= 256 and rng.integers(3):
+            room = 256 // SIZES[t] - entries  # values past the field's end are read and dropped
+            n_vals = entries + int(rng.integers(0, room // 4 + 1))
+            parts.append(", ".join(_value_text(rng, t) for _ in range(n_vals)))
+        elif t not in PARSED and rng.integers(2):
+            parts.append("1, 2, 3")  # the reference reads no defaults for this spelling
+        lines.append(_line(rng, parts))
+    for g in (_line(rng, ["smoothingradius", "1", real, repr(h)]),
+              _line(rng, ["gridbounds", "2, 3" if rng.integers(2) else "2,3", real, bounds])):
+        lines.insert(int(rng.integers(1, len(lines) + 1)), g)
+    out = []
+    for ln in lines:
+        if rng.integers(8) == 0:
+            out.append("# a comment | 3 | float")
+        if rng.integers(8) == 0:
+            out.append("")
+        out.append(ln)
+    return "\n".join(out) + ("\n" if rng.integers(2) else "")
+
+
+def _layout(ps):
+    nf = ps.num_fields
+    dims = []
+    for f in range(nf):
+        o = ps.dimensions_offsets[f]
+        dims.append([ps.dimensions[o + d] for d in range(ps.num_dimensions[f])])
+    return {"entry_sizes": [ps.entry_sizes[f] for f in range(nf)],
+            "data_sizes": [ps.data_sizes[f] for f in range(nf)],
+            "data_offsets": [ps.data_offsets[f] for f in range(nf)], "dims": dims}
+
+
+def _types(data_ptrs, n, stride):
+    base = ctypes.cast(data_ptrs, ctypes.c_void_p).value
+    return [ctypes.c_int.from_address(base + f * stride).value for f in range(n)]
+
+
+def _blob(ptr, size):
+    return ctypes.string_at(ptr, size) if size else b""
+
+
+@pytest.mark.parametrize("block", range(4))
+def test_builder_equals_reference_builder_on_random_specs(block):
+    rng = np.random.default_rng(1000 + block)
+    stride = ctypes.sizeof(bnd.DataPtr)
+    for case in range(N_SPECS // 4):
+        spec = random_spec(rng)
+        rs = ref.RefStore(spec)
+        ps = bnd.psdata()
+        bnd.build_psdata_from_string(ctypes.byref(ps), spec.encode())
+        try:
+            assert bnd.field_names(ps) == rs.layout["names"], spec
+            got = _layout(ps)
+            for k in ("entry_sizes", "data_sizes", "data_offsets", "dims"):
+                assert got[k] == rs.layout[k], (k, spec)
+            n = ps.num_fields
+            assert _types(ps.data_ptrs, n, stride) == _types(rs.ps.data_ptrs, n, stride), spec
+            assert bnd.psdata_data_size(ps) == rs.size, spec
+            assert _blob(ps.data, rs.size) == _blob(rs.ps.data, rs.size), spec
+        finally:
+            bnd.free_psdata(ctypes.byref(ps))
+            rs.free()
