@@ -20,6 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -477,12 +478,42 @@ extern "C" void free_psdata(psdata *d) {
 }
 
 // ---------------------------------------------------------------------------
-// config sections (src/config.c:19-106): `$heading` lines split the file;
-// text before the first `$` is ignored; at most 8 sections.
+// config sections (src/config.c:19-106).  A file splits into `$title` lines,
+// each followed by its section's text up to the next `$`.  The reference
+// cuts the file with the C library's tokenizer, and its rules decide what a
+// malformed file gives, so the same rules are kept here (take() below):
+//   - text before the first `$` is skipped;
+//   - a title is the run after `$` up to the end of its line; a `$` at the
+//     very start of the file keeps any newlines right after it as the
+//     title's start, elsewhere empty lines before a title are skipped;
+//   - a section's text runs to the next `$`, skipping `$`s in front of it,
+//     so a section with no text takes the next `$title` line and text as
+//     its own;
+//   - a title with no text after it is dropped;
+//   - at most 8 sections are kept, counted across loads until
+//     unload_config (a second load_config adds to the first's sections and
+//     a title found in both returns the first's text).
 
 namespace {
-std::string g_config;
-std::vector<std::pair<std::string, size_t>> g_sections;  // title, content offset
+// The files read since the last unload_config, split in place; the
+// sections point into them.
+std::vector<std::unique_ptr<std::string>> g_conf_files;
+std::vector<std::pair<const char *, const char *>> g_sections;  // title, text
+
+// The next token of the text at *at: skip characters of `seps`, take the
+// run up to the next one, end it in place with a NUL and move *at past it.
+// nullptr when only separators are left.
+char *take(char **at, const char *seps) {
+    char *q = *at + strspn(*at, seps);
+    if (!*q) {
+        *at = q;
+        return nullptr;
+    }
+    char *e = q + strcspn(q, seps);
+    if (*e) *e++ = '\0';
+    *at = e;
+    return q;
+}
 }  // namespace
 
 extern "C" int load_config(const char *path) {
@@ -494,39 +525,36 @@ extern "C" int load_config(const char *path) {
     fseek(f, 0, SEEK_END);
     long end = ftell(f);
     fseek(f, 0, SEEK_SET);
-    std::string s((size_t)(end > 0 ? end : 0), '\0');
-    if (end > 0 && fread(&s[0], 1, (size_t)end, f) != (size_t)end) s.clear();
+    auto text = std::make_unique<std::string>((size_t)(end > 0 ? end : 0), '\0');
+    if (end > 0 && fread(&(*text)[0], 1, (size_t)end, f) != (size_t)end) text->clear();
     fclose(f);
-    g_sections.clear();
-    // Each section is `$title\ncontent` and runs to the next `$`; content is
-    // stored NUL-terminated in g_config so get_config_section can return it.
-    g_config.clear();
-    size_t pos = s.find('$');
-    while (pos != std::string::npos && g_sections.size() < 8) {
-        size_t nl = s.find('\n', pos + 1);
-        if (nl == std::string::npos) break;  // a title with no content is dropped
-        std::string title = s.substr(pos + 1, nl - pos - 1);
-        size_t next = s.find('$', nl + 1);
-        std::string content = s.substr(nl + 1, (next == std::string::npos ? s.size() : next) - nl - 1);
-        if (title.empty() || content.empty()) {
-            pos = next;
-            continue;
-        }
-        g_sections.push_back({title, g_config.size()});
-        g_config += content;
-        g_config += '\0';
-        pos = next;
+    g_conf_files.push_back(std::move(text));
+    char *buf = &(*g_conf_files.back())[0];  // NUL-terminated by std::string
+    char *at = buf, *title;
+    if (buf[0] == '$') {
+        at = buf + 1;
+        take(&at, "\n");
+        title = buf + 1;
+    } else {
+        take(&at, "$");
+        title = take(&at, "\n");
+    }
+    while (title && g_sections.size() < 8) {
+        char *body = take(&at, "$");
+        if (!body) break;
+        g_sections.emplace_back(title, body);
+        title = take(&at, "\n");
     }
     return 0;
 }
 
 extern "C" const char *get_config_section(const char *heading) {
     for (auto &s : g_sections)
-        if (s.first == heading) return g_config.data() + s.second;
+        if (!strcmp(s.first, heading)) return s.second;
     return nullptr;
 }
 
 extern "C" void unload_config(void) {
-    g_config.clear();
     g_sections.clear();
+    g_conf_files.clear();
 }
