@@ -11,7 +11,9 @@ strtol/strtof/strtod accept, comment and blank lines, and irregular
 spacing.  Both builders make the store; names, dimensions, entry sizes,
 data sizes, offsets (including the first field's wrapped alignment,
 build_psdata.c:381), field types, the grid arrays and every byte of the
-data blob must agree.
+data blob must agree, and so must the store's queries and writes
+(src/particle_system.c:84-112: get_field_psdata, set_field_psdata,
+psdata_names_size, psdata_dimensions_size, psdata_data_size).
 
 Specifications stay inside what the reference defines: the three grid
 fields are present with one float type (build_psdata.c:43-84 dereferences
@@ -158,10 +160,24 @@ def _blob(ptr, size):
     return ctypes.string_at(ptr, size) if size else b""
 
 
+def reference_store_functions():
+    lib = ref.psdata_lib()
+    for fn in ("psdata_names_size", "psdata_dimensions_size"):
+        getattr(lib, fn).argtypes = [ref.psdata]
+        getattr(lib, fn).restype = ctypes.c_uint
+    lib.get_field_psdata.argtypes = [ref.psdata, ctypes.c_char_p]
+    lib.get_field_psdata.restype = ctypes.c_int
+    lib.set_field_psdata.argtypes = [ctypes.POINTER(ref.psdata), ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint,
+                                     ctypes.c_uint]
+    lib.set_field_psdata.restype = None
+    return lib
+
+
 @pytest.mark.parametrize("block", range(4))
 def test_builder_equals_reference_builder_on_random_specs(block):
     rng = np.random.default_rng(1000 + block)
     stride = ctypes.sizeof(bnd.DataPtr)
+    lib = reference_store_functions()
     for case in range(N_SPECS // 4):
         spec = random_spec(rng)
         rs = ref.RefStore(spec)
@@ -175,6 +191,26 @@ def test_builder_equals_reference_builder_on_random_specs(block):
             n = ps.num_fields
             assert _types(ps.data_ptrs, n, stride) == _types(rs.ps.data_ptrs, n, stride), spec
             assert bnd.psdata_data_size(ps) == rs.size, spec
+            assert _blob(ps.data, rs.size) == _blob(rs.ps.data, rs.size), spec
+            for fn in ("psdata_names_size", "psdata_dimensions_size"):
+                assert getattr(bnd, fn)(ps) == getattr(lib, fn)(rs.ps), (fn, spec)
+            names = rs.layout["names"]
+            for name in names + ["nosuch", "", names[0] + "x"]:
+                assert bnd.get_field_psdata(ps, name) == lib.get_field_psdata(rs.ps, name.encode()), (name, spec)
+            # set_field_psdata: bytes at an offset inside a field (the
+            # reference checks only the name)
+            for _ in range(4):
+                f = int(rng.integers(len(names)))
+                ds = rs.layout["data_sizes"][f]
+                if ds == 0:
+                    continue
+                off = int(rng.integers(ds))
+                size = int(rng.integers(1, ds - off + 1))
+                src = ctypes.create_string_buffer(bytes(rng.integers(0, 256, size, dtype=np.uint8)), size)
+                bnd.set_field_psdata(ctypes.byref(ps), names[f], ctypes.addressof(src), size, off)
+                lib.set_field_psdata(ctypes.byref(rs.ps), names[f].encode(), ctypes.addressof(src), size, off)
+            bnd.set_field_psdata(ctypes.byref(ps), "nosuch", ctypes.addressof(src), 1, 0)
+            lib.set_field_psdata(ctypes.byref(rs.ps), b"nosuch", ctypes.addressof(src), 1, 0)
             assert _blob(ps.data, rs.size) == _blob(rs.ps.data, rs.size), spec
         finally:
             bnd.free_psdata(ctypes.byref(ps))
