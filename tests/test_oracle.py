@@ -217,3 +217,67 @@ def test_oracle_reproduces_reference_scene_builders(prec):
         for a, ang in enumerate(g["angles"]):
             orc.rotate_particles(*ang)
             assert np.array_equal(orc.a["position"], g[pre + "rotate%d/position" % a]), (c, a)
+
+
+SOLID_OUT = {"corot": ["rotation", "strain", "stress", "apq_temp"], "svk": ["deformation", "stress"]}
+
+
+@pytest.mark.parametrize("mat", ["corot", "svk"])
+@pytest.mark.parametrize("with_planes", [False, True])
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_oracle_matches_compiled_reference_live_solids(mat, with_planes, prec):
+    """Seeded solid lattices of random shape, stiffness and jitter, deformed
+    after their set-up, three substeps in the oracle (guards off) and in
+    the reference's compiled kernels: in FP32 every field equal bit for
+    bit; in FP64 the integer fields equal and the others as the golden
+    files are checked (the reference's double build keeps its float
+    literals, e.g. PI = 3.1415926535f, common.cl:15, in the kernel
+    normalisations, so density0 differs by 3e-8 relative)."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("oracle/_ref not built on this machine")
+    rng = np.random.default_rng({"corot": 11, "svk": 12}[mat] + 2 * with_planes + (prec == "f64"))
+    for case in range(2):
+        dims = [int(x) for x in rng.integers(3, 7, 3)]
+        sc = scenes.solid_lattice(*dims, material=mat, youngs_modulus=float(rng.uniform(1e4, 1e5)),
+                                  poisson=float(rng.uniform(0.2, 0.45)), jitter=float(rng.uniform(0, 1e-3)),
+                                  clamp_layers=int(rng.integers(1, 3)), seed=int(rng.integers(1000)))
+        if with_planes:
+            sc.entries = [("symmetry_planes", "3, 2, 2", "float", None) if e[0] == "symmetry_planes" else e
+                          for e in sc.entries]
+        if prec == "f64":
+            sc = sc.to_double()
+        vel = rng.normal(0, 0.01, (sc.n, 3))
+        ps, v = host_store(sc, velocity=vel)
+        if with_planes:
+            planes = np.zeros((2, 2, 3))
+            planes[0, 1, 0] = 1.0                       # x = 0, normal +x
+            planes[1, 0, 1], planes[1, 1, 1] = 0.01, 1.0  # y = 0.01, normal +y
+            v["symmetry_planes"][...] = planes
+        orc = OracleScene(v, prec, guards=0)
+        rs = ref.RefStore(sc.spec)
+        for k in list(sc.init) + ["velocity"] + (["symmetry_planes"] if with_planes else []):
+            rs.view(k)[...] = v[k]
+        n = sc.n
+        orc.setup_solid()
+        for k in ("init_original_position", "compute_particle_bins", "compute_original_density"):
+            rs.call(mat, prec, k, n)
+        kick = rng.normal(0, 5e-4, (n, 3)).astype(orc.T)
+        orc.a["position"][:n] += kick
+        rs.view("position")[:n] += kick
+        recipe = ["compute_density", "compute_rotations_and_strains" if mat == "corot" else "compute_deformations",
+                  "compute_stresses", "compute_forces_solids", "step_forward"]
+        for _ in range(3):
+            orc.substep(mat)
+            rs.call(mat, prec, "compute_particle_bins", n)
+            for k in recipe:
+                rs.call(mat, prec, k, n)
+        for k in ["position", "velocity", "density", "density0", "force", "num_neighbours", "cellparticles",
+                  "gridcell"] + SOLID_OUT[mat]:
+            want = rs.view(k)[:n]
+            if prec == "f32" or want.dtype.kind in "ui":
+                assert np.array_equal(orc.a[k][:n].reshape(want.shape), want), (k, case)
+            else:
+                check(orc.a[k][:n], want, k)
+        rs.free()
+        free_data_cpu(ps)
