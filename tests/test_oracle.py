@@ -281,3 +281,63 @@ def test_oracle_matches_compiled_reference_live_solids(mat, with_planes, prec):
                 check(orc.a[k][:n], want, k)
         rs.free()
         free_data_cpu(ps)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_oracle_bodies_and_constraints_live(prec):
+    """set_body_position, set_body_rotation (rigidbody.cl) and
+    apply_plane_constraints (constraints.cl) on seeded random scenes --
+    three kinematic bodies with random members (particle 0 in a body or
+    not), poses, moves and rotations; two random constraint planes with
+    random particle masks -- in the oracle (guards off) and in the
+    reference's compiled kernels: equal bit for bit in FP32, as the golden
+    files are checked in FP64."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("oracle/_ref not built on this machine")
+    rng = np.random.default_rng(31 + (prec == "f64"))
+    for case in range(4):
+        sc = scenes.solid_lattice(*[int(x) for x in rng.integers(3, 6, 3)], material="corot", clamp_layers=0,
+                                  seed=int(rng.integers(1000)), jitter=1e-3)
+        sc.entries = [("body_count", "1", "unsigned int", 3) if e[0] == "body_count" else
+                      (("plane_constraints", "3, 2, 2", "float", None) if e[0] == "plane_constraints" else e)
+                      for e in sc.entries]
+        if prec == "f64":
+            sc = sc.to_double()
+        n = sc.n
+        members = rng.integers(0, 4, n).astype(np.uint32)
+        members[0] = int(rng.integers(0, 4))
+        pc = np.zeros((2, 2, 3))
+        pc[:, 0] = rng.uniform(0.0, 0.03, (2, 3))
+        nrm = rng.normal(size=(2, 3))
+        pc[:, 1] = nrm / np.linalg.norm(nrm, axis=1, keepdims=True)
+        values = {"body_number": members, "body_dynamic": np.zeros(3, np.uint32),
+                  "velocity": rng.normal(0, 0.1, (n, 3)), "plane_constraints": pc,
+                  "plane_constraints_particles": rng.integers(0, 4, n).astype(np.uint32),
+                  "body_position": rng.uniform(0, 0.05, (3, 3)),
+                  "body_euler_rotation": rng.uniform(-1, 1, (3, 3)),
+                  "rotation": np.tile(np.eye(3), (n, 1, 1))}
+        ps, v = host_store(sc, **values)
+        orc = OracleScene(v, prec, guards=0)
+        rs = ref.RefStore(sc.spec)
+        for k in list(sc.init) + list(values):
+            rs.view(k)[...] = v[k]
+        for step in range(3):
+            body = int(rng.integers(0, 3))
+            move = rng.uniform(-0.02, 0.02, 3)
+            orc.set_body_position(body, move)
+            rs.call("corot", prec, "set_body_position", n, body=body, vec=tuple(move.astype(orc.T)))
+            euler = rng.uniform(-np.pi, np.pi, 3)
+            orc.set_body_rotation(body, euler)
+            rs.call("corot", prec, "set_body_rotation", n, body=body, vec=tuple(euler.astype(orc.T)))
+            orc.call("apply_plane_constraints")
+            rs.call("corot", prec, "apply_plane_constraints", n)
+            for k in ("position", "velocity", "rotation", "body_position", "body_euler_rotation"):
+                want = rs.view(k)
+                got = orc.a[k][: want.shape[0]].reshape(want.shape)
+                if prec == "f32":
+                    assert np.array_equal(got, want), (k, case, step)
+                else:
+                    check(got, want, k)
+        rs.free()
+        free_data_cpu(ps)
