@@ -341,3 +341,45 @@ def test_oracle_bodies_and_constraints_live(prec):
                     check(got, want, k)
         rs.free()
         free_data_cpu(ps)
+
+
+def test_oracle_matches_compiled_reference_live_fluid_edges():
+    """Seeded fluid scenes with the cases the neighbour search must get
+    right: a dense cluster (stencil rows of more than 64 candidates),
+    particles past the grid's upper bounds (clamped into edge cells) and
+    n < pnum (the tail ignored); three substeps in the oracle (guards off)
+    and in the reference's compiled kernels, FP32, equal bit for bit."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("oracle/_ref not built on this machine")
+    rng = np.random.default_rng(41)
+    for case in range(3):
+        sc = scenes.wcsph_block(10, 6, 5, jitter=0.0, seed=0, walls=False)  # pnum 300, grid [0, 0.4]^3, h 0.02
+        P = sc.n
+        pos = np.empty((P, 3))
+        pos[:200] = rng.uniform(0.05, 0.2, (200, 3))
+        centre = rng.uniform(0.08, 0.15, 3)
+        d = rng.normal(size=(80, 3))
+        pos[200:280] = centre + 0.012 * d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(0.1, 1, (80, 1))
+        pos[280:] = rng.uniform(0.38, 0.47, (20, 3))
+        n = P - int(rng.integers(0, 15))
+        # the cluster's particles start with more than 64 neighbours each
+        r = np.linalg.norm(pos[200:280, None] - pos[None, 200:280], axis=2)
+        assert (r < 0.02).sum(axis=1).min() > 64
+        ps, v = host_store(sc, position=pos, n=n, velocity=rng.normal(0, 0.05, (P, 3)))
+        orc = OracleScene(v, "f32", guards=0)
+        rs = ref.RefStore(sc.spec)
+        for k in ("position", "n", "velocity"):
+            rs.view(k)[...] = v[k]
+        for _ in range(3):
+            orc.substep("fluid")
+            rs.call("fluid", "f32", "compute_particle_bins", P)
+            for k in ("compute_density", "compute_forces_fluids", "step_forward"):
+                rs.call("fluid", "f32", k, P)
+        for k in ("position", "velocity", "density", "force", "num_neighbours", "gridcell", "cellparticles"):
+            want = rs.view(k)[:n]
+            assert np.array_equal(orc.a[k][:n].reshape(want.shape), want), (k, case)
+        for k in ("gridcount", "celloffset"):
+            assert np.array_equal(orc.a[k], rs.view(k).reshape(-1)), (k, case)
+        rs.free()
+        free_data_cpu(ps)
