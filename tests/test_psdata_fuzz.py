@@ -215,3 +215,47 @@ def test_builder_equals_reference_builder_on_random_specs(block):
         finally:
             bnd.free_psdata(ctypes.byref(ps))
             rs.free()
+
+
+def _printed(call):
+    """What `call` writes to the process's standard output (C stdio)."""
+    import os
+    import sys
+    import tempfile
+    libc = ctypes.CDLL(None)
+    sys.stdout.flush()
+    libc.fflush(None)
+    with tempfile.TemporaryFile() as tmp:
+        saved = os.dup(1)
+        os.dup2(tmp.fileno(), 1)
+        try:
+            call()
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        tmp.seek(0)
+        return tmp.read()
+
+
+def test_display_psdata_prints_what_the_reference_prints():
+    """display_psdata (particle_system.c:38-82): the same text for every
+    field of seeded random stores (8-byte entries as %g, 4-byte ones as
+    their bits with %u, 1-byte ones not at all; fields of more than three
+    dimensions print their name only)."""
+    lib = ref.psdata_lib()
+    lib.display_psdata.argtypes = [ref.psdata, ctypes.c_void_p]
+    lib.display_psdata.restype = None
+    rng = np.random.default_rng(77)
+    for case in range(100):
+        spec = random_spec(rng)
+        rs = ref.RefStore(spec)
+        ps = bnd.psdata()
+        bnd.build_psdata_from_string(ctypes.byref(ps), spec.encode())
+        try:
+            want = _printed(lambda: lib.display_psdata(rs.ps, None))
+            got = _printed(lambda: bnd.display_psdata(ps, None))
+            assert want and got == want, spec
+        finally:
+            bnd.free_psdata(ctypes.byref(ps))
+            rs.free()
