@@ -797,10 +797,11 @@ def _fill(view, val):
         view[...] = arr
 
 
-def cpu_sample(scene, material, steps, nthreads, reference):
+def cpu_sample(scene, material, steps, nthreads, reference, warmup=1):
     """Times the CPU oracle (or, with `reference`, the reference's own
     kernels in a store the reference's own builder made) on `steps`
-    substeps of the scene; returns (particle-steps, seconds, kind)."""
+    substeps of the scene, after `warmup` untimed ones (at least one);
+    returns (particle-steps, seconds, kind)."""
     kind = "port"
     if reference:
         from oracle import ref
@@ -844,7 +845,8 @@ def cpu_sample(scene, material, steps, nthreads, reference):
 
         def closer():
             free_data_cpu(ps)
-    one()  # warm
+    for _ in range(max(1, warmup)):
+        one()
     t0 = time.perf_counter()
     for _ in range(steps):
         one()
@@ -983,8 +985,9 @@ def run_ours(args, rank, world, local_rank):
 def run_reference(args, rank, world):
     """The reference's own kernels (kernels/*.cl compiled for the host CPU
     into oracle/_ref, run by OpenMP over all host cores) in stores its own
-    builder made, on the same workload: `steps` substeps of every scene.
-    Neither the sph package nor the CUDA library is loaded."""
+    builder made, on the same workload: `warmup` untimed substeps, then
+    `steps` timed ones, of every scene.  Neither the sph package nor the
+    CUDA library is loaded."""
     if rank != 0:
         return None
     scs = cpu_workload(args.workload, args.seed, standalone=True)
@@ -993,7 +996,7 @@ def run_reference(args, rank, world):
     el = 0.0
     kinds = set()
     for x in scs:
-        w, e, kind = cpu_sample(x, x.material, args.steps, nthreads, reference=True)
+        w, e, kind = cpu_sample(x, x.material, args.steps, nthreads, reference=True, warmup=args.warmup)
         work += w
         el += e
         kinds.add(kind)
