@@ -383,3 +383,40 @@ def test_oracle_matches_compiled_reference_live_fluid_edges():
             assert np.array_equal(orc.a[k], rs.view(k).reshape(-1)), (k, case)
         rs.free()
         free_data_cpu(ps)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_oracle_scene_builders_live(prec):
+    """populate_position_cuboid and rotate_particles (common.cl:533-604) on
+    seeded random cuboids (8 to 216 points against pnum 120, so below and
+    above it; corners in any order) and angles, in the oracle and in the
+    reference's compiled kernels: positions and n equal bit for bit."""
+    from oracle import ref
+    if not ref.available():
+        pytest.skip("oracle/_ref not built on this machine")
+    rng = np.random.default_rng(51 + (prec == "f64"))
+    sc = scenes.wcsph_block(6, 5, 4, jitter=0.0, seed=0, walls=False)  # pnum 120
+    if prec == "f64":
+        sc = sc.to_double()
+    for case in range(12):
+        ps, v = host_store(sc)
+        orc = OracleScene({k: np.array(a) for k, a in v.items()}, prec)
+        rs = ref.RefStore(sc.spec)
+        rs.view("position")[...] = v["position"]
+        free_data_cpu(ps)
+        orc.state.n = 0
+        rs.view("n")[...] = 0
+        c1 = rng.uniform(-1, 1, 3)
+        c2 = rng.uniform(-1, 1, 3)
+        # at least 2 points per axis: with 1 the reference divides 0 by 0
+        size = [int(x) for x in rng.integers(2, 7, 3)]
+        orc.populate_position_cuboid(c1, c2, size)
+        rs.populate_cuboid("fluid", prec, tuple(c1), tuple(c2), tuple(size))
+        assert orc.n == int(np.ravel(rs.view("n"))[0]), case
+        assert np.array_equal(orc.a["position"], rs.view("position")), case
+        for _ in range(2):
+            ang = rng.uniform(-4, 4, 3)
+            orc.rotate_particles(*ang)
+            rs.rotate("fluid", prec, tuple(ang), sc.n)
+            assert np.array_equal(orc.a["position"], rs.view("position")), case
+        rs.free()
