@@ -6,7 +6,8 @@ an exact FP64 one, and the store shape that uploads may not change.
   positions and n bit for bit after populate_position_cuboid (every
   operation rounded as in the source), positions within 1e-6 of their
   magnitude after each rotate_particles (cosf/sinf may differ from the host
-  libm's in the last bit; the products are rounded as in the source).
+  libm's in the last bit; the products are rounded as in the source); the
+  same against the oracle on seeded random cuboids and angles.
 - compute_rotations_and_strains: R of every soft particle within 1e-7 of
   the exact polar factor U V^T of the particle's own Apq (apq_temp, from
   an FP64 SVD), on a rotated and stretched lattice; body particles keep
@@ -49,6 +50,35 @@ def test_scene_builders_match_reference():
             assert max_rel(got, g[pre + "rotate%d/position" % a]) <= 1e-6, (c, a)
             # and the reference's FP64 run of the same calls
             assert max_rel(got, g["f64/cuboid%d/rotate%d/position" % (c, a)]) <= 1e-6, (c, a)
+        ps.close()
+
+
+def test_scene_builders_random_against_oracle():
+    """Seeded random cuboids (8 to 216 points against pnum 120, corners in
+    any order) and angles: the GPU's populate_position_cuboid equals the
+    oracle's bit for bit (positions and n), and each rotate_particles stays
+    within 1e-6 of it."""
+    sc = scenes.wcsph_block(6, 5, 4, jitter=0.0, seed=0, walls=False)
+    rng = np.random.default_rng(61)
+    for case in range(10):
+        ps = ParticleSystem(spec=sc.spec, kernel_files=scenes.FLUID_KERNELS)
+        ps.set_fields(n=0)
+        orc = oracle_of(ps, "f32", guards=0)
+        c1, c2 = rng.uniform(-1, 1, 3), rng.uniform(-1, 1, 3)
+        size = [int(x) for x in rng.integers(2, 7, 3)]
+        c1f, c2f = c1.astype(np.float32), c2.astype(np.float32)
+        bnd.populate_position_cuboid_device_opencl(ps.psdata_opencl, *[float(x) for x in c1f],
+                                                   *[float(x) for x in c2f], *size)
+        orc.populate_position_cuboid(c1f, c2f, size)
+        ps.sync_device_to_host()
+        assert int(ps.get_fields("n")[0][0]) == orc.n, case
+        assert np.array_equal(ps.get_fields("position")[0], orc.a["position"]), case
+        for _ in range(2):
+            ang = rng.uniform(-4, 4, 3).astype(np.float32)
+            bnd.rotate_particles_device_opencl(ps.psdata_opencl, *[float(x) for x in ang])
+            orc.rotate_particles(*ang)
+            ps.sync_device_to_host()
+            assert max_rel(ps.get_fields("position")[0], orc.a["position"]) <= 1e-6, case
         ps.close()
 
 
