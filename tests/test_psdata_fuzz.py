@@ -259,3 +259,14 @@ def test_display_psdata_prints_what_the_reference_prints():
         finally:
             bnd.free_psdata(ctypes.byref(ps))
             rs.free()
+
+
+def test_specifications_the_reference_cannot_build_are_errors():
+    """Where the reference's builder divides by zero (a grid narrower than
+    one cell in some axis: gridcount's first dimension is 0, and its
+    alignment divides by it), this builder reports an error instead."""
+    spec = ("pnum | 1 | unsigned int | 4\nsmoothingradius | 1 | float | 0.5\n"
+            "gridbounds | 2, 3 | float | 0, 0.2, 0, 1, 0, 1\nposition | 3, pnum | float\n")
+    ps = bnd.psdata()
+    with pytest.raises(bnd.SphError):
+        bnd.build_psdata_from_string(ctypes.byref(ps), spec)
