@@ -262,11 +262,17 @@ def test_display_psdata_prints_what_the_reference_prints():
 
 
 def test_specifications_the_reference_cannot_build_are_errors():
-    """Where the reference's builder divides by zero (a grid narrower than
-    one cell in some axis: gridcount's first dimension is 0, and its
-    alignment divides by it), this builder reports an error instead."""
+    """Where the reference's builder divides by zero (a multi-dimensional
+    field whose first dimension is 0, e.g. gridcount of a grid narrower
+    than one cell along x: its alignment divides by it), this builder
+    reports an error instead."""
     spec = ("pnum | 1 | unsigned int | 4\nsmoothingradius | 1 | float | 0.5\n"
             "gridbounds | 2, 3 | float | 0, 0.2, 0, 1, 0, 1\nposition | 3, pnum | float\n")
     ps = bnd.psdata()
+    with pytest.raises(bnd.SphError):
+        bnd.build_psdata_from_string(ctypes.byref(ps), spec)
+    # a multi-dimensional field whose first dimension names no field (0)
+    spec = ("pnum | 1 | unsigned int | 4\nsmoothingradius | 1 | float | 0.1\n"
+            "gridbounds | 2, 3 | float | 0, 1, 0, 1, 0, 1\nx | nosuch, pnum | float\n")
     with pytest.raises(bnd.SphError):
         bnd.build_psdata_from_string(ctypes.byref(ps), spec)
