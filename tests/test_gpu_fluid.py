@@ -59,6 +59,35 @@ def test_bins_outside_grid_and_crowded_cells():
     ps.close()
 
 
+def test_substep_on_crowded_outside_and_ragged_scene_against_oracle():
+    """One fused substep of a scene that holds a crowded cluster (stencil
+    rows of more than 64 candidates: the scan path), particles clamped into
+    edge cells from below and above the grid, and n < pnum, against the
+    oracle: cell tables and neighbour counts exact, densities within 1e-5,
+    velocities within 1e-5 and positions within 1e-6 (relative L2)."""
+    sc = scenes.wcsph_block(10, 10, 10, jitter=1e-4, seed=17, walls=False)
+    pos = sc.init["position"].copy()
+    rng = np.random.default_rng(8)
+    pos[:30] = rng.uniform(-0.3, -0.01, size=(30, 3))            # below the box
+    pos[30:130] = 0.105 + rng.uniform(0, 0.006, size=(100, 3))   # 100 within 0.006 m
+    pos[130:160] = rng.uniform(0.45, 0.9, size=(30, 3))          # above the box
+    n = sc.n - 37
+    ps = sc.system()
+    ps.set_fields(position=pos, n=n)
+    orc = oracle_of(ps)
+    ps.update_fused(1)
+    orc.run("fluid", 1)
+    ps.sync_device_to_host()
+    for f in ("gridcell", "cellparticles", "num_neighbours"):
+        assert np.array_equal(ps.get_fields(f)[0][:n], orc.a[f][:n]), f
+    assert orc.a["num_neighbours"][30:130].min() > 64
+    assert max_rel(ps.get_fields("density")[0][:n], orc.a["density"][:n]) <= 1e-5
+    assert rel_err(ps.get_fields("velocity")[0][:n], orc.a["velocity"][:n]) <= 1e-5
+    assert rel_err(ps.get_fields("position")[0][:n], orc.a["position"][:n]) <= 1e-6
+    assert ps.status() & 2
+    ps.close()
+
+
 @pytest.mark.parametrize("n_active", [0, 1, 777])
 def test_bins_ragged_n(n_active):
     sc = scenes.wcsph_block(10, 10, 10, jitter=1e-4, seed=9)
