@@ -276,3 +276,43 @@ def test_specifications_the_reference_cannot_build_are_errors():
             "gridbounds | 2, 3 | float | 0, 1, 0, 1, 0, 1\nx | nosuch, pnum | float\n")
     with pytest.raises(bnd.SphError):
         bnd.build_psdata_from_string(ctypes.byref(ps), spec)
+
+
+def test_host_fields_equal_the_reference():
+    """create_host_field_psdata / get_host_field_psdata
+    (particle_system.c:116-164) on seeded random sequences of names
+    (repeats included) and sizes: the same indices, names and sizes."""
+    lib = ref.psdata_lib()
+    lib.create_host_field_psdata.argtypes = [ctypes.POINTER(ref.psdata), ctypes.c_char_p, ctypes.c_void_p,
+                                             ctypes.c_uint]
+    lib.create_host_field_psdata.restype = ctypes.c_int
+    lib.get_host_field_psdata.argtypes = [ctypes.POINTER(ref.psdata), ctypes.c_char_p]
+    lib.get_host_field_psdata.restype = ctypes.c_int
+    libc = ctypes.CDLL(None)
+    libc.malloc.restype = ctypes.c_void_p
+    libc.malloc.argtypes = [ctypes.c_size_t]
+    rng = np.random.default_rng(88)
+    for case in range(20):
+        spec = random_spec(rng)
+        rs = ref.RefStore(spec)
+        ps = bnd.psdata()
+        bnd.build_psdata_from_string(ctypes.byref(ps), spec)
+        try:
+            pool = ["h%d" % k for k in range(5)] + ["position_mex", ""]
+            for _ in range(int(rng.integers(1, 12))):
+                name = pool[int(rng.integers(len(pool)))]
+                size = int(rng.integers(0, 64))
+                # both stores own (and free) their buffers
+                a = lib.create_host_field_psdata(ctypes.byref(rs.ps), name.encode(), libc.malloc(max(size, 1)), size)
+                b = bnd.create_host_field_psdata(ctypes.byref(ps), name, libc.malloc(max(size, 1)), size)
+                assert a == b, (case, name)
+                for q in pool + ["nosuch"]:
+                    assert (bnd.get_host_field_psdata(ctypes.byref(ps), q)
+                            == lib.get_host_field_psdata(ctypes.byref(rs.ps), q.encode())), (case, q)
+            assert ps.num_host_fields == rs.ps.num_host_fields
+            sizes = ctypes.cast(rs.ps.host_data_size, ctypes.POINTER(ctypes.c_uint))
+            assert [ps.host_data_size[i] for i in range(ps.num_host_fields)] == \
+                [sizes[i] for i in range(rs.ps.num_host_fields)]
+        finally:
+            bnd.free_psdata(ctypes.byref(ps))
+            rs.free()
